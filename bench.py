@@ -1,0 +1,386 @@
+"""Benchmark: MLUPS of the fused D2Q9 collide+stream step and its HBM roofline.
+
+Workload (one GPU): 4096 x 2048 lattice, channel edges (equilibrium inlet at
+ux = 0.08, zero-gradient outflow, periodic top/bottom), tau = 0.55, 200 seeded
+solid circles with radii uniform in 4..32 cells, none within 64 cells of the
+inlet.  Synthetic geometry from a fixed seed; no dataset is involved.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one fused launch over the whole grid.  `value` times K steps with the
+state resident in HBM (CUDA events on the engine's stream).  `e2e` runs the
+same K steps through the public API with host buffers: populations and mask
+uploaded from pinned host memory, K steps, rho / ux / uy read back, all inside
+the timed region.  The grid (570 MB in f32) is larger than L2, so no flush is
+needed between steps.  With --gpus N > 1 (torchrun) every rank advances its own
+replica of the grid: weak scaling, no collective on the data path.
+
+--impl reference times the reference's own step arithmetic on the host cores:
+its WGSL shaders translated to C++ (oracle/_ref) when built, else the oracle
+restatement, on a bounded sample of the same grid.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "MLUPS & % of HBM roofline: FP32 vs FP16-store vs learned closure at equal error"
+NX, NY, TAU, UX, NCIRC, SEED = 4096, 2048, 0.55, 0.08, 200, 1
+BYTES_PER_CELL = {"f32": 72.0, "f16": 36.0, "bf16": 36.0, "f64": 144.0}  # algorithmic, per update
+FALLBACK_HBM_GBS = 6800.0
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return FALLBACK_HBM_GBS, "fallback"
+
+
+def ncu_traffic(kernel_key):
+    """DRAM bytes per launch from the committed ncu summary, if present."""
+    p = os.path.join(HERE, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    return d.get(kernel_key)
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload_mask():
+    from lbm_gb300 import geometry
+    return geometry.random_circles(NX, NY, NCIRC, 4, 32, seed=SEED, inlet_clearance=64)
+
+
+def time_storage(lbm, torch, storage, mask, steps, warmup):
+    """Device-resident MLUPS of one storage format; returns (ms_per_step, launches)."""
+    lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, storage)
+    stream = torch.cuda.current_stream()
+    lat.set_stream(stream.cuda_stream)
+    lat.set_inlet_velocity(UX)
+    lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+    lat.draw_mask(mask)
+    lat.iterate(warmup)
+    lat.synchronize()
+    l0 = lat.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    lat.iterate(steps)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    lat.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    launches = lat.launch_count() - l0
+    lat.close()
+    return ms, launches
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+    import lbm_gb300 as lbm
+    from lbm_gb300 import build as B
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    if rank == 0 or not os.path.exists(B.LIB):
+        B.build()
+    if world > 1:
+        dist.barrier()
+    lbm.load_library()
+    mask = workload_mask()
+    n = NX * NY
+    hbm_peak, peak_kind = peaks()
+
+    # --- value: K steps with the state resident, f32 ---------------------------
+    lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
+    stream = torch.cuda.current_stream()
+    lat.set_stream(stream.cuda_stream)
+    lat.set_inlet_velocity(UX)
+    lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+    lat.draw_mask(mask)
+    lat.iterate(args.warmup)
+    lat.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = lat.launch_count()
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        e0.record(stream)
+        lat.iterate(args.steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    lat.synchronize()
+    launches = lat.launch_count() - l0
+    dev_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([dev_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        dev_ms = float(t.item())
+    ms_step = dev_ms / args.steps
+    mlups = world * n * args.steps / (dev_ms * 1e-3) / 1e6
+    kernel_ms = ms_step  # one launch per step
+    achieved = BYTES_PER_CELL["f32"] * n / (kernel_ms * 1e-3) / 1e9
+    lat.close()
+
+    # --- e2e: the public API with pinned host buffers, copies inside the timing --
+    pops_h = torch.empty(9 * n, dtype=torch.float32, pin_memory=True)
+    mask_h = torch.from_numpy(mask.reshape(-1).copy()).pin_memory()
+    outs = [torch.empty(n, dtype=torch.float32, pin_memory=True) for _ in range(3)]
+    src = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
+    src.set_inlet_velocity(UX)
+    src.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+    pops_h.numpy()[:] = src.populations().reshape(-1)
+    src.close()
+    lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
+    lat.set_inlet_velocity(UX)
+    L = lbm.load_library()
+    import ctypes
+
+    def e2e_once(k):
+        lbm._check(L.lbm_write_populations(lat.handle, ctypes.c_void_p(pops_h.data_ptr())))
+        lbm._check(L.lbm_set_mask(lat.handle, ctypes.c_void_p(mask_h.data_ptr())))
+        lbm._check(L.lbm_step(lat.handle, k))
+        for o, f in zip(outs, (0, 3, 4)):  # rho, ux, uy
+            lbm._check(L.lbm_read_field(lat.handle, f, ctypes.c_void_p(o.data_ptr())))
+
+    e2e_once(max(args.warmup, 1))
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_once(args.steps)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    lat.close()
+    e2e_mlups = world * n * args.steps / e2e_s / 1e6
+    h2d = (9 * n * 4 + n) / args.steps
+    d2h = 3 * n * 4 / args.steps
+
+    # --- storage variants (same workload) -----------------------------------------
+    variants = {}
+    if not args.no_variants:
+        for name, st in (("f16", lbm.F16), ("bf16", lbm.BF16)):
+            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup)
+            gbs = BYTES_PER_CELL[name] * n / (vms * 1e-3) / 1e9
+            variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
+                              "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
+
+    if rank != 0:
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+
+    cpu = None if args.no_cpu_baseline else cpu_baseline(mask, budget_s=args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": round(mlups, 1), "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded circles, equilibrium init +-1e-4 noise)",
+        "config": {"workload": "D2Q9 BGK channel 4096x2048, 200 circles r 4-32, tau 0.55, ux 0.08",
+                   "nx": NX, "ny": NY, "cells": n, "solid_fraction": round(float(mask.mean()), 4),
+                   "storage": "f32", "l2": "state 570 MB > 129 MB L2: no flush",
+                   "parallelism": "replicas x%d" % world},
+        "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h),
+                "what": "write_populations + set_mask from pinned host, K steps, read rho/ux/uy to pinned host"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                     "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic("k_step_f32_channel"),
+                     "peak_source": peak_kind, "bytes_per_cell": BYTES_PER_CELL["f32"],
+                     "kernel": "lbm::k_step<StF32, EDGE_CHANNEL>"},
+        "variants": variants,
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "wall_s_timed": round(wall, 4),
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+def cpu_baseline(mask, budget_s=12.0, threads=None):
+    """The reference's step arithmetic on the host cores, on a bounded number
+    of steps of the same grid and barrier layout (its own edge semantics)."""
+    import numpy as np
+    from oracle import pyoracle as P
+    have_ref = P.build(ref=True) or P.ref_available()
+    threads = threads or os.cpu_count() or 1
+    n = NX * NY
+    o = P.Oracle(NX, NY, 1.0 / TAU, P.EDGE_REF, P.P_F32, threads=threads)
+    o.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+    m = mask.copy()
+    m[0] = 1
+    m[-1] = 1
+    if have_ref:
+        pops, _, _, _ = o.state()
+        sim = P.RefShaders(NX, NY, np.float32(1.0 / TAU), threads=threads)
+        sim.put_state(pops.astype(np.float32))
+        sim.set_barrier(m)
+        step, kind = sim.iterate, "reference"
+    else:
+        o.set_mask(m)
+        step, kind = o.step, "port"
+    step(1)  # warm-up
+    done, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and done < 200:
+        step(1)
+        done += 1
+    dt = time.perf_counter() - t0
+    return {"value": round(n * done / dt / 1e6, 2), "unit": "MLUPS", "cores": threads, "kind": kind,
+            "sample": "%d steps of the %dx%d grid (%s, 8 passes per step, f32, OpenMP %d threads)" % (
+                done, NX, NY, "reference WGSL translated to C++" if kind == "reference" else "oracle port",
+                threads)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    mask = workload_mask()
+    from oracle import pyoracle as P
+    import numpy as np
+    have_ref = P.build(ref=True) or P.ref_available()
+    threads = os.cpu_count() or 1
+    n = NX * NY
+    o = P.Oracle(NX, NY, 1.0 / TAU, P.EDGE_REF, P.P_F32, threads=threads)
+    o.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+    m = mask.copy()
+    m[0] = 1
+    m[-1] = 1
+    if have_ref:
+        pops, _, _, _ = o.state()
+        sim = P.RefShaders(NX, NY, np.float32(1.0 / TAU), threads=threads)
+        sim.put_state(pops.astype(np.float32))
+        sim.set_barrier(m)
+        step, kind = sim.iterate, "reference"
+    else:
+        o.set_mask(m)
+        step, kind = o.step, "port"
+    tw = time.perf_counter()
+    for _ in range(args.warmup):
+        step(1)
+    per = (time.perf_counter() - tw) / max(args.warmup, 1)
+    # each step is one full-grid update; the count is bounded so the run ends in ~2 minutes
+    steps = max(3, min(args.steps, int(120.0 / max(per, 1e-6))))
+    args.steps = steps
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step(1)
+    dt = time.perf_counter() - t0
+    mlups = n * steps / dt / 1e6
+    sample = "%d steps of the %dx%d grid, %s, f32, OpenMP %d threads" % (
+        args.steps, NX, NY, "reference WGSL shaders translated to C++ (8 passes per step)" if kind == "reference"
+        else "oracle port", threads)
+    line = {"impl": "reference", "metric": METRIC, "value": round(mlups, 2), "unit": "MLUPS", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded circles)",
+            "config": {"workload": "D2Q9 BGK channel 4096x2048, 200 circles r 4-32, tau 0.55, ux 0.08",
+                       "nx": NX, "ny": NY, "cells": n, "edges": "reference (walls, linear wrap)"},
+            "cpu_baseline": {"value": round(mlups, 2), "unit": "MLUPS", "cores": threads, "kind": kind,
+                             "sample": sample},
+            "e2e": {"value": round(mlups, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

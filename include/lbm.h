@@ -1,0 +1,166 @@
+/*
+ * lbm.h -- C ABI of the GB300 D2Q9 lattice-Boltzmann engine (liblbm_gb300.so).
+ *
+ * Drop-in for the step path of the lbm-wgpu crate (PPLUSCHT/LBM): construct a
+ * grid, set and clear barrier cells, set inlet velocity and viscosity, step N
+ * times, read back rho / ux / uy / curl.  Every entry point below names the
+ * reference interface it replaces (paths relative to the reference tree).
+ *
+ * Conventions
+ *   - Every function returns an int status: LBM_OK (0) or an LBM_ERR_* code;
+ *     lbm_last_error() returns a thread-local message for the last failure.
+ *   - The caller owns every host array passed in or out; the library owns all
+ *     device memory of a simulation.  Host arrays are row-major, x fastest,
+ *     index = x + y * nx, row 0 first (the reference's index(), lbm.rs:1517).
+ *   - A handle is used by one host thread at a time.  Work is queued on the
+ *     handle's CUDA stream; functions that return data to the host
+ *     synchronise that stream, lbm_step does not (use lbm_synchronize).
+ *   - Population order is the reference's (set_equil, lbm.rs:632-640):
+ *     0 nw, 1 n, 2 ne, 3 w, 4 rest, 5 e, 6 sw, 7 s, 8 se; north is row - 1.
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lbm_sim lbm_sim;
+
+/* status codes */
+#define LBM_OK 0
+#define LBM_ERR_ARG 1      /* invalid argument */
+#define LBM_ERR_CUDA 2     /* CUDA runtime error (message has the CUDA error) */
+#define LBM_ERR_NOMEM 3    /* device or host allocation failed */
+#define LBM_ERR_STATE 4    /* non-finite density detected by the step kernel */
+
+/* edge modes */
+#define LBM_EDGE_REF 0     /* the reference: walls on rows 0 and ny-1, column 0 and
+                              the last row never streamed, linear-index neighbours */
+#define LBM_EDGE_CHANNEL 1 /* column 0 frozen equilibrium inlet at (1, u_in, 0),
+                              zero-gradient outflow at column nx-1, periodic top/bottom */
+
+/* population storage */
+#define LBM_STORE_F32 0
+#define LBM_STORE_F16 1    /* binary16 deviations f_i - w_i, f32 arithmetic */
+#define LBM_STORE_BF16 2   /* bfloat16 deviations f_i - w_i, f32 arithmetic */
+#define LBM_STORE_F64 3    /* f64 storage and arithmetic (oracle-grade runs) */
+
+/* readback fields (lbm_read_field) */
+#define LBM_FIELD_RHO 0        /* density */
+#define LBM_FIELD_JX 1         /* x momentum: the reference's "ux" summary (ux.wgsl:41) */
+#define LBM_FIELD_JY 2         /* y momentum (north positive): the reference's "uy" (uy.wgsl:41) */
+#define LBM_FIELD_UX 3         /* velocity jx / rho */
+#define LBM_FIELD_UY 4         /* velocity jy / rho */
+#define LBM_FIELD_CURL 5       /* curl.wgsl:49 on momenta, 10*(...)/rho; 0 in column 0
+                                  and the last row */
+#define LBM_FIELD_VORTICITY 6  /* central-difference dx(uy) - dy(ux) of velocities */
+#define LBM_FIELD_SPEED 7      /* |u| */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* lbm_last_error(void);
+
+/* Library version string. */
+const char* lbm_version(void);
+
+/* LBM::new (lbm-wgpu/src/lbm.rs:726): allocate an nx x ny grid on the
+ * current CUDA device with relaxation rate omega, barrier = init_barrier
+ * (lbm.rs:595-605) in LBM_EDGE_REF (no walls in LBM_EDGE_CHANNEL), state =
+ * set_equil(0.1, 0, 1) (lbm.rs:740).  nx, ny >= 3; ny <= 65535; nx * ny < 2^31. */
+int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage, lbm_sim** out);
+
+/* Drop of LBM: free all device memory of the handle. */
+int lbm_destroy(lbm_sim* sim);
+
+/* Dimensions and mode of a handle (any pointer may be NULL). */
+int lbm_get_info(const lbm_sim* sim, uint32_t* nx, uint32_t* ny, int* edge_mode, int* storage);
+
+/* Queue the handle's work on an external CUDA stream (a cudaStream_t passed as
+ * void*; NULL restores the handle's own stream). */
+int lbm_set_stream(lbm_sim* sim, void* cuda_stream);
+
+/* Launch shape of the step kernel: rows of cells each thread walks (default
+ * 8; no counterpart in the reference, whose dispatch is fixed at 256-wide
+ * 1-D workgroups, lbm.rs:102-106). */
+int lbm_set_tuning(lbm_sim* sim, int rows_per_thread);
+
+/* draw_shape / draw_barrier_updates (lbm.rs:1337-1356, barrier_draw.wgsl:13-17):
+ * npairs (location, value) pairs; value 1 sets a solid cell, any other value
+ * clears it; locations >= nx*ny clamp to the last cell (the shader's clamped
+ * store).  Pairs apply in order: the last pair for a cell wins. */
+int lbm_set_barrier(lbm_sim* sim, const uint32_t* idx_val_pairs, size_t npairs);
+
+/* reset_barrier (lbm.rs:1362-1365): the two wall rows in LBM_EDGE_REF, all
+ * fluid in LBM_EDGE_CHANNEL. */
+int lbm_reset_barrier(lbm_sim* sim);
+
+/* Whole-mask upload / download: one byte per cell, nonzero = solid (the
+ * reference uploads whole barrier buffers in reset_barrier, lbm.rs:1364). */
+int lbm_set_mask(lbm_sim* sim, const uint8_t* mask);
+int lbm_get_mask(lbm_sim* sim, uint8_t* mask);
+
+/* update_omega_buffer (lbm.rs:1358-1360). */
+int lbm_set_omega(lbm_sim* sim, float omega);
+
+/* WASMInteraction::update_viscosity + lib.rs:181-186: omega = 1/(3 nu + 0.5). */
+int lbm_set_viscosity(lbm_sim* sim, float nu);
+
+/* custom_speed (lbm.rs:1090-1102) when reset_field != 0: the whole field is
+ * re-initialised to set_equil(ux, 0, 1) and the step count restarts at 0.
+ * With reset_field == 0 only the inlet changes: in LBM_EDGE_CHANNEL the frozen
+ * inlet column, in LBM_EDGE_REF column 0 (its de-facto inlet). */
+int lbm_set_inlet_velocity(lbm_sim* sim, float ux, int reset_field);
+
+/* reset_to_equilibrium (lbm.rs:1076-1088): set_equil(0.1, 0, 1) everywhere. */
+int lbm_reset_to_equilibrium(lbm_sim* sim);
+
+/* set_equil (lbm.rs:611-643) per cell at (rho, ux + nx_i, uy + ny_i), where
+ * nx_i, ny_i are seeded uniform noise in [-noise_amp, noise_amp) from a
+ * splitmix64 hash of (seed, cell, component).  Step count restarts at 0. */
+int lbm_init_equilibrium(lbm_sim* sim, float rho, float ux, float uy, float noise_amp, uint64_t seed);
+
+/* single_cell (lbm.rs:1482-1515): rest state with population `direction` set
+ * to 4.0 at the reference's cell for that direction. */
+int lbm_single_cell(lbm_sim* sim, int direction);
+
+/* iterate (lbm.rs:1065-1068) without the draw: n fused collide+stream steps.
+ * The density / momentum buffers hold the moments of the last step's
+ * collision (the reference's density_bg after iterate). Asynchronous. */
+int lbm_step(lbm_sim* sim, uint32_t n);
+
+/* Wait for queued work; returns LBM_ERR_STATE if a step saw a non-finite density. */
+int lbm_synchronize(lbm_sim* sim);
+
+/* set_summary + calculate_summary (lbm.rs:1051-1063) with a real readback:
+ * nx*ny floats of LBM_FIELD_* into out. */
+int lbm_read_field(lbm_sim* sim, int field, float* out);
+
+/* Current populations (the reference's set compute_step%2 plus the rest plane
+ * "origin"): 9 * nx * ny values, plane-major, reference order. */
+int lbm_read_populations(lbm_sim* sim, float* out);
+int lbm_read_populations_f64(lbm_sim* sim, double* out);
+
+/* Upload populations (9 planes, reference order) to both buffer sets, as
+ * custom_speed / single_cell upload states (lbm.rs:1092-1095); the step
+ * count restarts at 0. */
+int lbm_write_populations(lbm_sim* sim, const float* in);
+int lbm_write_populations_f64(lbm_sim* sim, const double* in);
+
+/* get_compute_num (lbm.rs:1170-1172): steps since the last re-initialisation. */
+int lbm_step_count(const lbm_sim* sim, uint64_t* out);
+
+/* Kernels launched by this handle so far (instrumentation). */
+int lbm_launch_count(const lbm_sim* sim, uint64_t* out);
+
+/* FP64 sums over fluid cells of rho, jx, jy from the last step's moments
+ * (global mass and momentum; no counterpart in the reference). */
+int lbm_conservation(lbm_sim* sim, double out[3]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_H */

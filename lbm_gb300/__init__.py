@@ -1,0 +1,253 @@
+"""GB300 D2Q9 lattice-Boltzmann engine: Python host side over the C ABI.
+
+`Lattice` mirrors the simulation surface of the reference's engine
+(lbm-wgpu/src/lbm.rs, `impl LBM`) with the same names and argument meaning:
+
+    reference (lbm.rs)                     here
+    LBM::new(driver, omega, x, y)  :726    Lattice(x, y, omega, edge=..., storage=...)
+    draw_shape(driver, shape)      :1337   draw_points(pairs) / draw_mask(...)
+    reset_barrier(driver)          :1362   reset_barrier()
+    update_omega_buffer(driver, w) :1358   update_omega_buffer(w)
+    custom_speed(driver, ux)       :1090   custom_speed(ux)
+    reset_to_equilibrium(driver)   :1076   reset_to_equilibrium()
+    single_cell(driver, index)     :1502   single_cell(index)
+    iterate(driver, n)             :1065   iterate(n)  (compute part; returns nothing)
+    set_summary(stat) + draw       :1061   summary(stat) -> numpy array
+    get_compute_num()              :1170   get_compute_num()
+
+Errors raise `LBMError` with the library's message.  The compute path is the
+CUDA library liblbm_gb300.so; there is no CPU fallback: importing works
+without a GPU, but creating a Lattice needs the library and a CUDA device.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = ["Lattice", "LBMError", "load_library", "EDGE_REF", "EDGE_CHANNEL", "F32", "F16", "BF16", "F64",
+           "SummaryStat", "FIELD"]
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
+
+EDGE_REF, EDGE_CHANNEL = 0, 1
+F32, F16, BF16, F64 = 0, 1, 2, 3
+FIELD = {"rho": 0, "jx": 1, "jy": 2, "ux": 3, "uy": 4, "curl": 5, "vorticity": 6, "speed": 7}
+
+
+class SummaryStat:
+    """The reference's SummaryStat enum (lbm.rs:10-16): Curl, Ux, Uy, Rho, Speed."""
+    Curl, Ux, Uy, Rho, Speed = 0, 1, 2, 3, 4
+
+
+class LBMError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("lbm error %d: %s" % (code, msg))
+        self.code = code
+
+
+_lib = None
+
+# (name, restype, argtypes) of every entry point declared in include/lbm.h
+_P = ctypes.c_void_p
+_SIGS = [
+    ("lbm_last_error", ctypes.c_char_p, []),
+    ("lbm_version", ctypes.c_char_p, []),
+    ("lbm_create", ctypes.c_int, [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(_P)]),
+    ("lbm_destroy", ctypes.c_int, [_P]),
+    ("lbm_get_info", ctypes.c_int, [_P, _P, _P, _P, _P]),
+    ("lbm_set_stream", ctypes.c_int, [_P, _P]),
+    ("lbm_set_tuning", ctypes.c_int, [_P, ctypes.c_int]),
+    ("lbm_set_barrier", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    ("lbm_reset_barrier", ctypes.c_int, [_P]),
+    ("lbm_set_mask", ctypes.c_int, [_P, _P]),
+    ("lbm_get_mask", ctypes.c_int, [_P, _P]),
+    ("lbm_set_omega", ctypes.c_int, [_P, ctypes.c_float]),
+    ("lbm_set_viscosity", ctypes.c_int, [_P, ctypes.c_float]),
+    ("lbm_set_inlet_velocity", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
+    ("lbm_reset_to_equilibrium", ctypes.c_int, [_P]),
+    ("lbm_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                                            ctypes.c_uint64]),
+    ("lbm_single_cell", ctypes.c_int, [_P, ctypes.c_int]),
+    ("lbm_step", ctypes.c_int, [_P, ctypes.c_uint32]),
+    ("lbm_synchronize", ctypes.c_int, [_P]),
+    ("lbm_read_field", ctypes.c_int, [_P, ctypes.c_int, _P]),
+    ("lbm_read_populations", ctypes.c_int, [_P, _P]),
+    ("lbm_read_populations_f64", ctypes.c_int, [_P, _P]),
+    ("lbm_write_populations", ctypes.c_int, [_P, _P]),
+    ("lbm_write_populations_f64", ctypes.c_int, [_P, _P]),
+    ("lbm_step_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    ("lbm_launch_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
+    ("lbm_conservation", ctypes.c_int, [_P, _P]),
+]
+
+
+def load_library(path=None):
+    """Load liblbm_gb300.so (built by lbm_gb300/build.py) and declare its ABI."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError("%s is missing: build it with `python lbm_gb300/build.py` "
+                                "(or __graft_entry__.build())" % p)
+    L = ctypes.CDLL(p)
+    for name, res, args in _SIGS:
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise LBMError(rc, _lib.lbm_last_error().decode())
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+class Lattice:
+    """One nx x ny D2Q9 lattice on the current CUDA device."""
+
+    def __init__(self, x, y, omega=1.0 / (0.5 + 0.3), edge=EDGE_REF, storage=F32):
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.lbm_create(int(x), int(y), float(omega), int(edge), int(storage), ctypes.byref(h)))
+        self._h = h
+        self.x, self.y, self.edge, self.storage = int(x), int(y), int(edge), int(storage)
+        self.summary_stat = SummaryStat.Curl
+
+    # -- lifetime ---------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.lbm_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    # -- barrier ------------------------------------------------------------
+    def draw_points(self, pairs):
+        """draw_barrier_updates: (location, value) u32 pairs, value 1 = solid."""
+        p = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1)
+        if p.size % 2:
+            raise ValueError("pairs must have an even number of entries")
+        _check(_lib.lbm_set_barrier(self._h, _ptr(p), p.size // 2))
+
+    def draw_mask(self, mask):
+        """Upload a whole [y, x] mask (nonzero = solid)."""
+        m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        if m.size != self.x * self.y:
+            raise ValueError("mask has %d cells, lattice %d" % (m.size, self.x * self.y))
+        _check(_lib.lbm_set_mask(self._h, _ptr(m)))
+
+    def mask(self):
+        m = np.zeros(self.x * self.y, np.uint8)
+        _check(_lib.lbm_get_mask(self._h, _ptr(m)))
+        return m.reshape(self.y, self.x)
+
+    def reset_barrier(self):
+        _check(_lib.lbm_reset_barrier(self._h))
+
+    # -- parameters -------------------------------------------------------
+    def update_omega_buffer(self, omega):
+        _check(_lib.lbm_set_omega(self._h, float(omega)))
+
+    def update_viscosity(self, nu):
+        _check(_lib.lbm_set_viscosity(self._h, float(nu)))
+
+    def custom_speed(self, ux):
+        _check(_lib.lbm_set_inlet_velocity(self._h, float(ux), 1))
+
+    def set_inlet_velocity(self, ux, reset_field=False):
+        _check(_lib.lbm_set_inlet_velocity(self._h, float(ux), 1 if reset_field else 0))
+
+    def reset_to_equilibrium(self):
+        _check(_lib.lbm_reset_to_equilibrium(self._h))
+
+    def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
+        _check(_lib.lbm_init_equilibrium(self._h, rho, ux, uy, noise, seed))
+
+    def single_cell(self, index):
+        _check(_lib.lbm_single_cell(self._h, int(index)))
+
+    def set_tuning(self, rows_per_thread):
+        _check(_lib.lbm_set_tuning(self._h, int(rows_per_thread)))
+
+    def set_stream(self, stream_ptr):
+        _check(_lib.lbm_set_stream(self._h, ctypes.c_void_p(stream_ptr) if stream_ptr else None))
+
+    # -- stepping -----------------------------------------------------------
+    def iterate(self, n):
+        _check(_lib.lbm_step(self._h, int(n)))
+
+    def synchronize(self):
+        _check(_lib.lbm_synchronize(self._h))
+
+    def get_compute_num(self):
+        v = ctypes.c_uint64()
+        _check(_lib.lbm_step_count(self._h, ctypes.byref(v)))
+        return v.value
+
+    def launch_count(self):
+        v = ctypes.c_uint64()
+        _check(_lib.lbm_launch_count(self._h, ctypes.byref(v)))
+        return v.value
+
+    # -- readback -----------------------------------------------------------
+    def field(self, name):
+        code = FIELD[name] if isinstance(name, str) else int(name)
+        out = np.zeros(self.x * self.y, np.float32)
+        _check(_lib.lbm_read_field(self._h, code, _ptr(out)))
+        return out.reshape(self.y, self.x)
+
+    def set_summary(self, stat):
+        self.summary_stat = stat
+
+    def summary(self, stat=None):
+        """Raw values of a SummaryStat (momenta for Ux/Uy, like ux.wgsl:41 / uy.wgsl:41)."""
+        stat = self.summary_stat if stat is None else stat
+        name = {SummaryStat.Curl: "curl", SummaryStat.Ux: "jx", SummaryStat.Uy: "jy", SummaryStat.Rho: "rho",
+                SummaryStat.Speed: "speed"}[stat]
+        return self.field(name)
+
+    def populations(self, f64=False):
+        out = np.zeros(9 * self.x * self.y, np.float64 if f64 else np.float32)
+        fn = _lib.lbm_read_populations_f64 if f64 else _lib.lbm_read_populations
+        _check(fn(self._h, _ptr(out)))
+        return out.reshape(9, self.y, self.x)
+
+    def write_populations(self, pops):
+        a = np.asarray(pops)
+        if a.dtype == np.float64:
+            a = np.ascontiguousarray(a).reshape(-1)
+            fn = _lib.lbm_write_populations_f64
+        else:
+            a = np.ascontiguousarray(a, dtype=np.float32).reshape(-1)
+            fn = _lib.lbm_write_populations
+        if a.size != 9 * self.x * self.y:
+            raise ValueError("need 9*x*y values")
+        _check(fn(self._h, _ptr(a)))
+
+    def conservation(self):
+        out = np.zeros(3, np.float64)
+        _check(_lib.lbm_conservation(self._h, _ptr(out)))
+        return out

@@ -1,0 +1,585 @@
+// C ABI of the single-lattice engine (include/lbm.h): handle management,
+// the state machine of the fused representation, mask upkeep and readback.
+#include <cuda_runtime.h>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include <cstdarg>
+
+#include "../../include/lbm.h"
+#include "lbm_kernels.cuh"
+
+using namespace lbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+#define CK_LAUNCH()                                                                       \
+  do {                                                                                    \
+    cudaError_t e_ = cudaGetLastError();                                                  \
+    if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+  } while (0)
+
+constexpr int kBlockX = 128;
+constexpr int kReduceBlocks = 608;  // 4 x 152 SMs
+
+size_t store_bytes(int storage) {
+  switch (storage) {
+    case STORE_F32: return 4;
+    case STORE_F64: return 8;
+    default: return 2;
+  }
+}
+
+}  // namespace
+
+struct lbm_sim {
+  int device = 0;
+  int edge = 0, storage = 0;
+  float omega = 1.0f, u_in = 0.1f;
+  Layout L{};
+  size_t es = 4;   // bytes per stored population
+  size_t cs = 4;   // bytes of the arithmetic type (moments)
+  void* f[2] = {nullptr, nullptr};
+  void* rest = nullptr;
+  uint32_t* mask_d = nullptr;
+  void* mom = nullptr;  // rho, jx, jy planes
+  int* flag_d = nullptr;
+  double* partial_d = nullptr;  // reduction partials
+  float* staging_d = nullptr;   // readback staging (9 planes of f64 at most)
+  size_t staging_bytes = 0;
+  std::vector<uint8_t> mask_h;
+  std::vector<uint32_t> words_h;
+  cudaStream_t own_stream = nullptr, stream = nullptr;
+  int cur = 0;               // buffer holding the latest state
+  bool materialised = true;  // cur holds a pre-collision state
+  bool moments_valid = false;
+  uint64_t steps = 0, launches = 0;
+  int rows = 8;
+};
+
+namespace {
+
+void* mom_plane(lbm_sim* s, int k) { return (char*)s->mom + (size_t)k * s->L.ps * s->cs; }
+
+template <class F> int dispatch_storage(int storage, F&& f) {
+  switch (storage) {
+    case STORE_F32: return f(StF32{});
+    case STORE_F16: return f(StF16{});
+    case STORE_BF16: return f(StBF16{});
+    case STORE_F64: return f(StF64{});
+  }
+  return fail(LBM_ERR_ARG, "bad storage %d", storage);
+}
+
+void pack_words(lbm_sim* s, uint32_t y0, uint32_t y1) {
+  const int nx = s->L.nx, mw = s->L.mw;
+  for (uint32_t y = y0; y < y1; y++) {
+    uint32_t* row = s->words_h.data() + (size_t)y * mw;
+    std::fill(row, row + mw, 0u);
+    const uint8_t* m = s->mask_h.data() + (size_t)y * nx;
+    for (int x = 0; x < nx; x++)
+      if (m[x]) row[x >> 5] |= 1u << (x & 31);
+  }
+}
+
+int upload_words(lbm_sim* s, uint32_t y0, uint32_t y1) {
+  if (y1 <= y0) return LBM_OK;
+  const size_t off = (size_t)y0 * s->L.mw, cnt = (size_t)(y1 - y0) * s->L.mw;
+  CK(cudaMemcpyAsync(s->mask_d + off, s->words_h.data() + off, cnt * 4, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));  // words_h is pageable and reused
+  return LBM_OK;
+}
+
+void default_walls(lbm_sim* s) {
+  std::fill(s->mask_h.begin(), s->mask_h.end(), 0);
+  if (s->edge == EDGE_REF) {
+    const size_t nx = s->L.nx, ny = s->L.ny;
+    for (size_t x = 0; x < nx; x++) { s->mask_h[x] = 1; s->mask_h[x + (ny - 1) * nx] = 1; }
+  }
+}
+
+// Bring the reference's pre-collision state S_k into buffer `cur`.
+int materialise(lbm_sim* s) {
+  if (s->materialised) return LBM_OK;
+  const int dst = 1 - s->cur;
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using S = typename decltype(tag)::S;
+    if (s->edge == EDGE_REF)
+      k_materialise<S, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (S*)s->f[dst], s->mask_d);
+    else
+      k_materialise<S, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (S*)s->f[dst], s->mask_d);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  s->cur = dst;
+  s->materialised = true;
+  return LBM_OK;
+}
+
+int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64_t seed, int single,
+                long long single_cell) {
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    using C = typename St::C;
+    k_init<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)rho, (C)ux, (C)uy,
+                                                  (C)amp, seed, s->edge == EDGE_CHANNEL, (C)s->u_in, single,
+                                                  single_cell);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  s->cur = 0;
+  s->materialised = true;
+  s->moments_valid = false;
+  s->steps = 0;
+  return LBM_OK;
+}
+
+int check_sim(const lbm_sim* s) {
+  if (!s) return fail(LBM_ERR_ARG, "null handle");
+  return LBM_OK;
+}
+
+#define CHECK_SIM(s)                      \
+  do {                                    \
+    int rc_ = check_sim(s);               \
+    if (rc_) return rc_;                  \
+    CK(cudaSetDevice((s)->device));       \
+  } while (0)
+
+void release(lbm_sim* s) {
+  cudaFree(s->f[0]); cudaFree(s->f[1]); cudaFree(s->rest); cudaFree(s->mask_d); cudaFree(s->mom);
+  cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
+  if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+int compute_moments(lbm_sim* s) {
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    using C = typename St::C;
+    k_moments<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
+                                                     (C*)mom_plane(s, 0), (C*)mom_plane(s, 1), (C*)mom_plane(s, 2));
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  s->moments_valid = true;
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* lbm_last_error(void) { return g_err.c_str(); }
+const char* lbm_version(void) { return "lbm_gb300 0.1 (sm_103a)"; }
+
+int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage, lbm_sim** out) {
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  *out = nullptr;
+  if (nx < 3 || ny < 3) return fail(LBM_ERR_ARG, "grid %ux%u: both sides must be >= 3", nx, ny);
+  if ((uint64_t)nx * ny >= (1ull << 31) || ny > 65535)
+    return fail(LBM_ERR_ARG, "grid %ux%u too large (nx*ny < 2^31, ny <= 65535)", nx, ny);
+  if (edge_mode != EDGE_REF && edge_mode != EDGE_CHANNEL) return fail(LBM_ERR_ARG, "bad edge mode %d", edge_mode);
+  if (storage < STORE_F32 || storage > STORE_F64) return fail(LBM_ERR_ARG, "bad storage %d", storage);
+  lbm_sim* s = new lbm_sim();
+  CK(cudaGetDevice(&s->device));
+  s->edge = edge_mode;
+  s->storage = storage;
+  s->omega = omega;
+  s->es = store_bytes(storage);
+  s->cs = storage == STORE_F64 ? 8 : 4;
+  s->L.nx = (int)nx;
+  s->L.ny = (int)ny;
+  s->L.pitch = (int)((nx + 31) / 32 * 32);
+  s->L.mw = s->L.pitch / 32;
+  s->L.ps = ((long long)s->L.pitch * ny + 127) / 128 * 128;
+  const size_t plane = (size_t)s->L.ps * s->es;
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      release(s);
+      delete s;
+      return fail(LBM_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+    }
+    return LBM_OK;
+  };
+  int rc;
+  if ((rc = alloc(&s->f[0], 8 * plane))) return rc;
+  if ((rc = alloc(&s->f[1], 8 * plane))) return rc;
+  if ((rc = alloc(&s->rest, plane))) return rc;
+  if ((rc = alloc((void**)&s->mask_d, (size_t)s->L.mw * ny * 4))) return rc;
+  if ((rc = alloc(&s->mom, 3 * (size_t)s->L.ps * s->cs))) return rc;
+  if ((rc = alloc((void**)&s->flag_d, 4))) return rc;
+  if ((rc = alloc((void**)&s->partial_d, (size_t)kReduceBlocks * 3 * 8))) return rc;
+  s->staging_bytes = (size_t)9 * nx * ny * 8;
+  if ((rc = alloc((void**)&s->staging_d, s->staging_bytes))) return rc;
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    release(s);
+    delete s;
+    return fail(LBM_ERR_CUDA, "cudaStreamCreate failed");
+  }
+  s->stream = s->own_stream;
+  cudaMemsetAsync(s->flag_d, 0, 4, s->stream);
+  cudaMemsetAsync(s->mom, 0, 3 * (size_t)s->L.ps * s->cs, s->stream);
+  s->mask_h.assign((size_t)nx * ny, 0);
+  s->words_h.assign((size_t)s->L.mw * ny, 0);
+  default_walls(s);
+  pack_words(s, 0, ny);
+  if ((rc = upload_words(s, 0, ny)) || (rc = launch_init(s, 1.0, 0.1, 0.0, 0.0, 0, -1, -1))) {
+    release(s);
+    delete s;
+    return rc;
+  }
+  *out = s;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_sim* s) {
+  if (!s) return LBM_OK;
+  cudaSetDevice(s->device);
+  cudaStreamSynchronize(s->stream);
+  release(s);
+  delete s;
+  return LBM_OK;
+}
+
+int lbm_get_info(const lbm_sim* s, uint32_t* nx, uint32_t* ny, int* edge, int* storage) {
+  if (!s) return fail(LBM_ERR_ARG, "null handle");
+  if (nx) *nx = (uint32_t)s->L.nx;
+  if (ny) *ny = (uint32_t)s->L.ny;
+  if (edge) *edge = s->edge;
+  if (storage) *storage = s->storage;
+  return LBM_OK;
+}
+
+int lbm_set_stream(lbm_sim* s, void* stream) {
+  CHECK_SIM(s);
+  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  return LBM_OK;
+}
+
+int lbm_set_tuning(lbm_sim* s, int rows_per_thread) {
+  CHECK_SIM(s);
+  if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
+  s->rows = rows_per_thread;
+  return LBM_OK;
+}
+
+int lbm_set_barrier(lbm_sim* s, const uint32_t* pairs, size_t npairs) {
+  CHECK_SIM(s);
+  if (npairs && !pairs) return fail(LBM_ERR_ARG, "pairs is null");
+  if (npairs == 0) return LBM_OK;
+  int rc = materialise(s);
+  if (rc) return rc;
+  const size_t n = s->mask_h.size();
+  uint32_t ymin = UINT32_MAX, ymax = 0;
+  for (size_t k = 0; k < npairs; k++) {
+    size_t loc = pairs[2 * k];
+    if (loc >= n) loc = n - 1;  // barrier_draw.wgsl:17 clamped store
+    s->mask_h[loc] = pairs[2 * k + 1] == 1u ? 1 : 0;
+    const uint32_t y = (uint32_t)(loc / s->L.nx);
+    ymin = std::min(ymin, y);
+    ymax = std::max(ymax, y);
+  }
+  pack_words(s, ymin, ymax + 1);
+  return upload_words(s, ymin, ymax + 1);
+}
+
+int lbm_reset_barrier(lbm_sim* s) {
+  CHECK_SIM(s);
+  int rc = materialise(s);
+  if (rc) return rc;
+  default_walls(s);
+  pack_words(s, 0, s->L.ny);
+  return upload_words(s, 0, s->L.ny);
+}
+
+int lbm_set_mask(lbm_sim* s, const uint8_t* mask) {
+  CHECK_SIM(s);
+  if (!mask) return fail(LBM_ERR_ARG, "mask is null");
+  int rc = materialise(s);
+  if (rc) return rc;
+  for (size_t i = 0; i < s->mask_h.size(); i++) s->mask_h[i] = mask[i] ? 1 : 0;
+  pack_words(s, 0, s->L.ny);
+  return upload_words(s, 0, s->L.ny);
+}
+
+int lbm_get_mask(lbm_sim* s, uint8_t* mask) {
+  if (!s || !mask) return fail(LBM_ERR_ARG, "null argument");
+  std::memcpy(mask, s->mask_h.data(), s->mask_h.size());
+  return LBM_OK;
+}
+
+int lbm_set_omega(lbm_sim* s, float omega) {
+  if (!s) return fail(LBM_ERR_ARG, "null handle");
+  if (!(omega > 0.0f && omega < 2.0f)) return fail(LBM_ERR_ARG, "omega %g outside (0, 2)", (double)omega);
+  s->omega = omega;
+  return LBM_OK;
+}
+
+int lbm_set_viscosity(lbm_sim* s, float nu) {
+  if (!(nu > 0.0f)) return fail(LBM_ERR_ARG, "viscosity %g must be > 0", (double)nu);
+  return lbm_set_omega(s, 1.0f / (3.0f * nu + 0.5f));  // lib.rs:183
+}
+
+int lbm_set_inlet_velocity(lbm_sim* s, float ux, int reset_field) {
+  CHECK_SIM(s);
+  s->u_in = ux;
+  if (reset_field) return launch_init(s, 1.0, ux, 0.0, 0.0, 0, -1, -1);
+  int rc = materialise(s);
+  if (rc) return rc;
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    using C = typename St::C;
+    k_inlet<St><<<(s->L.ny + 127) / 128, 128, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)ux);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  rc = dispatch_storage(s->storage, launch);
+  if (!rc) s->launches++;
+  return rc;
+}
+
+int lbm_reset_to_equilibrium(lbm_sim* s) {
+  CHECK_SIM(s);
+  return launch_init(s, 1.0, 0.1, 0.0, 0.0, 0, -1, -1);
+}
+
+int lbm_init_equilibrium(lbm_sim* s, float rho, float ux, float uy, float amp, uint64_t seed) {
+  CHECK_SIM(s);
+  if (!(amp >= 0.0f)) return fail(LBM_ERR_ARG, "noise amplitude %g", (double)amp);
+  return launch_init(s, rho, ux, uy, amp, seed, -1, -1);
+}
+
+int lbm_single_cell(lbm_sim* s, int dir) {
+  CHECK_SIM(s);
+  const long long X = s->L.nx, Y = s->L.ny;
+  long long x = 0, y = 0;
+  switch (dir) {  // set_single_cell, lbm.rs:1487-1496
+    case 0: x = X - 2; y = Y - 2; break;
+    case 1: x = 3 * X / 4; y = Y - 2; break;
+    case 2: x = X / 3; y = Y - 2; break;
+    case 3: x = X - 2; y = Y / 2; break;
+    case 4: x = 3 * X / 4; y = Y / 2; break;
+    case 5: x = X / 2; y = Y / 2; break;
+    case 6: x = X - 2; y = 1; break;
+    case 7: x = 3 * X / 4; y = 1; break;
+    case 8: x = X / 2; y = 1; break;
+    default: return launch_init(s, 1.0, 0.0, 0.0, 0.0, 0, -1, -1);
+  }
+  return launch_init(s, 1.0, 0.0, 0.0, 0.0, 0, dir, x + y * X);
+}
+
+int lbm_step(lbm_sim* s, uint32_t n) {
+  CHECK_SIM(s);
+  if (n == 0) return LBM_OK;
+  const int rows = s->rows;
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, (s->L.ny + rows - 1) / rows);
+  for (uint32_t k = 0; k < n; k++) {
+    const bool last = k + 1 == n;
+    const int src = s->cur;
+    const int dst = s->materialised ? s->cur : 1 - s->cur;
+    auto launch = [&](auto tag) -> int {
+      using St = decltype(tag);
+      using S = typename St::S;
+      using C = typename St::C;
+      StepArgs<S, C> a;
+      a.L = s->L;
+      a.src = (const S*)s->f[src];
+      a.dst = (S*)s->f[dst];
+      a.rest = (S*)s->rest;
+      a.mask = s->mask_d;
+      a.omega = (C)s->omega;
+      a.materialised = s->materialised ? 1 : 0;
+      a.rows = rows;
+      a.rho_out = last ? (C*)mom_plane(s, 0) : nullptr;
+      a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
+      a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
+      a.flag = s->flag_d;
+      if (s->edge == EDGE_REF) k_step<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(a);
+      else k_step<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(a);
+      CK_LAUNCH();
+      return LBM_OK;
+    };
+    int rc = dispatch_storage(s->storage, launch);
+    if (rc) return rc;
+    s->launches++;
+    s->cur = dst;
+    s->materialised = false;
+    s->steps++;
+  }
+  s->moments_valid = true;
+  return LBM_OK;
+}
+
+int lbm_synchronize(lbm_sim* s) {
+  CHECK_SIM(s);
+  CK(cudaStreamSynchronize(s->stream));
+  int flag = 0;
+  CK(cudaMemcpy(&flag, s->flag_d, 4, cudaMemcpyDeviceToHost));
+  if (flag & 1) return fail(LBM_ERR_STATE, "non-finite density detected");
+  return LBM_OK;
+}
+
+int lbm_read_field(lbm_sim* s, int field, float* out) {
+  CHECK_SIM(s);
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  if (field < 0 || field > 7) return fail(LBM_ERR_ARG, "bad field %d", field);
+  if (!s->moments_valid) {
+    // No step since the last initialisation: moments of the current state.
+    int rc = materialise(s);
+    if (rc) return rc;
+    rc = compute_moments(s);
+    if (rc) return rc;
+  }
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  float* tmp = s->staging_d;
+  if (s->storage == STORE_F64)
+    k_field<double><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const double*)mom_plane(s, 0),
+                                                    (const double*)mom_plane(s, 1), (const double*)mom_plane(s, 2), tmp);
+  else
+    k_field<float><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const float*)mom_plane(s, 0),
+                                                   (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), tmp);
+  CK_LAUNCH();
+  s->launches++;
+  CK(cudaMemcpyAsync(out, tmp, (size_t)s->L.nx * s->L.ny * 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+static int read_pops(lbm_sim* s, void* out, bool f64) {
+  CHECK_SIM(s);
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  int rc = materialise(s);
+  if (rc) return rc;
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    if (f64)
+      k_read_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
+                                                                (double*)s->staging_d);
+    else
+      k_read_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
+                                                               (float*)s->staging_d);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  CK(cudaMemcpyAsync(out, s->staging_d, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyDeviceToHost,
+                     s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_read_populations(lbm_sim* s, float* out) { return read_pops(s, out, false); }
+int lbm_read_populations_f64(lbm_sim* s, double* out) { return read_pops(s, out, true); }
+
+static int write_pops(lbm_sim* s, const void* in, bool f64) {
+  CHECK_SIM(s);
+  if (!in) return fail(LBM_ERR_ARG, "in is null");
+  CK(cudaMemcpyAsync(s->staging_d, in, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyHostToDevice,
+                     s->stream));
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    if (f64)
+      k_write_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
+                                                                 (const double*)s->staging_d);
+    else
+      k_write_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
+                                                                (const float*)s->staging_d);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  CK(cudaStreamSynchronize(s->stream));
+  s->cur = 0;
+  s->materialised = true;
+  s->moments_valid = false;
+  s->steps = 0;
+  return LBM_OK;
+}
+
+int lbm_write_populations(lbm_sim* s, const float* in) { return write_pops(s, in, false); }
+int lbm_write_populations_f64(lbm_sim* s, const double* in) { return write_pops(s, in, true); }
+
+int lbm_conservation(lbm_sim* s, double out[3]) {
+  CHECK_SIM(s);
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  if (!s->moments_valid) {
+    int rc = materialise(s);
+    if (rc) return rc;
+    rc = compute_moments(s);
+    if (rc) return rc;
+  }
+  if (s->storage == STORE_F64)
+    k_conservation_partial<double><<<kReduceBlocks, 256, 0, s->stream>>>(
+        s->L, s->mask_d, (const double*)mom_plane(s, 0), (const double*)mom_plane(s, 1),
+        (const double*)mom_plane(s, 2), s->partial_d);
+  else
+    k_conservation_partial<float><<<kReduceBlocks, 256, 0, s->stream>>>(
+        s->L, s->mask_d, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1),
+        (const float*)mom_plane(s, 2), s->partial_d);
+  CK_LAUNCH();
+  double* res = (double*)s->staging_d;
+  k_conservation_final<<<1, 256, 0, s->stream>>>(s->partial_d, kReduceBlocks, res);
+  CK_LAUNCH();
+  s->launches += 2;
+  CK(cudaMemcpyAsync(out, res, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_step_count(const lbm_sim* s, uint64_t* out) {
+  if (!s || !out) return fail(LBM_ERR_ARG, "null argument");
+  *out = s->steps;
+  return LBM_OK;
+}
+
+int lbm_launch_count(const lbm_sim* s, uint64_t* out) {
+  if (!s || !out) return fail(LBM_ERR_ARG, "null argument");
+  *out = s->launches;
+  return LBM_OK;
+}
+
+}  // extern "C"

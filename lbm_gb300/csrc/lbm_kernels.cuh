@@ -1,0 +1,385 @@
+// Kernels of the single-lattice D2Q9 engine.
+//
+// State representation.  The reference (lbm-wgpu/src/lbm.rs:1112-1134) runs,
+// per step k, an in-place collision of buffer set k%2 followed by a pull
+// stream into set (k+1)%2 that skips solid cells, column 0 and the last row.
+// Writing P_k for the post-collision state of step k, set (k+1)%2 therefore
+// holds pull(P_k) in streamed cells and P_{k-1} elsewhere.  The fused kernel
+// stores P_k in buffer k%2 and computes
+//     P_k(i) = C( streamed(i) ? pull(P_{k-1})(i) : P_{k-2}(i) )
+// reading P_{k-1} from buffer (k-1)%2 and P_{k-2}(i) from buffer k%2 at the
+// cell's own index before overwriting it: one read and one write of each
+// population per cell, 72 B/cell in f32.  A "materialised" buffer holds a
+// pre-collision state S_k instead (after initialisation or a state edit); the
+// next step then collides it in place without pulling.
+#pragma once
+#include "lbm_device.cuh"
+
+namespace lbm {
+
+template <class S, class C> struct StepArgs {
+  Layout L;
+  const S* __restrict__ src;  // 8 planes, P_{k-1}
+  S* __restrict__ dst;        // 8 planes, P_{k-2} (or a materialised S_k) -> P_k
+  S* __restrict__ rest;       // rest plane, updated in place
+  const uint32_t* __restrict__ mask;
+  C omega;
+  int materialised;  // 1: dst holds S_k, collide in place without pulling
+  int rows;          // rows per thread
+  C* __restrict__ rho_out;    // moments of this step's collision, or null
+  C* __restrict__ jx_out;
+  C* __restrict__ jy_out;
+  int* __restrict__ flag;     // bit 0: non-finite density seen
+};
+
+__device__ __forceinline__ uint32_t mask_bit(const uint32_t* __restrict__ mask, int mw, int x, int y) {
+  return (__ldg(mask + (long long)y * mw + (x >> 5)) >> (x & 31)) & 1u;
+}
+
+// Solid bits of columns x-1, x, x+1 of one row (bit 0, 1, 2) for an interior
+// cell: the word holding x plus, for lanes at a word edge, the neighbour word.
+__device__ __forceinline__ uint32_t row_triplet(const uint32_t* __restrict__ mrow, int x) {
+  const int b = x & 31, wx = x >> 5;
+  const uint32_t w = __ldg(mrow + wx);
+  const uint32_t left = b == 0 ? (__ldg(mrow + wx - 1) >> 31) : ((w >> (b - 1)) & 1u);
+  const uint32_t right = b == 31 ? (__ldg(mrow + wx + 1) & 1u) : ((w >> (b + 1)) & 1u);
+  return left | (((w >> b) & 1u) << 1) | (right << 2);
+}
+
+// Upstream cell of direction q at (x, y) for edge cells, by edge mode.
+// EDGE_REF: linear index i - cx - cy*nx in u32 arithmetic, clamped to the last
+// cell (e_w/n_s/ne_sw/se_nw_stream.wgsl index helpers, clamped access).
+// EDGE_CHANNEL: x clamped at the outflow column, y periodic.
+template <int EDGE> __device__ __forceinline__ void upstream_edge(const Layout& L, int x, int y, int q,
+                                                                  int& ux_, int& uy_) {
+  if (EDGE == EDGE_REF) {
+    const uint32_t n = (uint32_t)L.nx * (uint32_t)L.ny;
+    uint32_t j = (uint32_t)x + (uint32_t)y * (uint32_t)L.nx - (uint32_t)cx(q) - (uint32_t)(cy(q) * L.nx);
+    if (j >= n) j = n - 1;
+    ux_ = (int)(j % (uint32_t)L.nx);
+    uy_ = (int)(j / (uint32_t)L.nx);
+  } else {
+    int a = x - cx(q);
+    if (a > L.nx - 1) a = L.nx - 1;
+    if (a < 0) a = 0;
+    int b = y - cy(q);
+    if (b < 0) b += L.ny;
+    if (b >= L.ny) b -= L.ny;
+    ux_ = a;
+    uy_ = b;
+  }
+}
+
+// One cell of the fused step.  Loads the 9 pre-collision populations (pulled
+// from src with half-way bounce-back, or own from dst), computes the moments,
+// collides and stores.
+template <class St, int EDGE>
+__device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typename St::C>& a, int x, int y) {
+  using S = typename St::S;
+  using C = typename St::C;
+  const Layout& L = a.L;
+  const long long own = (long long)y * L.pitch + x;
+  const bool interior = x >= 1 && x <= L.nx - 2 && y >= 1 && y <= L.ny - 2;
+  const bool frozen = EDGE == EDGE_CHANNEL && x == 0;
+  C f[9];
+  bool streamed;
+  if (interior) {
+    const uint32_t* mrow = a.mask + (long long)y * L.mw;
+    const uint32_t t0 = row_triplet(mrow, x);
+    streamed = !a.materialised && !((t0 >> 1) & 1u);
+    if (streamed) {
+      const uint32_t tm = row_triplet(mrow - L.mw, x);  // row y-1
+      const uint32_t tp = row_triplet(mrow + L.mw, x);  // row y+1
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        if (q == 4) continue;
+        // upstream (x - cx, y - cy): row y+1 for cy=-1, y-1 for cy=+1
+        const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
+        const bool solid_up = (trip >> (1 - cx(q))) & 1u;
+        const S* p = solid_up ? a.src + (long long)slot(8 - q) * L.ps + own
+                              : a.src + (long long)slot(q) * L.ps + own - cx(q) - (long long)cy(q) * L.pitch;
+        f[q] = St::load(*p, q);
+      }
+    }
+  } else {
+    const bool own_solid = mask_bit(a.mask, L.mw, x, y);
+    streamed = !a.materialised && !own_solid && x != 0 && !(EDGE == EDGE_REF && y == L.ny - 1);
+    if (streamed) {
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        if (q == 4) continue;
+        int ux_, uy_;
+        upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
+        const bool solid_up = mask_bit(a.mask, L.mw, ux_, uy_);
+        const S* p = solid_up ? a.src + (long long)slot(8 - q) * L.ps + own
+                              : a.src + (long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_;
+        f[q] = St::load(*p, q);
+      }
+    }
+  }
+  if (!streamed) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      if (q == 4) continue;
+      f[q] = St::load(a.dst[(long long)slot(q) * L.ps + own], q);
+    }
+  }
+  f[4] = St::load(a.rest[own], 4);
+  C rho, jx, jy;
+  moments<C>(f, rho, jx, jy);
+  if (!(rho == rho) || rho - rho != C(0)) atomicOr(a.flag, 1);  // NaN or Inf
+  if (a.rho_out) {
+    a.rho_out[own] = rho;
+    a.jx_out[own] = jx;
+    a.jy_out[own] = jy;
+  }
+  if (frozen) return;  // channel inlet: fixed equilibrium, never collided
+  bgk<C>(f, rho, jx, jy, a.omega);
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    a.dst[(long long)slot(q) * L.ps + own] = St::store(f[q], q);
+  }
+  a.rest[own] = St::store(f[4], 4);
+}
+
+// Fused collide + stream.  Block = 128 threads along x (4 warps, each aligned
+// to a 32-cell mask word); each thread walks `rows` consecutive rows.
+template <class St, int EDGE>
+__global__ void __launch_bounds__(128) k_step(StepArgs<typename St::S, typename St::C> a) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= a.L.nx) return;
+  const int y0 = blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, a.L.ny);
+  for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);
+}
+
+// Stream-only pass: turns the fused representation into the reference's
+// pre-collision state S_k in dst (streamed cells pull from src with
+// bounce-back; the others keep their own dst value).  Raw words are copied.
+template <class S, int EDGE>
+__global__ void k_materialise(Layout L, const S* __restrict__ src, S* __restrict__ dst,
+                              const uint32_t* __restrict__ mask) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  const bool own_solid = mask_bit(mask, L.mw, x, y);
+  if (own_solid || x == 0 || (EDGE == EDGE_REF && y == L.ny - 1)) return;
+  S v[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    int ux_, uy_;
+    upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
+    const bool solid_up = mask_bit(mask, L.mw, ux_, uy_);
+    v[q] = solid_up ? src[(long long)slot(8 - q) * L.ps + own]
+                    : src[(long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_];
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    dst[(long long)slot(q) * L.ps + own] = v[q];
+  }
+}
+
+// set_equil per cell with optional seeded noise, into both sets and the rest
+// plane.  In channel mode column 0 gets the inlet equilibrium (1, u_in, 0).
+// single >= 0 additionally sets population `single` of cell single_cell to 4.
+template <class St>
+__global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
+                       typename St::C rho0, typename St::C ux0, typename St::C uy0, typename St::C amp,
+                       uint64_t seed, int channel, typename St::C u_in, int single, long long single_cell) {
+  using C = typename St::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  const uint64_t cell = (uint64_t)x + (uint64_t)y * (uint64_t)L.nx;
+  C ux = ux0, uy = uy0, rho = rho0;
+  if (amp != C(0)) {
+    ux = ux + amp * (C(2.0) * noise_u01<C>(seed, cell, 0) - C(1.0));
+    uy = uy + amp * (C(2.0) * noise_u01<C>(seed, cell, 1) - C(1.0));
+  }
+  if (channel && x == 0) { ux = u_in; uy = C(0); rho = C(1); }
+  C eq[9];
+  set_equil<C>(ux, uy, rho, eq);
+  if (single >= 0 && (long long)cell == single_cell) eq[single] = C(4.0);
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const auto v = St::store(eq[q], q);
+    if (q == 4) { rest[own] = v; continue; }
+    f0[(long long)slot(q) * L.ps + own] = v;
+    f1[(long long)slot(q) * L.ps + own] = v;
+  }
+}
+
+// Column-0 inlet rewrite: set_equil(u_in, 0, 1) into both sets and the rest plane.
+template <class St>
+__global__ void k_inlet(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
+                        typename St::C u_in) {
+  using C = typename St::C;
+  const int y = blockIdx.x * blockDim.x + threadIdx.x;
+  if (y >= L.ny) return;
+  const long long own = (long long)y * L.pitch;
+  C eq[9];
+  set_equil<C>(u_in, C(0), C(1), eq);
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const auto v = St::store(eq[q], q);
+    if (q == 4) { rest[own] = v; continue; }
+    f0[(long long)slot(q) * L.ps + own] = v;
+    f1[(long long)slot(q) * L.ps + own] = v;
+  }
+}
+
+// Populations of a materialised set (plus the rest plane) to a compact
+// plane-major array of 9 * nx * ny values in the reference order.
+template <class St, class O>
+__global__ void k_read_pops(Layout L, const typename St::S* f, const typename St::S* rest, O* out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  const long long n = (long long)L.nx * L.ny, c = (long long)y * L.nx + x;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const auto s = q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own];
+    out[q * n + c] = (O)St::load(s, q);
+  }
+}
+
+// Compact plane-major populations into both sets and the rest plane.
+template <class St, class I>
+__global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
+                             const I* in) {
+  using C = typename St::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  const long long n = (long long)L.nx * L.ny, c = (long long)y * L.nx + x;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    const auto v = St::store((C)in[q * n + c], q);
+    if (q == 4) { rest[own] = v; continue; }
+    f0[(long long)slot(q) * L.ps + own] = v;
+    f1[(long long)slot(q) * L.ps + own] = v;
+  }
+}
+
+// Moments of a materialised state (no collision), for readback before the
+// first step after an initialisation.
+template <class St>
+__global__ void k_moments(Layout L, const typename St::S* f, const typename St::S* rest, typename St::C* rho_out,
+                          typename St::C* jx_out, typename St::C* jy_out) {
+  using C = typename St::C;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  C v[9];
+#pragma unroll
+  for (int q = 0; q < 9; q++) v[q] = St::load(q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own], q);
+  moments<C>(v, rho_out[own], jx_out[own], jy_out[own]);
+}
+
+// Deterministic FP64 sums of rho, jx, jy over fluid cells: per-block partial
+// sums in a fixed order, then one block adds the partials in a fixed order.
+template <class C>
+__global__ void __launch_bounds__(256) k_conservation_partial(Layout L, const uint32_t* __restrict__ mask,
+                                                             const C* __restrict__ rho, const C* __restrict__ jx,
+                                                             const C* __restrict__ jy, double* __restrict__ partial) {
+  __shared__ double sh[3][256];
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+  const long long n = (long long)L.nx * L.ny;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / L.nx), x = (int)(c % L.nx);
+    if (mask_bit(mask, L.mw, x, y)) continue;
+    const long long own = (long long)y * L.pitch + x;
+    s0 += (double)rho[own];
+    s1 += (double)jx[own];
+    s2 += (double)jy[own];
+  }
+  sh[0][threadIdx.x] = s0;
+  sh[1][threadIdx.x] = s1;
+  sh[2][threadIdx.x] = s2;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 3; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) partial[blockIdx.x * 3 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void __launch_bounds__(256) k_conservation_final(const double* __restrict__ partial, int nblocks,
+                                                           double* __restrict__ out) {
+  __shared__ double sh[3][256];
+  for (int k = 0; k < 3; k++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) s += partial[b * 3 + k];
+    sh[k][threadIdx.x] = s;
+  }
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w)
+      for (int k = 0; k < 3; k++) sh[k][threadIdx.x] += sh[k][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x < 3) out[threadIdx.x] = sh[threadIdx.x][0];
+}
+
+// Readback fields from the moment planes (LBM_FIELD_* codes of lbm.h).
+template <class C>
+__global__ void k_field(Layout L, int edge, int field, const C* __restrict__ rho, const C* __restrict__ jx,
+                        const C* __restrict__ jy, float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+  const long long c = (long long)y * L.nx + x;
+  float v = 0.0f;
+  switch (field) {
+    case 0: v = (float)rho[own]; break;
+    case 1: v = (float)jx[own]; break;
+    case 2: v = (float)jy[own]; break;
+    case 3: v = (float)(jx[own] / rho[own]); break;
+    case 4: v = (float)(jy[own] / rho[own]); break;
+    case 5: {  // curl.wgsl:49 on linear indices, clamped
+      if (x == 0 || y >= L.ny - 1) break;
+      const uint32_t n = (uint32_t)L.nx * (uint32_t)L.ny, i = (uint32_t)c;
+      auto at = [&](uint32_t j) -> long long {
+        if (j >= n) j = n - 1;
+        return (long long)(j / (uint32_t)L.nx) * L.pitch + (j % (uint32_t)L.nx);
+      };
+      const C d = jy[at(i + 1u)] - jy[at(i - 1u)] - jx[at(i - (uint32_t)L.nx)] + jx[at(i + (uint32_t)L.nx)];
+      v = (float)(C(10.0) * d / rho[own]);
+      break;
+    }
+    case 6: {  // vorticity d(uy)/dx - d(ux)/dy_north = d(uy)/dx + d(ux)/drow
+      const int xl = max(x - 1, 0), xr = min(x + 1, L.nx - 1);
+      int yu = y - 1, yd = y + 1;
+      if (edge == EDGE_CHANNEL) { yu = (yu + L.ny) % L.ny; yd = yd % L.ny; }
+      else { yu = max(yu, 0); yd = min(yd, L.ny - 1); }
+      auto u = [&](const C* j, int xx, int yy) {
+        const long long k = (long long)yy * L.pitch + xx;
+        return j[k] / rho[k];
+      };
+      const C dx = (u(jy, xr, y) - u(jy, xl, y)) / C(xr - xl > 0 ? xr - xl : 1);
+      const int dyn = edge == EDGE_CHANNEL ? 2 : (yd - yu > 0 ? yd - yu : 1);
+      const C dy = (u(jx, x, yd) - u(jx, x, yu)) / C(dyn);
+      v = (float)(dx + dy);  // dy is along +row = -north
+      break;
+    }
+    case 7: {
+      const C ux = jx[own] / rho[own], uy = jy[own] / rho[own];
+      v = (float)sqrt(ux * ux + uy * uy);
+      break;
+    }
+    default: break;
+  }
+  out[c] = v;
+}
+
+}  // namespace lbm

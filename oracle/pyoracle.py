@@ -1,0 +1,256 @@
+"""ctypes wrappers around the CPU checkers.  TEST INFRASTRUCTURE ONLY.
+
+`Oracle` wraps liboracle.so (the C++ restatement, lbm_oracle.cpp) and `RefShaders`
+wraps _ref/libref.so (the reference's WGSL translated by wgsl2cpp.py and driven
+by ref_host.cpp).  Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline use them; the product package lbm_gb300 never imports this module.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libref.so")
+
+EDGE_REF, EDGE_CHANNEL = 0, 1
+P_F32, P_F16, P_BF16, P_F64 = 0, 1, 2, 3
+
+_c_u8p = ctypes.POINTER(ctypes.c_uint8)
+_c_u32p = ctypes.POINTER(ctypes.c_uint32)
+_c_f32p = ctypes.POINTER(ctypes.c_float)
+_c_f64p = ctypes.POINTER(ctypes.c_double)
+
+
+def build(ref=True):
+    """Compile liboracle.so and, when possible, the translated reference."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if ref:
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True, text=True)
+        return r.returncode == 0
+    return os.path.exists(REF_SO)
+
+
+def _ptr(a, t):
+    return a.ctypes.data_as(t) if a is not None else None
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(ref=False)
+        L = ctypes.CDLL(ORACLE_SO)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_set_omega.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_set_inlet.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_init_equilibrium.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                           ctypes.c_double, ctypes.c_uint64]
+        L.orc_single_cell.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_apply_inlet.argtypes = [ctypes.c_void_p]
+        L.orc_set_mask.argtypes = [ctypes.c_void_p, _c_u8p]
+        L.orc_get_mask.argtypes = [ctypes.c_void_p, _c_u8p]
+        L.orc_apply_barrier_pairs.argtypes = [ctypes.c_void_p, _c_u32p, ctypes.c_size_t]
+        L.orc_reset_barrier.argtypes = [ctypes.c_void_p]
+        L.orc_step.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.orc_step_count.restype = ctypes.c_uint64
+        L.orc_step_count.argtypes = [ctypes.c_void_p]
+        L.orc_get_state.argtypes = [ctypes.c_void_p, _c_f64p, _c_f64p, _c_f64p, _c_f64p]
+        L.orc_get_raw_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_put_state.argtypes = [ctypes.c_void_p, _c_f64p]
+        L.orc_curl_ref.argtypes = [ctypes.c_void_p, _c_f64p]
+        L.orc_float_to_half.restype = ctypes.c_uint16
+        L.orc_float_to_half.argtypes = [ctypes.c_float]
+        L.orc_half_to_float.restype = ctypes.c_float
+        L.orc_half_to_float.argtypes = [ctypes.c_uint16]
+        L.orc_float_to_bf16.restype = ctypes.c_uint16
+        L.orc_float_to_bf16.argtypes = [ctypes.c_float]
+        L.orc_noise_u01.restype = ctypes.c_double
+        L.orc_noise_u01.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
+        _lib = L
+    return _lib
+
+
+class Oracle:
+    """The C++ restatement of the reference step (8 passes, reference order)."""
+
+    def __init__(self, nx, ny, omega, edge=EDGE_REF, prec=P_F32, threads=None):
+        self.nx, self.ny, self.n = nx, ny, nx * ny
+        self.prec = prec
+        self.h = lib().orc_create(nx, ny, omega, edge, prec)
+        if not self.h:
+            raise ValueError("orc_create failed")
+        lib().orc_set_threads(self.h, threads or os.cpu_count() or 1)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_destroy(self.h)
+            self.h = None
+
+    def set_threads(self, t):
+        lib().orc_set_threads(self.h, t)
+
+    def set_omega(self, w):
+        lib().orc_set_omega(self.h, w)
+
+    def set_inlet(self, u, apply=True):
+        lib().orc_set_inlet(self.h, u)
+        if apply:
+            lib().orc_apply_inlet(self.h)
+
+    def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
+        lib().orc_init_equilibrium(self.h, rho, ux, uy, noise, seed)
+
+    def single_cell(self, d):
+        lib().orc_single_cell(self.h, d)
+
+    def set_mask(self, mask):
+        m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
+        assert m.size == self.n
+        lib().orc_set_mask(self.h, _ptr(m, _c_u8p))
+
+    def mask(self):
+        m = np.zeros(self.n, np.uint8)
+        lib().orc_get_mask(self.h, _ptr(m, _c_u8p))
+        return m.reshape(self.ny, self.nx)
+
+    def barrier_pairs(self, pairs):
+        p = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1)
+        lib().orc_apply_barrier_pairs(self.h, _ptr(p, _c_u32p), p.size // 2)
+
+    def reset_barrier(self):
+        lib().orc_reset_barrier(self.h)
+
+    def step(self, n=1):
+        lib().orc_step(self.h, n)
+
+    @property
+    def step_count(self):
+        return lib().orc_step_count(self.h)
+
+    def state(self):
+        """(pops[9, ny, nx], rho, jx, jy) as float64 arrays."""
+        p = np.zeros(9 * self.n)
+        r, jx, jy = np.zeros(self.n), np.zeros(self.n), np.zeros(self.n)
+        lib().orc_get_state(self.h, _ptr(p, _c_f64p), _ptr(r, _c_f64p), _ptr(jx, _c_f64p), _ptr(jy, _c_f64p))
+        s = (self.ny, self.nx)
+        return p.reshape(9, *s), r.reshape(s), jx.reshape(s), jy.reshape(s)
+
+    def raw_state(self):
+        """Raw storage words of the current set and the other set, [9, ny, nx] each."""
+        dt = {P_F32: np.float32, P_F64: np.float64, P_F16: np.uint16, P_BF16: np.uint16}[self.prec]
+        a = np.zeros(9 * self.n, dt)
+        b = np.zeros(9 * self.n, dt)
+        lib().orc_get_raw_state(self.h, a.ctypes.data_as(ctypes.c_void_p), b.ctypes.data_as(ctypes.c_void_p))
+        return a.reshape(9, self.ny, self.nx), b.reshape(9, self.ny, self.nx)
+
+    def put_state(self, pops9):
+        p = np.ascontiguousarray(pops9, dtype=np.float64).reshape(-1)
+        lib().orc_put_state(self.h, _ptr(p, _c_f64p))
+
+    def curl_ref(self):
+        out = np.zeros(self.n)
+        lib().orc_curl_ref(self.h, _ptr(out, _c_f64p))
+        return out.reshape(self.ny, self.nx)
+
+
+_ref = None
+
+
+def ref_available():
+    return os.path.exists(REF_SO)
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            raise FileNotFoundError(REF_SO)
+        L = ctypes.CDLL(REF_SO)
+        L.ref_create.restype = ctypes.c_void_p
+        L.ref_create.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_float]
+        L.ref_destroy.argtypes = [ctypes.c_void_p]
+        L.ref_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.ref_set_omega.argtypes = [ctypes.c_void_p, ctypes.c_float]
+        L.ref_put_state.argtypes = [ctypes.c_void_p, _c_f32p]
+        L.ref_set_barrier_buffer.argtypes = [ctypes.c_void_p, _c_u32p]
+        L.ref_get_barrier_buffer.argtypes = [ctypes.c_void_p, _c_u32p]
+        L.ref_draw_points.argtypes = [ctypes.c_void_p, _c_u32p, ctypes.c_uint32]
+        L.ref_iterate.argtypes = [ctypes.c_void_p, ctypes.c_uint64]
+        L.ref_compute_step.restype = ctypes.c_uint64
+        L.ref_compute_step.argtypes = [ctypes.c_void_p]
+        L.ref_get_state.argtypes = [ctypes.c_void_p, _c_f32p, _c_f32p, _c_f32p, _c_f32p]
+        L.ref_get_sets.argtypes = [ctypes.c_void_p, _c_f32p, _c_f32p]
+        L.ref_summary.argtypes = [ctypes.c_void_p, ctypes.c_int, _c_f32p]
+        _ref = L
+    return _ref
+
+
+class RefShaders:
+    """The reference's WGSL step, translated to C++ and run on the CPU (f32)."""
+
+    def __init__(self, nx, ny, omega, threads=None):
+        self.nx, self.ny, self.n = nx, ny, nx * ny
+        self.h = ref_lib().ref_create(nx, ny, omega)
+        ref_lib().ref_set_threads(self.h, threads or os.cpu_count() or 1)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            ref_lib().ref_destroy(self.h)
+            self.h = None
+
+    def set_threads(self, t):
+        ref_lib().ref_set_threads(self.h, t)
+
+    def set_omega(self, w):
+        ref_lib().ref_set_omega(self.h, w)
+
+    def put_state(self, pops9):
+        p = np.ascontiguousarray(pops9, dtype=np.float32).reshape(-1)
+        ref_lib().ref_put_state(self.h, _ptr(p, _c_f32p))
+
+    def set_barrier(self, mask):
+        b = np.ascontiguousarray(mask, dtype=np.uint32).reshape(-1)
+        ref_lib().ref_set_barrier_buffer(self.h, _ptr(b, _c_u32p))
+
+    def barrier(self):
+        b = np.zeros(self.n, np.uint32)
+        ref_lib().ref_get_barrier_buffer(self.h, _ptr(b, _c_u32p))
+        return b.reshape(self.ny, self.nx)
+
+    def draw_points(self, pairs):
+        p = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1)
+        ref_lib().ref_draw_points(self.h, _ptr(p, _c_u32p), p.size // 2)
+
+    def iterate(self, n):
+        ref_lib().ref_iterate(self.h, n)
+
+    @property
+    def step_count(self):
+        return ref_lib().ref_compute_step(self.h)
+
+    def state(self):
+        p = np.zeros(9 * self.n, np.float32)
+        r, jx, jy = (np.zeros(self.n, np.float32) for _ in range(3))
+        ref_lib().ref_get_state(self.h, _ptr(p, _c_f32p), _ptr(r, _c_f32p), _ptr(jx, _c_f32p), _ptr(jy, _c_f32p))
+        s = (self.ny, self.nx)
+        return p.reshape(9, *s), r.reshape(s), jx.reshape(s), jy.reshape(s)
+
+    def sets(self):
+        a = np.zeros(9 * self.n, np.float32)
+        b = np.zeros(9 * self.n, np.float32)
+        ref_lib().ref_get_sets(self.h, _ptr(a, _c_f32p), _ptr(b, _c_f32p))
+        return a.reshape(9, self.ny, self.nx), b.reshape(9, self.ny, self.nx)
+
+    def summary(self, stat):
+        out = np.zeros(self.n, np.float32)
+        ref_lib().ref_summary(self.h, stat, _ptr(out, _c_f32p))
+        return out.reshape(self.ny, self.nx)

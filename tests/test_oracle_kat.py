@@ -1,0 +1,139 @@
+"""Known-answer behaviours of the oracle (the reference's tutorial demos restated
+as deterministic tests) and its storage-format conversions."""
+import numpy as np
+import pytest
+
+STREAM_OMEGA = 1.0 / (3.0 * 1e7 + 0.5)  # update_viscosity(1e7), tutorial StreamDemo
+
+
+def test_pure_streaming_pulse_moves_one_row_per_step(oracle_mod):
+    """SingleNorth (lbm.rs:1488): the n pulse at (3X/4, Y-2) moves to row - 1 each step."""
+    P = oracle_mod
+    nx, ny = 40, 30
+    o = P.Oracle(nx, ny, STREAM_OMEGA, P.EDGE_REF, P.P_F64)
+    o.single_cell(1)
+    x0, y0 = 3 * nx // 4, ny - 2
+    for k in range(1, 8):
+        o.step(1)
+        pops, _, _, _ = o.state()
+        excess = pops[1] - np.median(pops[1])
+        y, x = np.unravel_index(np.argmax(excess), excess.shape)
+        # each step collides in place then pulls: after k steps it sits k rows up
+        assert (x, y) == (x0, y0 - k), k
+        assert excess.max() == pytest.approx(4.0 - 1.0 / 9.0, rel=1e-6)
+
+
+def test_bounce_back_reverses_pulse_at_wall(oracle_mod):
+    """NoSlipDemo (tutorial.ts:186-191): the ne pulse of SingleNorthEast at
+    (X/3, Y-2) travels (+1, -1) per step and comes back off the row-0 wall as sw."""
+    P = oracle_mod
+    nx, ny = 24, 8
+    o = P.Oracle(nx, ny, STREAM_OMEGA, P.EDGE_REF, P.P_F64)
+    o.single_cell(2)
+    x0, y0 = nx // 3, ny - 2
+    for k in range(1, ny - 2):
+        o.step(1)
+        pops, _, _, _ = o.state()
+        ex = pops[2] - np.median(pops[2])
+        assert np.unravel_index(np.argmax(ex), ex.shape) == (y0 - k, x0 + k)
+    o.step(1)  # the pulse at row 1 meets the wall: cell (x0+5, 1) takes it as sw
+    pops, _, _, _ = o.state()
+    ex = pops[6] - np.median(pops[6])
+    assert np.unravel_index(np.argmax(ex), ex.shape) == (1, x0 + ny - 3)
+    assert ex.max() == pytest.approx(4.0 - 1.0 / 36.0, rel=1e-6)
+    o.step(2)
+    pops, _, _, _ = o.state()
+    ex = pops[6] - np.median(pops[6])
+    assert np.unravel_index(np.argmax(ex), ex.shape) == (3, x0 + ny - 5)
+
+
+def test_north_pulse_bounces_into_south(oracle_mod):
+    P = oracle_mod
+    nx, ny = 12, 6
+    o = P.Oracle(nx, ny, STREAM_OMEGA, P.EDGE_REF, P.P_F64)
+    pops = np.zeros((9, ny, nx))
+    w = np.array([1 / 36, 1 / 9, 1 / 36, 1 / 9, 4 / 9, 1 / 9, 1 / 36, 1 / 9, 1 / 36])
+    pops[:] = w[:, None, None]
+    pops[1, 1, 5] += 2.0  # north pulse in row 1, under the wall row 0
+    o.put_state(pops)
+    o.step(1)
+    p, _, _, _ = o.state()
+    # the step collides in place then pulls: cell (5,1) pulls n from row 2 (rest
+    # level) and s from row 0, which is solid, so it takes its own n: now an s pulse.
+    assert p[7, 1, 5] - w[7] == pytest.approx(2.0, rel=1e-6)
+    assert abs(p[1, 1, 5] - w[1]) < 1e-6
+
+
+def test_equilibrium_fixed_point(oracle_mod):
+    P = oracle_mod
+    o = P.Oracle(32, 16, 1.0 / 0.6, P.EDGE_REF, P.P_F64)
+    o.init_equilibrium(1.0, 0.0, 0.0)
+    p0, _, _, _ = o.state()
+    o.step(50)
+    p, _, _, _ = o.state()
+    assert np.abs(p - p0).max() < 1e-14
+
+
+def test_closed_box_conserves_mass(oracle_mod):
+    P = oracle_mod
+    nx, ny = 30, 20
+    o = P.Oracle(nx, ny, 1.0 / 0.7, P.EDGE_REF, P.P_F64)
+    o.init_equilibrium(1.0, 0.05, 0.0, 1e-2, 4)
+    m = o.mask().copy()
+    m[:, 0] = 1
+    m[:, -1] = 1
+    m[8:12, 10:14] = 1
+    o.set_mask(m)
+    fluid = m == 0
+    o.step(1)
+    _, rho0, _, _ = o.state()
+    o.step(300)
+    _, rho, _, _ = o.state()
+    assert abs(rho[fluid].sum() - rho0[fluid].sum()) < 1e-10 * rho0[fluid].sum()
+
+
+def test_half_conversion_matches_numpy(oracle_mod):
+    L = oracle_mod.lib()
+    rng = np.random.default_rng(0)
+    vals = np.concatenate([rng.standard_normal(4000).astype(np.float32) * 0.05,
+                           rng.standard_normal(2000).astype(np.float32) * 1e-6,
+                           rng.standard_normal(500).astype(np.float32) * 1e5,
+                           np.array([0.0, -0.0, 6.1e-5, 5.96e-8, 2.98e-8, 65504.0, 65520.0, 1e-10], np.float32)])
+    for v in vals:
+        h = L.orc_float_to_half(float(v))
+        want = np.array([v], np.float32).astype(np.float16).view(np.uint16)[0]
+        assert h == want, (v, h, want)
+        assert L.orc_half_to_float(h) == np.float32(np.uint16(h).view(np.float16)), v
+
+
+def bf16_rne(v):
+    u = np.array([v], np.float32).view(np.uint32)[0].astype(np.uint64)
+    u = u + 0x7FFF + ((u >> 16) & 1)
+    return int((u >> 16) & 0xFFFF)
+
+
+def test_bf16_conversion_round_to_nearest_even(oracle_mod):
+    L = oracle_mod.lib()
+    rng = np.random.default_rng(1)
+    for v in np.concatenate([rng.standard_normal(3000).astype(np.float32) * 0.03,
+                             np.array([1.00390625, 1.01171875, -1.00390625], np.float32)]):
+        assert L.orc_float_to_bf16(float(v)) == bf16_rne(v)
+
+
+def test_low_precision_storage_tracks_f64(oracle_mod):
+    """f16 / bf16 (f - w) storage against the f64 oracle on a short channel run.
+    Tolerances: |d rho|, |d u| <= 5e-4 for f16 and <= 3e-3 for bf16."""
+    P = oracle_mod
+
+    def run(prec):
+        o = P.Oracle(24, 12, 1.0 / 0.6, P.EDGE_CHANNEL, prec)
+        o.init_equilibrium(1.0, 0.08, 0.0, 1e-3, 1)
+        o.step(20)
+        _, r, jx, jy = o.state()
+        return r, jx / r, jy / r
+
+    r64, ux64, uy64 = run(P.P_F64)
+    for prec, tol in ((P.P_F16, 5e-4), (P.P_BF16, 3e-3)):
+        r, ux, uy = run(prec)
+        assert np.abs(r - r64).max() <= tol
+        assert max(np.abs(ux - ux64).max(), np.abs(uy - uy64).max()) <= tol
