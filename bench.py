@@ -124,7 +124,7 @@ def workload_mask():
 def time_storage(lbm, torch, storage, mask, steps, warmup):
     """Device-resident MLUPS of one storage format; returns (ms_per_step, launches)."""
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, storage)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
     lat.set_stream(stream.cuda_stream)
     lat.set_inlet_velocity(UX)
     lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
@@ -167,7 +167,7 @@ def run_ours(args):
 
     # --- value: K steps with the state resident, f32 ---------------------------
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()  # the engine's kernels and the timing events share this stream
     lat.set_stream(stream.cuda_stream)
     lat.set_inlet_velocity(UX)
     lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)

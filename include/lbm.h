@@ -69,7 +69,8 @@ const char* lbm_version(void);
 /* LBM::new (lbm-wgpu/src/lbm.rs:726): allocate an nx x ny grid on the
  * current CUDA device with relaxation rate omega, barrier = init_barrier
  * (lbm.rs:595-605) in LBM_EDGE_REF (no walls in LBM_EDGE_CHANNEL), state =
- * set_equil(0.1, 0, 1) (lbm.rs:740).  nx, ny >= 3; ny <= 65535; nx * ny < 2^31. */
+ * set_equil(0.1, 0, 1) (lbm.rs:740).  nx, ny >= 3; ny <= 65535; the padded grid
+ * (nx rounded up to 32, times ny) below 2^29 cells. */
 int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage, lbm_sim** out);
 
 /* Drop of LBM: free all device memory of the handle. */
@@ -78,14 +79,23 @@ int lbm_destroy(lbm_sim* sim);
 /* Dimensions and mode of a handle (any pointer may be NULL). */
 int lbm_get_info(const lbm_sim* sim, uint32_t* nx, uint32_t* ny, int* edge_mode, int* storage);
 
-/* Queue the handle's work on an external CUDA stream (a cudaStream_t passed as
- * void*; NULL restores the handle's own stream). */
+/* Queue the handle's work on a CUDA stream (a cudaStream_t passed as void*;
+ * NULL is CUDA's legacy default stream).  A new handle uses its own
+ * non-blocking stream, which lbm_get_stream returns. */
 int lbm_set_stream(lbm_sim* sim, void* cuda_stream);
+int lbm_get_stream(const lbm_sim* sim, void** cuda_stream);
 
-/* Launch shape of the step kernel: rows of cells each thread walks (default
- * 8; no counterpart in the reference, whose dispatch is fixed at 256-wide
- * 1-D workgroups, lbm.rs:102-106). */
-int lbm_set_tuning(lbm_sim* sim, int rows_per_thread);
+/* Step kernel variant and launch shape; every variant gives identical
+ * results.  kernel 0: one cell per thread, rows_per_thread rows each;
+ * 1: the same with the next row's loads issued before the current row's
+ * collision; 2, 3, 4, 5: row segments staged in shared memory by the
+ * bulk-copy engine with a ring of 5, 4, 6, 8 stages, a producer warp and 8
+ * consumer warps per 256-column strip (rows_per_thread is then the minimum
+ * band height).  Defaults: 3 for f32, 5 for f16 / bf16; f64 storage always
+ * uses kernel 0.  No counterpart in the
+ * reference, whose dispatch is fixed at 256-wide 1-D workgroups
+ * (lbm.rs:102-106). */
+int lbm_set_tuning(lbm_sim* sim, int rows_per_thread, int kernel);
 
 /* draw_shape / draw_barrier_updates (lbm.rs:1337-1356, barrier_draw.wgsl:13-17):
  * npairs (location, value) pairs; value 1 sets a solid cell, any other value

@@ -58,7 +58,8 @@ _SIGS = [
     ("lbm_destroy", ctypes.c_int, [_P]),
     ("lbm_get_info", ctypes.c_int, [_P, _P, _P, _P, _P]),
     ("lbm_set_stream", ctypes.c_int, [_P, _P]),
-    ("lbm_set_tuning", ctypes.c_int, [_P, ctypes.c_int]),
+    ("lbm_get_stream", ctypes.c_int, [_P, ctypes.POINTER(_P)]),
+    ("lbm_set_tuning", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int]),
     ("lbm_set_barrier", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     ("lbm_reset_barrier", ctypes.c_int, [_P]),
     ("lbm_set_mask", ctypes.c_int, [_P, _P]),
@@ -189,11 +190,17 @@ class Lattice:
     def single_cell(self, index):
         _check(_lib.lbm_single_cell(self._h, int(index)))
 
-    def set_tuning(self, rows_per_thread):
-        _check(_lib.lbm_set_tuning(self._h, int(rows_per_thread)))
+    def set_tuning(self, rows_per_thread=8, kernel=1):
+        _check(_lib.lbm_set_tuning(self._h, int(rows_per_thread), int(kernel)))
 
     def set_stream(self, stream_ptr):
+        """Queue work on a cudaStream_t given as an integer (0 = the legacy default stream)."""
         _check(_lib.lbm_set_stream(self._h, ctypes.c_void_p(stream_ptr) if stream_ptr else None))
+
+    def get_stream(self):
+        v = ctypes.c_void_p()
+        _check(_lib.lbm_get_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
 
     # -- stepping -----------------------------------------------------------
     def iterate(self, n):

@@ -10,6 +10,7 @@
 
 #include "../../include/lbm.h"
 #include "lbm_kernels.cuh"
+#include "lbm_stage.cuh"
 
 using namespace lbm;
 
@@ -41,6 +42,7 @@ int fail(int code, const char* fmt, ...) {
 
 constexpr int kBlockX = 128;
 constexpr int kReduceBlocks = 608;  // 4 x 152 SMs
+constexpr long long kPadCells = 4096;
 
 size_t store_bytes(int storage) {
   switch (storage) {
@@ -59,9 +61,12 @@ struct lbm_sim {
   Layout L{};
   size_t es = 4;   // bytes per stored population
   size_t cs = 4;   // bytes of the arithmetic type (moments)
-  void* f[2] = {nullptr, nullptr};
+  void* f[2] = {nullptr, nullptr};  // first element of plane 0 (inside the padded allocation)
   void* rest = nullptr;
   uint32_t* mask_d = nullptr;
+  void* f_base[2] = {nullptr, nullptr};  // allocations
+  void* rest_base = nullptr;
+  void* mask_base = nullptr;
   void* mom = nullptr;  // rho, jx, jy planes
   int* flag_d = nullptr;
   double* partial_d = nullptr;  // reduction partials
@@ -75,6 +80,9 @@ struct lbm_sim {
   bool moments_valid = false;
   uint64_t steps = 0, launches = 0;
   int rows = 8;
+  int kernel = 2;  // step kernel variant (lbm_set_tuning)
+  int sms = 0;     // multiprocessors of the device
+  int staged_variant = -1, staged_bands = 0, staged_rows = 0;  // cached launch shape
 };
 
 namespace {
@@ -176,9 +184,48 @@ int check_sim(const lbm_sim* s) {
   } while (0)
 
 void release(lbm_sim* s) {
-  cudaFree(s->f[0]); cudaFree(s->f[1]); cudaFree(s->rest); cudaFree(s->mask_d); cudaFree(s->mom);
+  cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
+}
+
+// Staged step launch: one strip of kStageW columns per grid column, row bands
+// sized so that all CTAs are resident at once (one wave, equal work).
+template <class St, int EDGE, int NS>
+int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
+  constexpr int W = kStageW, TPB = kStageThreads;
+  using G = StageGeom<typename St::S>;
+  const size_t smem = (size_t)NS * G::kBytes;
+  auto kern = k_step_ws<St, EDGE, NS>;
+  if (s->staged_variant != s->kernel) {
+    CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem));
+    if (occ < 1) return fail(LBM_ERR_CUDA, "staged step kernel does not fit on a multiprocessor");
+    const int strips = (s->L.nx + W - 1) / W;
+    int bands = (occ * s->sms + strips - 1) / strips;
+    bands = std::max(1, std::min(bands, s->L.ny));
+    // at least `rows` rows per band (the tuning value): short bands re-read
+    // their two halo rows too often
+    s->staged_rows = std::max((s->L.ny + bands - 1) / bands, std::min(s->rows, s->L.ny));
+    s->staged_bands = (s->L.ny + s->staged_rows - 1) / s->staged_rows;
+    s->staged_variant = s->kernel;
+  }
+  a.rows = s->staged_rows;
+  dim3 grid((s->L.nx + W - 1) / W, s->staged_bands);
+  kern<<<grid, TPB, smem, s->stream>>>(a);
+  CK_LAUNCH();
+  return LBM_OK;
+}
+
+// Staged variants by ring depth.
+template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
+  switch (s->kernel) {
+    case 2: return launch_staged<St, EDGE, 5>(s, a);
+    case 3: return launch_staged<St, EDGE, 4>(s, a);
+    case 4: return launch_staged<St, EDGE, 6>(s, a);
+    default: return launch_staged<St, EDGE, 8>(s, a);
+  }
 }
 
 int compute_moments(lbm_sim* s) {
@@ -210,20 +257,27 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   if (!out) return fail(LBM_ERR_ARG, "out is null");
   *out = nullptr;
   if (nx < 3 || ny < 3) return fail(LBM_ERR_ARG, "grid %ux%u: both sides must be >= 3", nx, ny);
-  if ((uint64_t)nx * ny >= (1ull << 31) || ny > 65535)
-    return fail(LBM_ERR_ARG, "grid %ux%u too large (nx*ny < 2^31, ny <= 65535)", nx, ny);
+  const uint64_t padded = ((uint64_t)(nx + 127) / 128 * 128 * ny + 127) / 128 * 128;
+  if (8 * padded >= (1ull << 32) || ny > 65535)
+    return fail(LBM_ERR_ARG, "grid %ux%u too large (8 planes of the padded grid must stay below 2^32 cells, "
+                "ny <= 65535)", nx, ny);
   if (edge_mode != EDGE_REF && edge_mode != EDGE_CHANNEL) return fail(LBM_ERR_ARG, "bad edge mode %d", edge_mode);
   if (storage < STORE_F32 || storage > STORE_F64) return fail(LBM_ERR_ARG, "bad storage %d", storage);
   lbm_sim* s = new lbm_sim();
   CK(cudaGetDevice(&s->device));
   s->edge = edge_mode;
   s->storage = storage;
+  // fastest measured variant per storage width (4-stage ring for 4-byte
+  // words, 8-stage ring for 2-byte words); f64 runs the per-cell kernel
+  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 5);
   s->omega = omega;
   s->es = store_bytes(storage);
   s->cs = storage == STORE_F64 ? 8 : 4;
   s->L.nx = (int)nx;
   s->L.ny = (int)ny;
-  s->L.pitch = (int)((nx + 31) / 32 * 32);
+  // Rows are padded to 128 cells so every row of every plane, and every mask
+  // row, starts on a 16-byte boundary (bulk-copy alignment).
+  s->L.pitch = (int)((nx + 127) / 128 * 128);
   s->L.mw = s->L.pitch / 32;
   s->L.ps = ((long long)s->L.pitch * ny + 127) / 128 * 128;
   const size_t plane = (size_t)s->L.ps * s->es;
@@ -236,11 +290,20 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
     }
     return LBM_OK;
   };
+  // Population, rest and mask buffers carry kPadCells elements (words for
+  // the mask) of padding before and after, so the staged step kernel's
+  // row-segment copies with halos never leave an allocation.
+  auto alloc_padded = [&](void** base, void** p, size_t elems, size_t esz) -> int {
+    int r = alloc(base, (elems + 2 * (size_t)kPadCells) * esz);
+    if (!r) *p = (char*)*base + (size_t)kPadCells * esz;
+    return r;
+  };
   int rc;
-  if ((rc = alloc(&s->f[0], 8 * plane))) return rc;
-  if ((rc = alloc(&s->f[1], 8 * plane))) return rc;
-  if ((rc = alloc(&s->rest, plane))) return rc;
-  if ((rc = alloc((void**)&s->mask_d, (size_t)s->L.mw * ny * 4))) return rc;
+  if ((rc = alloc_padded(&s->f_base[0], &s->f[0], 8 * (size_t)s->L.ps, s->es))) return rc;
+  if ((rc = alloc_padded(&s->f_base[1], &s->f[1], 8 * (size_t)s->L.ps, s->es))) return rc;
+  if ((rc = alloc_padded(&s->rest_base, &s->rest, (size_t)s->L.ps, s->es))) return rc;
+  if ((rc = alloc_padded(&s->mask_base, (void**)&s->mask_d, (size_t)s->L.mw * ny, 4))) return rc;
+  (void)plane;
   if ((rc = alloc(&s->mom, 3 * (size_t)s->L.ps * s->cs))) return rc;
   if ((rc = alloc((void**)&s->flag_d, 4))) return rc;
   if ((rc = alloc((void**)&s->partial_d, (size_t)kReduceBlocks * 3 * 8))) return rc;
@@ -252,6 +315,9 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
     return fail(LBM_ERR_CUDA, "cudaStreamCreate failed");
   }
   s->stream = s->own_stream;
+  cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
+  if (s->sms < 1) s->sms = 1;
+  cudaMemsetAsync(s->mask_base, 0, ((size_t)s->L.mw * ny + 2 * (size_t)kPadCells) * 4, s->stream);
   cudaMemsetAsync(s->flag_d, 0, 4, s->stream);
   cudaMemsetAsync(s->mom, 0, 3 * (size_t)s->L.ps * s->cs, s->stream);
   s->mask_h.assign((size_t)nx * ny, 0);
@@ -287,14 +353,23 @@ int lbm_get_info(const lbm_sim* s, uint32_t* nx, uint32_t* ny, int* edge, int* s
 
 int lbm_set_stream(lbm_sim* s, void* stream) {
   CHECK_SIM(s);
-  s->stream = stream ? (cudaStream_t)stream : s->own_stream;
+  s->stream = (cudaStream_t)stream;  // NULL is CUDA's legacy default stream
   return LBM_OK;
 }
 
-int lbm_set_tuning(lbm_sim* s, int rows_per_thread) {
+int lbm_get_stream(const lbm_sim* s, void** stream) {
+  if (!s || !stream) return fail(LBM_ERR_ARG, "null argument");
+  *stream = (void*)s->stream;
+  return LBM_OK;
+}
+
+int lbm_set_tuning(lbm_sim* s, int rows_per_thread, int kernel) {
   CHECK_SIM(s);
   if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
+  if (kernel < 0 || kernel > 5) return fail(LBM_ERR_ARG, "kernel %d", kernel);
   s->rows = rows_per_thread;
+  s->kernel = kernel;
+  s->staged_variant = -1;  // recompute the staged launch shape
   return LBM_OK;
 }
 
@@ -408,6 +483,9 @@ int lbm_step(lbm_sim* s, uint32_t n) {
   CHECK_SIM(s);
   if (n == 0) return LBM_OK;
   const int rows = s->rows;
+  // f64 always runs the per-cell kernel: the pipelined and staged variants
+  // would spill its doubled register footprint.
+  const int variant = s->storage == STORE_F64 ? 0 : s->kernel;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, (s->L.ny + rows - 1) / rows);
   for (uint32_t k = 0; k < n; k++) {
     const bool last = k + 1 == n;
@@ -430,8 +508,15 @@ int lbm_step(lbm_sim* s, uint32_t n) {
       a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
       a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
       a.flag = s->flag_d;
-      if (s->edge == EDGE_REF) k_step<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(a);
-      else k_step<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(a);
+      if (variant >= 2) {
+        return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
+      } else if (variant == 1) {
+        if (s->edge == EDGE_REF) k_step_pf<St, EDGE_REF, 8><<<grid, kBlockX, 0, s->stream>>>(a);
+        else k_step_pf<St, EDGE_CHANNEL, 8><<<grid, kBlockX, 0, s->stream>>>(a);
+      } else {
+        if (s->edge == EDGE_REF) k_step<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(a);
+        else k_step<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(a);
+      }
       CK_LAUNCH();
       return LBM_OK;
     };
@@ -452,6 +537,7 @@ int lbm_synchronize(lbm_sim* s) {
   int flag = 0;
   CK(cudaMemcpy(&flag, s->flag_d, 4, cudaMemcpyDeviceToHost));
   if (flag & 1) return fail(LBM_ERR_STATE, "non-finite density detected");
+  if (flag & 2) return fail(LBM_ERR_STATE, "a staged step kernel gave up waiting for its copies");
   return LBM_OK;
 }
 

@@ -80,7 +80,8 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
   const Layout& L = a.L;
   const long long own = (long long)y * L.pitch + x;
   const bool interior = x >= 1 && x <= L.nx - 2 && y >= 1 && y <= L.ny - 2;
-  const bool frozen = EDGE == EDGE_CHANNEL && x == 0;
+  // channel mode: the inlet column and solid cells are inert (never collided)
+  const bool frozen = EDGE == EDGE_CHANNEL && (x == 0 || mask_bit(a.mask, L.mw, x, y));
   C f[9];
   bool streamed;
   if (interior) {
@@ -152,6 +153,170 @@ __global__ void __launch_bounds__(128) k_step(StepArgs<typename St::S, typename 
   const int y0 = blockIdx.y * a.rows;
   const int y1 = min(y0 + a.rows, a.L.ny);
   for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);
+}
+
+// ---------------------------------------------------------------------------
+// Software-pipelined fused step: one cell per thread, `rows` rows per thread.
+// Where each of a cell's 9 pre-collision populations comes from (pulled
+// neighbour, own opposite for bounce-back, own previous value for a cell that
+// is not streamed) depends only on the mask, so the thread resolves the next
+// row's 9 source addresses and issues their loads before it collides the
+// current row: a full row of loads per warp stays in flight during the
+// arithmetic, which is what keeps HBM busy at this occupancy.
+// ---------------------------------------------------------------------------
+
+// Source of a cell's populations: element offsets into src (or into dst when
+// the cell is not streamed), one per moving direction in slot order.
+struct CellSrc {
+  uint32_t off[8];
+  bool from_dst;
+};
+
+template <int EDGE>
+__device__ __forceinline__ void cell_sources(const Layout& L, const uint32_t* __restrict__ mask, bool materialised,
+                                             int x, int y, uint32_t tm, uint32_t t0, uint32_t tp, CellSrc& cs) {
+  const uint32_t own = (uint32_t)y * (uint32_t)L.pitch + (uint32_t)x;
+  const bool interior = x >= 1 && x <= L.nx - 2 && y >= 1 && y <= L.ny - 2;
+  bool streamed;
+  if (interior) {
+    streamed = !materialised && !((t0 >> 1) & 1u);
+  } else {
+    const bool own_solid = mask_bit(mask, L.mw, x, y);
+    streamed = !materialised && !own_solid && x != 0 && !(EDGE == EDGE_REF && y == L.ny - 1);
+  }
+  cs.from_dst = !streamed;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    const uint32_t base = (uint32_t)slot(q) * (uint32_t)L.ps;
+    uint32_t o = base + own;
+    if (streamed) {
+      if (interior) {
+        const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
+        const bool solid_up = (trip >> (1 - cx(q))) & 1u;
+        o = solid_up ? (uint32_t)slot(8 - q) * (uint32_t)L.ps + own
+                     : base + own - (uint32_t)cx(q) - (uint32_t)(cy(q) * L.pitch);
+      } else {
+        int ux_, uy_;
+        upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
+        const bool solid_up = mask_bit(mask, L.mw, ux_, uy_);
+        o = solid_up ? (uint32_t)slot(8 - q) * (uint32_t)L.ps + own
+                     : base + (uint32_t)uy_ * (uint32_t)L.pitch + (uint32_t)ux_;
+      }
+    }
+    cs.off[slot(q)] = o;
+  }
+}
+
+// Mask triplet of row y (clamped rows give don't-care bits for edge rows).
+__device__ __forceinline__ uint32_t triplet_at(const Layout& L, const uint32_t* __restrict__ mask, int x, int y) {
+  if (x < 1 || x > L.nx - 2 || y < 0 || y > L.ny - 1) return 0u;
+  return row_triplet(mask + (long long)y * L.mw, x);
+}
+
+// Unconditional pulled loads of row y for an interior-shaped cell (edge cells
+// read clamped, in-bounds addresses whose values the per-cell fix-up replaces).
+template <class S>
+__device__ __forceinline__ void pulled_loads(const Layout& L, const S* __restrict__ src,
+                                             const S* __restrict__ rest, int x, int y, S v[9]) {
+  const int xl = max(x - 1, 0), xr = min(x + 1, L.pitch - 1);
+  const int ru = min(y + 1, L.ny - 1), rd = max(y - 1, 0);
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    const int ux_ = cx(q) > 0 ? xl : (cx(q) < 0 ? xr : x);
+    const int uy_ = cy(q) < 0 ? ru : (cy(q) > 0 ? rd : y);
+    v[q] = __ldg(src + (long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_);
+  }
+  v[4] = rest[(long long)y * L.pitch + x];
+}
+
+// After the unconditional loads, a per-cell fix-up: cells that are not
+// streamed take their own previous values from dst, bounce-back links take the
+// cell's own opposite population from src, edge cells resolve their
+// neighbours by the edge mode.  Only threads with such a cell issue these
+// (dependent) loads.
+template <class St, int EDGE, int MINB = 1>
+__global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, typename St::C> a) {
+  using S = typename St::S;
+  using C = typename St::C;
+  const Layout& L = a.L;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= L.nx) return;
+  const int y0 = blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, L.ny);
+  if (y0 >= y1) return;
+  if (a.materialised) {  // uniform: collide in place, per cell
+    for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);
+    return;
+  }
+  const bool xint = x >= 1 && x <= L.nx - 2;
+  // mask triplets of rows y-1 .. y+2, kept two rows ahead of their use
+  uint32_t tm = triplet_at(L, a.mask, x, y0 - 1);
+  uint32_t t0 = triplet_at(L, a.mask, x, y0);
+  uint32_t tp = triplet_at(L, a.mask, x, y0 + 1);
+  uint32_t tn = triplet_at(L, a.mask, x, y0 + 2);
+  S cur[9];
+  pulled_loads<S>(L, a.src, a.rest, x, y0, cur);
+  for (int y = y0; y < y1; y++) {
+    const long long own = (long long)y * L.pitch + x;
+    // next row's unconditional loads and the mask two rows ahead
+    S nxt[9];
+    const bool more = y + 1 < y1;
+    if (more) pulled_loads<S>(L, a.src, a.rest, x, y + 1, nxt);
+    const uint32_t t3 = triplet_at(L, a.mask, x, y + 3);
+    // fix-ups for this row
+    const bool interior = xint && y >= 1 && y <= L.ny - 2;
+    // channel mode: the inlet column and solid cells are inert
+    const bool frozen = EDGE == EDGE_CHANNEL &&
+                        (x == 0 || (interior ? ((t0 >> 1) & 1u) != 0u : mask_bit(a.mask, L.mw, x, y) != 0u));
+    if (interior) {
+      if ((t0 >> 1) & 1u) {  // solid: not streamed, own previous values
+#pragma unroll
+        for (int q = 0; q < 9; q++)
+          if (q != 4) cur[q] = a.dst[(long long)slot(q) * L.ps + own];
+      } else if ((tm | t0 | tp) & 7u) {  // a solid neighbour: bounce-back links
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          if (q == 4) continue;
+          const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
+          if ((trip >> (1 - cx(q))) & 1u) cur[q] = __ldg(a.src + (long long)slot(8 - q) * L.ps + own);
+        }
+      }
+    } else {  // edge cell: resolve every population by the edge rules
+      CellSrc cs;
+      cell_sources<EDGE>(L, a.mask, false, x, y, 0u, 0u, 0u, cs);
+      const S* base = cs.from_dst ? a.dst : a.src;
+#pragma unroll
+      for (int q = 0; q < 9; q++)
+        if (q != 4) cur[q] = base[cs.off[slot(q)]];
+    }
+    tm = t0; t0 = tp; tp = tn; tn = t3;
+    C f[9];
+#pragma unroll
+    for (int q = 0; q < 9; q++) f[q] = St::load(cur[q], q);
+    C rho, jx, jy;
+    moments<C>(f, rho, jx, jy);
+    if (!(rho - rho == C(0))) atomicOr(a.flag, 1);
+    if (a.rho_out) {
+      a.rho_out[own] = rho;
+      a.jx_out[own] = jx;
+      a.jy_out[own] = jy;
+    }
+    if (!frozen) {
+      bgk<C>(f, rho, jx, jy, a.omega);
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        if (q == 4) continue;
+        a.dst[(long long)slot(q) * L.ps + own] = St::store(f[q], q);
+      }
+      a.rest[own] = St::store(f[4], 4);
+    }
+    if (more) {
+#pragma unroll
+      for (int q = 0; q < 9; q++) cur[q] = nxt[q];
+    }
+  }
 }
 
 // Stream-only pass: turns the fused representation into the reference's

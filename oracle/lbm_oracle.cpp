@@ -35,7 +35,9 @@
 //                (column X-1 wraps onto column 0 of the adjacent row).
 //   EDGE_CHANNEL channel flow: column 0 is a frozen equilibrium inlet at
 //                (rho=1, u_in, 0); column X-1 is a zero-gradient outflow (pulls
-//                from x+1 read column X-1); top and bottom are periodic.
+//                from x+1 read column X-1); top and bottom are periodic; solid
+//                cells are inert (neither collided nor streamed), as usual for
+//                half-way bounce-back, which never reads a solid cell's values.
 //
 // Storage precisions: f32, f64, and f16 / bf16 storing (f_i - w_i) with the
 // arithmetic in f32; values are quantised only when a collision stores them.
@@ -205,7 +207,9 @@ template <class St> struct Sim : SimBase {
 
   void set_omega(double w) override { omega = (C)w; }
 
-  bool frozen(size_t i) const { return edge == EDGE_CHANNEL && (i % (size_t)X) == 0; }
+  // Channel mode: the inlet column and solid cells are inert (never
+  // collided); the reference mode collides every cell, solids included.
+  bool frozen(size_t i) const { return edge == EDGE_CHANNEL && ((i % (size_t)X) == 0 || barrier[i] == 1); }
 
   void fill_cell(size_t i, const C eq[9]) {
     for (int q = 0; q < 9; q++) {

@@ -23,12 +23,13 @@ def sha(a):
 
 
 @pytest.mark.parametrize("name", CASES)
-@pytest.mark.parametrize("rows", [8, 3])
-def test_gpu_matches_reference_fixture(lbm, cuda_ok, name, rows):
+@pytest.mark.parametrize("rows,kernel", [(8, 0), (3, 0), (8, 1), (3, 1), (1, 1), (8, 2), (1, 2), (13, 3), (3, 4),
+                                         (40, 5)])
+def test_gpu_matches_reference_fixture(lbm, cuda_ok, name, rows, kernel):
     g = golden(name)
     nx, ny, steps = int(g["nx"]), int(g["ny"]), int(g["steps"])
     with lbm.Lattice(nx, ny, float(g["omega"]), lbm.EDGE_REF, lbm.F32) as lat:
-        lat.set_tuning(rows)
+        lat.set_tuning(rows, kernel)
         lat.init_equilibrium(1.0, float(g["ux"]), 0.0, float(g["noise"]), int(g["seed"]))
         assert sha(lat.populations()) == str(g["init_sha"])
         lat.draw_mask(g["mask"])
@@ -72,9 +73,9 @@ def test_gpu_matches_reference_single_cell_fixture(lbm, cuda_ok):
 
 
 def run_pair(lbm, P, nx, ny, omega, edge, storage, prec, steps, mask, ux=0.1, noise=1e-3, seed=0, rows=8,
-             chunks=None, edits=None):
+             chunks=None, edits=None, kernel=1):
     lat = lbm.Lattice(nx, ny, omega, edge, storage)
-    lat.set_tuning(rows)
+    lat.set_tuning(rows, kernel)
     o = P.Oracle(nx, ny, float(np.float32(omega)), edge, prec)
     lat.set_inlet_velocity(ux)  # channel inlet speed (no field reset)
     o.set_inlet(float(np.float32(ux)), apply=False)
@@ -101,7 +102,8 @@ def assert_same_state(lat, o, f64=False):
 
 
 @pytest.mark.parametrize("edge", [0, 1])
-def test_gpu_config0_both_edge_modes(lbm, cuda_ok, oracle_mod, edge):
+@pytest.mark.parametrize("kernel", [0, 1, 2])
+def test_gpu_config0_both_edge_modes(lbm, cuda_ok, oracle_mod, edge, kernel):
     """256 x 128, tau 0.6, ux 0.1 +- 1e-4 noise, r=12 circle at (64,64), 1000 steps."""
     from lbm_gb300 import geometry
     P = oracle_mod
@@ -109,7 +111,8 @@ def test_gpu_config0_both_edge_modes(lbm, cuda_ok, oracle_mod, edge):
     if edge == 0:
         mask[0] = 1
         mask[-1] = 1
-    lat, o = run_pair(lbm, P, 256, 128, 1.0 / 0.6, edge, lbm.F32, P.P_F32, 1000, mask, ux=0.1, noise=1e-4, seed=0)
+    lat, o = run_pair(lbm, P, 256, 128, 1.0 / 0.6, edge, lbm.F32, P.P_F32, 1000, mask, ux=0.1, noise=1e-4, seed=0,
+                      kernel=kernel)
     assert_same_state(lat, o)
     lat.close()
 
@@ -119,14 +122,16 @@ STORAGES = [(0, 0, False), (3, 3, True), (1, 1, False), (2, 2, False)]  # (lbm s
 
 @pytest.mark.parametrize("storage,prec,f64", STORAGES)
 @pytest.mark.parametrize("edge", [0, 1])
-@pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5)])
-def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, edge, nx, ny, rows):
+@pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5), (600, 37, 7),
+                                        (1100, 700, 9)])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5])
+def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, edge, nx, ny, rows, kernel):
     P = oracle_mod
     rng = np.random.default_rng(nx * 1000 + ny + 7 * storage + edge)
     omega = float(np.float32(rng.uniform(0.7, 1.9)))
     mask = (rng.random((ny, nx)) < 0.15).astype(np.uint8)
     lat, o = run_pair(lbm, P, nx, ny, omega, edge, storage, prec, 60, mask, ux=0.07, noise=1e-2,
-                      seed=int(rng.integers(1 << 30)), rows=rows)
+                      seed=int(rng.integers(1 << 30)), rows=rows, kernel=kernel)
     assert_same_state(lat, o, f64=f64)
     lat.close()
 
