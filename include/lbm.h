@@ -169,6 +169,23 @@ int lbm_launch_count(const lbm_sim* sim, uint64_t* out);
  * (global mass and momentum; no counterpart in the reference). */
 int lbm_conservation(lbm_sim* sim, double out[3]);
 
+/* The same FP64 fluid sums for callers that cannot allocate device memory
+ * (an application that owns all device memory through its own pool, a
+ * real-time loop that cannot afford cudaMalloc's implicit synchronisation):
+ * no handle, no allocation.  No counterpart in the reference.
+ *   rho, jx, jy: device arrays of f32 moments, row pitch `pitch` elements;
+ *   solid: device array, one byte per cell (nonzero = excluded), or NULL;
+ *   out: device pointer to 3 doubles (sum rho, sum jx, sum jy);
+ *   stream: cudaStream_t as void* (NULL = the legacy default stream).
+ * Its scratch is a fixed 96 KiB array in the library's device image (present
+ * on every GPU that loads the library until exit), which limits ny * pitch to
+ * 2^28 cells; larger inputs return LBM_ERR_ARG before any device work.  All
+ * calls share that array, so calls that overlap on the GPU race: serialise
+ * them.  The first call on a device resolves the array's address there; make
+ * it before any stream capture.  Errors are reported by lbm_last_error(). */
+int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy, const uint8_t* solid, uint32_t nx,
+                             uint32_t ny, uint32_t pitch, double* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,8 @@ _SIGS = [
     ("lbm_step_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     ("lbm_launch_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     ("lbm_conservation", ctypes.c_int, [_P, _P]),
+    ("lbm_conservation_noalloc", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
+                                                _P, _P]),
 ]
 
 

@@ -54,6 +54,11 @@ size_t store_bytes(int storage) {
 
 }  // namespace
 
+namespace lbm_internal {
+// Lets the library's other translation units report through lbm_last_error().
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace lbm_internal
+
 struct lbm_sim {
   int device = 0;
   int edge = 0, storage = 0;

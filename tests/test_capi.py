@@ -33,7 +33,7 @@ def test_library_exports_every_declared_symbol(lbm):
 
 def test_python_mirror_binds_every_symbol(lbm):
     bound = {name for name, _, _ in lbm._SIGS}
-    assert declared_symbols() <= bound | {n for n in declared_symbols() if "noalloc" in n}
+    assert declared_symbols() <= bound
 
 
 def test_error_path_without_device(lbm):
