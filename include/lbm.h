@@ -91,8 +91,10 @@ int lbm_get_stream(const lbm_sim* sim, void** cuda_stream);
  * collision; 2, 3, 4, 5: row segments staged in shared memory by the
  * bulk-copy engine with a ring of 5, 4, 6, 8 stages, a producer warp and 8
  * consumer warps per 256-column strip (rows_per_thread is then the minimum
- * band height).  Defaults: 3 for f32, 5 for f16 / bf16; f64 storage always
- * uses kernel 0.  No counterpart in the
+ * band height); 6, 7, 8: the same with rings of 8, 6, 4 stages and two cells
+ * per consumer thread (channel mode; reference mode runs one).  Defaults: 3
+ * for f32, 8 for f16 / bf16; f64 storage always uses kernel 0.  No
+ * counterpart in the
  * reference, whose dispatch is fixed at 256-wide 1-D workgroups
  * (lbm.rs:102-106). */
 int lbm_set_tuning(lbm_sim* sim, int rows_per_thread, int kernel);

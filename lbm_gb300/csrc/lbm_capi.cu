@@ -196,12 +196,12 @@ void release(lbm_sim* s) {
 
 // Staged step launch: one strip of kStageW columns per grid column, row bands
 // sized so that all CTAs are resident at once (one wave, equal work).
-template <class St, int EDGE, int NS>
+template <class St, int EDGE, int NS, int CPT>
 int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
-  constexpr int W = kStageW, TPB = kStageThreads;
+  constexpr int W = kStageW, TPB = stage_threads<CPT>();
   using G = StageGeom<typename St::S>;
   const size_t smem = (size_t)NS * G::kBytes;
-  auto kern = k_step_ws<St, EDGE, NS>;
+  auto kern = k_step_ws<St, EDGE, NS, CPT>;
   if (s->staged_variant != s->kernel) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
@@ -223,13 +223,18 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   return LBM_OK;
 }
 
-// Staged variants by ring depth.
+// Staged variants: ring depth and cells per consumer thread (two cells per
+// thread exist for channel mode only; reference mode runs one).
 template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
+  constexpr int C2 = EDGE == EDGE_CHANNEL ? 2 : 1;
   switch (s->kernel) {
-    case 2: return launch_staged<St, EDGE, 5>(s, a);
-    case 3: return launch_staged<St, EDGE, 4>(s, a);
-    case 4: return launch_staged<St, EDGE, 6>(s, a);
-    default: return launch_staged<St, EDGE, 8>(s, a);
+    case 2: return launch_staged<St, EDGE, 5, 1>(s, a);
+    case 3: return launch_staged<St, EDGE, 4, 1>(s, a);
+    case 4: return launch_staged<St, EDGE, 6, 1>(s, a);
+    case 5: return launch_staged<St, EDGE, 8, 1>(s, a);
+    case 6: return launch_staged<St, EDGE, 8, C2>(s, a);
+    case 7: return launch_staged<St, EDGE, 6, C2>(s, a);
+    default: return launch_staged<St, EDGE, 4, C2>(s, a);
   }
 }
 
@@ -272,9 +277,10 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   CK(cudaGetDevice(&s->device));
   s->edge = edge_mode;
   s->storage = storage;
-  // fastest measured variant per storage width (4-stage ring for 4-byte
-  // words, 8-stage ring for 2-byte words); f64 runs the per-cell kernel
-  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 5);
+  // fastest measured variant per storage width: 4-stage ring, one cell per
+  // thread for 4-byte words; 4-stage ring, two cells per thread for 2-byte
+  // words (reference mode runs one cell per thread); f64: the per-cell kernel
+  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 8);
   s->omega = omega;
   s->es = store_bytes(storage);
   s->cs = storage == STORE_F64 ? 8 : 4;
@@ -371,7 +377,7 @@ int lbm_get_stream(const lbm_sim* s, void** stream) {
 int lbm_set_tuning(lbm_sim* s, int rows_per_thread, int kernel) {
   CHECK_SIM(s);
   if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
-  if (kernel < 0 || kernel > 5) return fail(LBM_ERR_ARG, "kernel %d", kernel);
+  if (kernel < 0 || kernel > 8) return fail(LBM_ERR_ARG, "kernel %d", kernel);
   s->rows = rows_per_thread;
   s->kernel = kernel;
   s->staged_variant = -1;  // recompute the staged launch shape
@@ -504,6 +510,10 @@ int lbm_step(lbm_sim* s, uint32_t n) {
       a.L = s->L;
       a.src = (const S*)s->f[src];
       a.dst = (S*)s->f[dst];
+      for (int p = 0; p < 8; p++) {
+        a.srcp[p] = a.src + (long long)p * s->L.ps;
+        a.dstp[p] = a.dst + (long long)p * s->L.ps;
+      }
       a.rest = (S*)s->rest;
       a.mask = s->mask_d;
       a.omega = (C)s->omega;

@@ -26,26 +26,88 @@ template <class C> __host__ __device__ inline C weight(int q) {
   return q == 4 ? C(4.0) / C(9.0) : ((q & 1) ? C(1.0) / C(9.0) : C(1.0) / C(36.0));
 }
 
-// Storage policies: S is the stored word, C the arithmetic type.
+template <class C> __device__ __forceinline__ void moments(const C f[9], C& rho, C& jx, C& jy);
+template <class C> __device__ __forceinline__ void bgk(C f[9], C rho, C jx, C jy, C w);
+
+// Deviation-form BGK on g_i = f_i - w_i, for 16-bit storage (f32 arithmetic,
+// explicit FMA, one IEEE reciprocal).  rho = 1 + drho keeps the density
+// deviation at full precision; f_i^eq - w_i = w_i * (c0 + rho * (t + t^2/2))
+// with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho u^2, and the
+// relaxation is g_i' = (1 - omega) g_i + (omega w_i) (c0 + rho (t + t^2/2)).
+__device__ __forceinline__ void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
+  const float s1 = (g[0] + g[1]) + (g[2] + g[3]);
+  const float s2 = (g[5] + g[6]) + (g[7] + g[8]);
+  drho = (s1 + g[4]) + s2;
+  jx = ((g[2] + g[5]) + g[8]) - ((g[0] + g[3]) + g[6]);
+  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  rho = 1.0f + drho;
+}
+__device__ __forceinline__ void relax_dev(float& g, float aw, float pt, float rho, float c0, float omw) {
+  g = __fmaf_rn(aw, __fmaf_rn(rho, pt, c0), omw * g);
+}
+__device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
+  const float inv = __frcp_rn(rho);
+  const float ux = jx * inv, uy = jy * inv;
+  const float u215 = 1.5f * __fmaf_rn(ux, ux, uy * uy);
+  const float c0 = __fmaf_rn(-rho, u215, drho);
+  const float tx = 3.0f * ux, ty = 3.0f * uy;
+  const float tp = tx + ty, tm = tx - ty;
+  const float hx = 0.5f * tx, hy = 0.5f * ty, hp = 0.5f * tp, hm = 0.5f * tm;
+  const float omw = 1.0f - omega;
+  const float aw1 = omega * (1.0f / 9.0f), aw2 = omega * (1.0f / 36.0f), aw0 = omega * (4.0f / 9.0f);
+  relax_dev(g[5], aw1, __fmaf_rn(hx, tx, tx), rho, c0, omw);   // e  (+x)
+  relax_dev(g[3], aw1, __fmaf_rn(hx, tx, -tx), rho, c0, omw);  // w  (-x)
+  relax_dev(g[1], aw1, __fmaf_rn(hy, ty, ty), rho, c0, omw);   // n  (+y)
+  relax_dev(g[7], aw1, __fmaf_rn(hy, ty, -ty), rho, c0, omw);  // s  (-y)
+  relax_dev(g[2], aw2, __fmaf_rn(hp, tp, tp), rho, c0, omw);   // ne (+x+y)
+  relax_dev(g[6], aw2, __fmaf_rn(hp, tp, -tp), rho, c0, omw);  // sw (-x-y)
+  relax_dev(g[8], aw2, __fmaf_rn(hm, tm, tm), rho, c0, omw);   // se (+x-y)
+  relax_dev(g[0], aw2, __fmaf_rn(hm, tm, -tm), rho, c0, omw);  // nw (-x+y)
+  g[4] = __fmaf_rn(aw0, c0, omw * g[4]);                        // rest (t = 0)
+}
+
+// Storage policies.  S is the stored word, C the arithmetic type, and a
+// "working value" is what the step kernels carry per population: f_i for
+// f32 / f64 (the reference's arithmetic), g_i = f_i - w_i for 16-bit storage.
+//   load / store      stored word <-> working value
+//   f_of / of_f       stored word <-> population value f_i (readout, init)
+//   moments / collide the collision in the working representation; `aux`
+//                     carries drho between them in the deviation form
 struct StF32 {
   using S = float; using C = float;
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
+  __device__ static C f_of(S s, int) { return s; }
+  __device__ static S of_f(C f, int) { return f; }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
+  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF64 {
   using S = double; using C = double;
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
+  __device__ static C f_of(S s, int) { return s; }
+  __device__ static S of_f(C f, int) { return f; }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
+  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF16 {  // binary16 deviation from the rest-state weight
   using S = __half; using C = float;
-  __device__ static C load(S s, int q) { return weight<float>(q) + __half2float(s); }
-  __device__ static S store(C v, int q) { return __float2half_rn(v - weight<float>(q)); }
+  __device__ static C load(S s, int) { return __half2float(s); }
+  __device__ static S store(C v, int) { return __float2half_rn(v); }
+  __device__ static C f_of(S s, int q) { return weight<float>(q) + __half2float(s); }
+  __device__ static S of_f(C f, int q) { return __float2half_rn(f - weight<float>(q)); }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
+  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
 };
 struct StBF16 {  // bfloat16 deviation from the rest-state weight
   using S = __nv_bfloat16; using C = float;
-  __device__ static C load(S s, int q) { return weight<float>(q) + __bfloat162float(s); }
-  __device__ static S store(C v, int q) { return __float2bfloat16_rn(v - weight<float>(q)); }
+  __device__ static C load(S s, int) { return __bfloat162float(s); }
+  __device__ static S store(C v, int) { return __float2bfloat16_rn(v); }
+  __device__ static C f_of(S s, int q) { return weight<float>(q) + __bfloat162float(s); }
+  __device__ static S of_f(C f, int q) { return __float2bfloat16_rn(f - weight<float>(q)); }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
+  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
 };
 
 // Device layout of one lattice.

@@ -21,6 +21,8 @@ template <class S, class C> struct StepArgs {
   Layout L;
   const S* __restrict__ src;  // 8 planes, P_{k-1}
   S* __restrict__ dst;        // 8 planes, P_{k-2} (or a materialised S_k) -> P_k
+  const S* srcp[8];           // src + slot * ps: per-plane bases (kernel-parameter operands)
+  S* dstp[8];                 // dst + slot * ps
   S* __restrict__ rest;       // rest plane, updated in place
   const uint32_t* __restrict__ mask;
   C omega;
@@ -127,7 +129,8 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
   }
   f[4] = St::load(a.rest[own], 4);
   C rho, jx, jy;
-  moments<C>(f, rho, jx, jy);
+  C aux;
+    St::moments(f, rho, aux, jx, jy);
   if (!(rho == rho) || rho - rho != C(0)) atomicOr(a.flag, 1);  // NaN or Inf
   if (a.rho_out) {
     a.rho_out[own] = rho;
@@ -135,7 +138,7 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
     a.jy_out[own] = jy;
   }
   if (frozen) return;  // channel inlet: fixed equilibrium, never collided
-  bgk<C>(f, rho, jx, jy, a.omega);
+  St::collide(f, rho, aux, jx, jy, a.omega);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     if (q == 4) continue;
@@ -296,7 +299,8 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
 #pragma unroll
     for (int q = 0; q < 9; q++) f[q] = St::load(cur[q], q);
     C rho, jx, jy;
-    moments<C>(f, rho, jx, jy);
+    C aux;
+    St::moments(f, rho, aux, jx, jy);
     if (!(rho - rho == C(0))) atomicOr(a.flag, 1);
     if (a.rho_out) {
       a.rho_out[own] = rho;
@@ -304,7 +308,7 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
       a.jy_out[own] = jy;
     }
     if (!frozen) {
-      bgk<C>(f, rho, jx, jy, a.omega);
+      St::collide(f, rho, aux, jx, jy, a.omega);
 #pragma unroll
       for (int q = 0; q < 9; q++) {
         if (q == 4) continue;
@@ -372,7 +376,7 @@ __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typenam
   if (single >= 0 && (long long)cell == single_cell) eq[single] = C(4.0);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::store(eq[q], q);
+    const auto v = St::of_f(eq[q], q);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -391,7 +395,7 @@ __global__ void k_inlet(Layout L, typename St::S* f0, typename St::S* f1, typena
   set_equil<C>(u_in, C(0), C(1), eq);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::store(eq[q], q);
+    const auto v = St::of_f(eq[q], q);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -410,7 +414,7 @@ __global__ void k_read_pops(Layout L, const typename St::S* f, const typename St
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     const auto s = q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own];
-    out[q * n + c] = (O)St::load(s, q);
+    out[q * n + c] = (O)St::f_of(s, q);
   }
 }
 
@@ -426,7 +430,7 @@ __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, t
   const long long n = (long long)L.nx * L.ny, c = (long long)y * L.nx + x;
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::store((C)in[q * n + c], q);
+    const auto v = St::of_f((C)in[q * n + c], q);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -446,7 +450,11 @@ __global__ void k_moments(Layout L, const typename St::S* f, const typename St::
   C v[9];
 #pragma unroll
   for (int q = 0; q < 9; q++) v[q] = St::load(q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own], q);
-  moments<C>(v, rho_out[own], jx_out[own], jy_out[own]);
+  C rho, aux, jx, jy;
+  St::moments(v, rho, aux, jx, jy);
+  rho_out[own] = rho;
+  jx_out[own] = jx;
+  jy_out[own] = jy;
 }
 
 // Deterministic FP64 sums of rho, jx, jy over fluid cells: per-block partial

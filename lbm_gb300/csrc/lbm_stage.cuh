@@ -63,9 +63,7 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                : "memory");
 }
 
-constexpr int kStageW = 256;        // columns per CTA, one per consumer thread
-constexpr int kConsumerWarps = kStageW / 32;
-constexpr int kStageThreads = kStageW + 32;  // consumers + one producer warp
+constexpr int kStageW = 256;  // columns per CTA
 
 // Shared-memory layout of one stage.
 template <class S> struct StageGeom {
@@ -80,38 +78,61 @@ template <class S> struct StageGeom {
   static_assert(kBytes % 16 == 0 && kSegBytes % 16 == 0 && kRestBytes % 16 == 0, "stage alignment");
 };
 
-// Solid bits of columns x-1, x, x+1 (bits 0..2) from a staged mask row; k is
-// the word index of x in the stage, b = x & 31.
-__device__ __forceinline__ uint32_t win3(const uint32_t* w, int k, int b) {
+// Solid bits of columns x0-1 .. x0+N (bits 0..N+1) from a staged mask row; k
+// is the word index of x0 in the stage, b = x0 & 31 (b + N <= 32).
+template <int N> __device__ __forceinline__ uint32_t winN(const uint32_t* w, int k, int b) {
   const uint32_t lo = w[k], hi = w[k + 1];
   const uint32_t prev = b == 0 ? (w[k - 1] >> 31) : ((lo >> (b - 1)) & 1u);
-  return ((__funnelshift_r(lo, hi, b) << 1) | prev) & 7u;
+  return ((__funnelshift_r(lo, hi, b) << 1) | prev) & ((1u << (N + 2)) - 1u);
 }
 
-template <class St, int EDGE, int NS>
-__global__ void __launch_bounds__(kStageThreads, 3) k_step_ws(StepArgs<typename St::S, typename St::C> a) {
+// Two adjacent working values stored as one 2-element word (the same
+// rounding as two separate St::store calls).
+__device__ __forceinline__ void store_pair(float* p, float a, float b) {
+  *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+__device__ __forceinline__ void store_pair(double* p, double a, double b) {
+  *reinterpret_cast<double2*>(p) = make_double2(a, b);
+}
+__device__ __forceinline__ void store_pair(__half* p, float a, float b) {
+  *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+}
+__device__ __forceinline__ void store_pair(__nv_bfloat16* p, float a, float b) {
+  *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
+}
+
+// Threads per CTA: kStageW / CPT consumers (CPT cells each) + one producer warp.
+template <int CPT> constexpr int stage_threads() { return kStageW / CPT + 32; }
+
+template <class St, int EDGE, int NS, int CPT>
+__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
+    k_step_ws(StepArgs<typename St::S, typename St::C> a) {
+  static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL), "two cells per thread: channel mode only");
   using S = typename St::S;
   using C = typename St::C;
   using G = StageGeom<S>;
+  constexpr int kConsumers = kStageW / CPT;
+  constexpr int kConsumerWarps = kConsumers / 32;
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NS];
   __shared__ __align__(8) uint64_t empty[NS];
   const Layout& L = a.L;
   const int tid = threadIdx.x;
-  const bool producer = tid >= kStageW;
+  const bool producer = tid >= kConsumers;
   const int xb = blockIdx.x * kStageW;
-  const int x = xb + tid;
+  const int x0 = xb + CPT * tid;
   const int y0 = blockIdx.y * a.rows;
   const int y1 = min(y0 + a.rows, L.ny);
   if (y0 >= y1) return;  // uniform per CTA
   if (a.materialised) {  // uniform: collide in place, per cell, from global memory
-    if (!producer && x < L.nx)
-      for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);
+    if (!producer)
+      for (int y = y0; y < y1; y++)
+        for (int j = 0; j < CPT; j++)
+          if (x0 + j < L.nx) step_cell<St, EDGE>(a, x0 + j, y);
     return;
   }
-  const int r_first = y0 - 1, r_last = y1;  // stages, inclusive
-  auto slot_of = [&](int r) { return (r - r_first) % NS; };
-  auto stage_ptr = [&](int r) -> unsigned char* { return smem + (size_t)slot_of(r) * G::kBytes; };
+  // stage r (r_first .. r_last) lives in ring slot (r - r_first) % NS
+  const int r_first = y0 - 1, r_last = y1;
   if (tid == 0) {
     for (int i = 0; i < NS; i++) {
       mbar_init(smem_addr(&full[i]), 1);
@@ -124,11 +145,11 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_step_ws(StepArgs<typename 
 
   if (producer) {
     if ((tid & 31) == 0) {
-      int r = r_first;
+      int r = r_first, s = 0;
+      uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
       bool ok = true;
       for (; r <= r_last; r++) {
-        const int i = r - r_first, s = i % NS;
-        if (i >= NS && !mbar_wait(smem_addr(&empty[s]), (uint32_t)((i / NS - 1) & 1))) {
+        if (r - r_first >= NS && !mbar_wait(smem_addr(&empty[s]), empty_parity)) {
           ok = false;
           break;
         }
@@ -138,12 +159,13 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_step_ws(StepArgs<typename 
         unsigned char* st = smem + (size_t)s * G::kBytes;
         const uint32_t bar = smem_addr(&full[s]);
         mbar_arrive_expect_tx(bar, G::kBytes);
+        const long long row = (long long)rr * L.pitch + xb;
 #pragma unroll
         for (int p = 0; p < 8; p++)
-          bulk_g2s(smem_addr(st + p * G::kSegBytes),
-                   a.src + (long long)p * L.ps + (long long)rr * L.pitch + xb - G::kHalo, G::kSegBytes, bar);
-        bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + (long long)rr * L.pitch + xb, G::kRestBytes, bar);
+          bulk_g2s(smem_addr(st + p * G::kSegBytes), a.srcp[p] + row - G::kHalo, G::kSegBytes, bar);
+        bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + row, G::kRestBytes, bar);
         bulk_g2s(smem_addr(st + G::kMaskOff), a.mask + (long long)rr * L.mw + (xb >> 5) - 4, G::kMaskBytes, bar);
+        if (++s == NS) { s = 0; empty_parity ^= 1u; }
       }
       if (!ok) atomicOr(a.flag, 2);
       // no copy may be in flight when the CTA exits: wait (bounded) for the
@@ -156,94 +178,162 @@ __global__ void __launch_bounds__(kStageThreads, 3) k_step_ws(StepArgs<typename 
     return;
   }
 
-  // ---- consumers: one cell (column x) per thread ----------------------------
+  // ---- consumers: CPT cells (columns x0 .. x0+CPT-1) per thread --------------
   const int lane = tid & 31;
-  const int e = G::kHalo + tid;  // element index of x in a moving segment
-  const int k = (x >> 5) - (xb >> 5) + 4, b = x & 31;
-  const bool in_row = x < L.nx;
-  auto wait_full = [&](int r) {
-    const int i = r - r_first;
-    return mbar_wait(smem_addr(&full[i % NS]), (uint32_t)((i / NS) & 1));
-  };
-  bool ok = wait_full(r_first) && wait_full(r_first + 1);
+  const int e = G::kHalo + CPT * tid;  // element index of x0 in a moving segment
+  const int k = (x0 >> 5) - (xb >> 5) + 4, b = x0 & 31;
+  constexpr uint32_t kWin = (1u << (CPT + 2)) - 1u;
+  // ring slots of stages y-1, y, y+1 and the phase parity of stage y+1
+  int slot_m = 0, slot_0 = 1 % NS, slot_p = 2 % NS;
+  uint32_t parity_p = 2 / NS;
+  bool ok = mbar_wait(smem_addr(&full[0]), 0) && mbar_wait(smem_addr(&full[1 % NS]), 1 / NS);
   uint32_t wm = 0, w0 = 0;
   if (ok) {
-    wm = win3(reinterpret_cast<const uint32_t*>(stage_ptr(r_first) + G::kMaskOff), k, b);
-    w0 = win3(reinterpret_cast<const uint32_t*>(stage_ptr(r_first + 1) + G::kMaskOff), k, b);
+    wm = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + G::kMaskOff), k, b);
+    w0 = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_0 * G::kBytes + G::kMaskOff), k, b);
   }
-  // column classes (the channel inlet, x = 0, falls outside xin: inert)
-  const int dxr = (EDGE == EDGE_CHANNEL && x == L.nx - 1) ? 0 : 1;  // outflow: x+1 pulls read column x
-  const bool xin = EDGE == EDGE_CHANNEL ? (x >= 1 && x <= L.nx - 1) : (x >= 1 && x <= L.nx - 2);
+  // column classes; the channel inlet (x = 0) is inert, the channel outflow
+  // (x = nx-1) pulls its x+1 populations from its own column
+  bool in_row[CPT], xin[CPT];
+  int dxr[CPT];
+#pragma unroll
+  for (int j = 0; j < CPT; j++) {
+    const int x = x0 + j;
+    in_row[j] = x < L.nx;
+    dxr[j] = (EDGE == EDGE_CHANNEL && x == L.nx - 1) ? 0 : 1;
+    xin[j] = EDGE == EDGE_CHANNEL ? (x >= 1 && x <= L.nx - 1) : (x >= 1 && x <= L.nx - 2);
+  }
   bool bad = false;
-  for (int y = y0; y < y1 && ok; y++) {
-    if (!wait_full(y + 1)) { ok = false; break; }
-    const unsigned char* sm = stage_ptr(y - 1);
-    const unsigned char* s0 = stage_ptr(y);
-    const unsigned char* sp = stage_ptr(y + 1);
-    const uint32_t wp = win3(reinterpret_cast<const uint32_t*>(sp + G::kMaskOff), k, b);
-    const bool own_solid = (w0 >> 1) & 1u;
-    const long long own = (long long)y * L.pitch + x;
+  uint32_t own = (uint32_t)y0 * (uint32_t)L.pitch + (uint32_t)x0;
+  for (int y = y0; y < y1 && ok; y++, own += (uint32_t)L.pitch) {
+    if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
+    const unsigned char* sm = smem + (size_t)slot_m * G::kBytes;
+    const unsigned char* s0 = smem + (size_t)slot_0 * G::kBytes;
+    const unsigned char* sp = smem + (size_t)slot_p * G::kBytes;
+    const uint32_t wp = winN<CPT>(reinterpret_cast<const uint32_t*>(sp + G::kMaskOff), k, b);
     const bool yin = EDGE == EDGE_CHANNEL || (y >= 1 && y <= L.ny - 2);
     // a warp with no solid bit near any of its cells skips the bounce-back
-    // test (all 32 lanes vote, before any lane branches)
-    const bool near_solid = __any_sync(0xffffffffu, ((wm | w0 | wp) & 7u) != 0u);
-    if (in_row && xin && yin && !(EDGE == EDGE_CHANNEL && own_solid)) {
+    // pass (all 32 lanes vote, before any lane branches)
+    const bool near_solid = __any_sync(0xffffffffu, ((wm | w0 | wp) & kWin) != 0u);
+    bool act[CPT], any_act = false;
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      const bool own_solid = (w0 >> (j + 1)) & 1u;
+      act[j] = in_row[j] && xin[j] && yin && !(EDGE == EDGE_CHANNEL && own_solid);
+      any_act |= act[j];
+    }
+    if (CPT == 1 && EDGE == EDGE_REF && act[0] && ((w0 >> 1) & 1u)) {
+      // reference mode: solids collide their own previous values (global memory)
       C f[9];
-      if (EDGE == EDGE_REF && own_solid) {  // reference mode: solids collide their own previous values
 #pragma unroll
-        for (int q = 0; q < 9; q++)
-          if (q != 4) f[q] = St::load(a.dst[(long long)slot(q) * L.ps + own], q);
-      } else {
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-          if (q == 4) continue;
-          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
-          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
-          const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr : 0);  // pull column offset
-          S v = seg[e + dx];
-          if (near_solid) {
-            const uint32_t rowwin = cy(q) < 0 ? wp : (cy(q) > 0 ? wm : w0);
-            if ((rowwin >> (1 + dx)) & 1u)  // upstream solid: own opposite population
-              v = reinterpret_cast<const S*>(s0 + slot(8 - q) * G::kSegBytes)[e];
-          }
-          f[q] = St::load(v, q);
-        }
-      }
+      for (int q = 0; q < 9; q++)
+        if (q != 4) f[q] = St::load(a.dstp[slot(q)][own], q);
       f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[tid], 4);
-      C rho, jx, jy;
-      moments<C>(f, rho, jx, jy);
+      C rho, jx, jy, aux;
+      St::moments(f, rho, aux, jx, jy);
       bad |= !(rho - rho == C(0));
       if (a.rho_out) {
         a.rho_out[own] = rho;
         a.jx_out[own] = jx;
         a.jy_out[own] = jy;
       }
-      bgk<C>(f, rho, jx, jy, a.omega);
+      St::collide(f, rho, aux, jx, jy, a.omega);
 #pragma unroll
       for (int q = 0; q < 9; q++)
-        if (q != 4) a.dst[(long long)slot(q) * L.ps + own] = St::store(f[q], q);
+        if (q != 4) a.dstp[slot(q)][own] = St::store(f[q], q);
       a.rest[own] = St::store(f[4], 4);
-    } else if (in_row && EDGE == EDGE_CHANNEL) {  // inlet column or a solid cell: inert
-      if (a.rho_out) {  // moments of its stored state
-        C f[9];
+    } else if (any_act) {
+      C f[9][CPT];
 #pragma unroll
-        for (int q = 0; q < 9; q++)
-          if (q != 4) f[q] = St::load(a.dst[(long long)slot(q) * L.ps + own], q);
-        f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[tid], 4);
-        C rho, jx, jy;
-        moments<C>(f, rho, jx, jy);
-        a.rho_out[own] = rho;
-        a.jx_out[own] = jx;
-        a.jy_out[own] = jy;
+      for (int q = 0; q < 9; q++) {  // plain pulls
+        if (q == 4) continue;
+        const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+        const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+#pragma unroll
+        for (int j = 0; j < CPT; j++) {
+          const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);  // pull column offset
+          f[q][j] = St::load(seg[e + j + dx], q);
+        }
       }
-    } else if (in_row) {  // reference-mode edge cell
-      step_cell<St, EDGE>(a, x, y);
+      if (near_solid) {  // half-way bounce-back: upstream solid -> own opposite population
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          if (q == 4) continue;
+          const uint32_t rowwin = cy(q) < 0 ? wp : (cy(q) > 0 ? wm : w0);
+          const S* opp = reinterpret_cast<const S*>(s0 + slot(8 - q) * G::kSegBytes);
+#pragma unroll
+          for (int j = 0; j < CPT; j++) {
+            const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);
+            if ((rowwin >> (j + 1 + dx)) & 1u) f[q][j] = St::load(opp[e + j], q);
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < CPT; j++) {
+        f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
+        C g[9];
+#pragma unroll
+        for (int q = 0; q < 9; q++) g[q] = f[q][j];
+        C rho, jx, jy, aux;
+        St::moments(g, rho, aux, jx, jy);
+        if (act[j]) {
+          bad |= !(rho - rho == C(0));
+          if (a.rho_out) {
+            a.rho_out[own + j] = rho;
+            a.jx_out[own + j] = jx;
+            a.jy_out[own + j] = jy;
+          }
+        }
+        St::collide(g, rho, aux, jx, jy, a.omega);
+#pragma unroll
+        for (int q = 0; q < 9; q++) f[q][j] = g[q];
+      }
+      if (CPT == 2 && act[0] && act[CPT - 1]) {  // both cells: one 2-element store per plane
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          S* p = q == 4 ? a.rest + own : a.dstp[slot(q)] + own;
+          store_pair(p, f[q][0], f[q][CPT - 1]);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < CPT; j++) {
+          if (!act[j]) continue;
+#pragma unroll
+          for (int q = 0; q < 9; q++)
+            if (q != 4) a.dstp[slot(q)][own + j] = St::store(f[q][j], q);
+          a.rest[own + j] = St::store(f[4][j], 4);
+        }
+      }
+    }
+    // cells outside the fast path
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      if (act[j] || !in_row[j]) continue;
+      if (EDGE == EDGE_CHANNEL) {  // inlet column or a solid cell: inert
+        if (a.rho_out) {           // moments of its stored state
+          C f[9];
+#pragma unroll
+          for (int q = 0; q < 9; q++)
+            if (q != 4) f[q] = St::load(a.dstp[slot(q)][own + j], q);
+          f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
+          C rho, jx, jy, aux;
+          St::moments(f, rho, aux, jx, jy);
+          a.rho_out[own + j] = rho;
+          a.jx_out[own + j] = jx;
+          a.jy_out[own + j] = jy;
+        }
+      } else {  // reference-mode edge cell
+        step_cell<St, EDGE>(a, x0 + j, y);
+      }
     }
     // stage y-1 is no longer needed by this warp
     __syncwarp();
-    if (lane == 0) mbar_arrive(smem_addr(&empty[slot_of(y - 1)]));
+    if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
     wm = w0;
     w0 = wp;
+    slot_m = slot_0;
+    slot_0 = slot_p;
+    if (++slot_p == NS) { slot_p = 0; parity_p ^= 1u; }
   }
   if (bad) atomicOr(a.flag, 1);
   if (!ok) atomicOr(a.flag, 2);

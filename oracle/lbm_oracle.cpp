@@ -118,17 +118,65 @@ template <class C> inline C weight(int q) {
   return (q & 1) ? C(1.0) / C(9.0) : C(1.0) / C(36.0);
 }
 
-// Storage policies: load returns f_q in the compute type; store quantises.
-struct StF32 { using S = float; using C = float;
-  static C load(S s, int) { return s; } static S store(C v, int) { return v; } };
-struct StF64 { using S = double; using C = double;
-  static C load(S s, int) { return s; } static S store(C v, int) { return v; } };
-struct StF16 { using S = uint16_t; using C = float;
-  static C load(S s, int q) { return weight<float>(q) + half_to_float(s); }
-  static S store(C v, int q) { return float_to_half_rn(v - weight<float>(q)); } };
-struct StBF16 { using S = uint16_t; using C = float;
-  static C load(S s, int q) { return weight<float>(q) + bf16_to_float(s); }
-  static S store(C v, int q) { return float_to_bf16_rn(v - weight<float>(q)); } };
+// Storage policies.  load / store convert between the stored word and the
+// working value of the collision; f_of / of_f between the stored word and the
+// population value f_q.  f32 / f64 work on f_q with the reference's
+// arithmetic (kDev = false).  16-bit storage keeps g_q = f_q - w_q and works
+// on g_q with the engine's own deviation-form collision (kDev = true; see
+// moments_dev / collide_dev below), which has no counterpart in the reference.
+struct StF32 { using S = float; using C = float; static constexpr bool kDev = false;
+  static C load(S s, int) { return s; } static S store(C v, int) { return v; }
+  static C f_of(S s, int) { return s; } static S of_f(C v, int) { return v; } };
+struct StF64 { using S = double; using C = double; static constexpr bool kDev = false;
+  static C load(S s, int) { return s; } static S store(C v, int) { return v; }
+  static C f_of(S s, int) { return s; } static S of_f(C v, int) { return v; } };
+struct StF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
+  static C load(S s, int) { return half_to_float(s); }
+  static S store(C v, int) { return float_to_half_rn(v); }
+  static C f_of(S s, int q) { return weight<float>(q) + half_to_float(s); }
+  static S of_f(C v, int q) { return float_to_half_rn(v - weight<float>(q)); } };
+struct StBF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
+  static C load(S s, int) { return bf16_to_float(s); }
+  static S store(C v, int) { return float_to_bf16_rn(v); }
+  static C f_of(S s, int q) { return weight<float>(q) + bf16_to_float(s); }
+  static S of_f(C v, int q) { return float_to_bf16_rn(v - weight<float>(q)); } };
+
+// Deviation-form BGK of the 16-bit storage modes, on g_q = f_q - w_q, with
+// rho = 1 + drho, one correctly rounded reciprocal and fused multiply-adds:
+// f_q^eq - w_q = w_q (c0 + rho (t + t^2/2)), t = 3 c_q.u, c0 = drho - 1.5 rho u^2,
+// relaxed as g_q' = (1 - omega) g_q + (omega w_q)(c0 + rho (t + t^2/2)).
+// Operation order is part of the definition (the GPU kernel uses the same).
+inline void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
+  const float s1 = (g[0] + g[1]) + (g[2] + g[3]);
+  const float s2 = (g[5] + g[6]) + (g[7] + g[8]);
+  drho = (s1 + g[4]) + s2;
+  jx = ((g[2] + g[5]) + g[8]) - ((g[0] + g[3]) + g[6]);
+  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  rho = 1.0f + drho;
+}
+inline void relax_dev(float& g, float aw, float pt, float rho, float c0, float omw) {
+  g = std::fma(aw, std::fma(rho, pt, c0), omw * g);
+}
+inline void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
+  const float inv = 1.0f / rho;
+  const float ux = jx * inv, uy = jy * inv;
+  const float u215 = 1.5f * std::fma(ux, ux, uy * uy);
+  const float c0 = std::fma(-rho, u215, drho);
+  const float tx = 3.0f * ux, ty = 3.0f * uy;
+  const float tp = tx + ty, tm = tx - ty;
+  const float hx = 0.5f * tx, hy = 0.5f * ty, hp = 0.5f * tp, hm = 0.5f * tm;
+  const float omw = 1.0f - omega;
+  const float aw1 = omega * (1.0f / 9.0f), aw2 = omega * (1.0f / 36.0f), aw0 = omega * (4.0f / 9.0f);
+  relax_dev(g[5], aw1, std::fma(hx, tx, tx), rho, c0, omw);
+  relax_dev(g[3], aw1, std::fma(hx, tx, -tx), rho, c0, omw);
+  relax_dev(g[1], aw1, std::fma(hy, ty, ty), rho, c0, omw);
+  relax_dev(g[7], aw1, std::fma(hy, ty, -ty), rho, c0, omw);
+  relax_dev(g[2], aw2, std::fma(hp, tp, tp), rho, c0, omw);
+  relax_dev(g[6], aw2, std::fma(hp, tp, -tp), rho, c0, omw);
+  relax_dev(g[8], aw2, std::fma(hm, tm, tm), rho, c0, omw);
+  relax_dev(g[0], aw2, std::fma(hm, tm, -tm), rho, c0, omw);
+  g[4] = std::fma(aw0, c0, omw * g[4]);
+}
 
 // splitmix64 finaliser; the seeded per-cell noise of the initial state.
 inline uint64_t mix64(uint64_t z) {
@@ -213,7 +261,7 @@ template <class St> struct Sim : SimBase {
 
   void fill_cell(size_t i, const C eq[9]) {
     for (int q = 0; q < 9; q++) {
-      S v = St::store(eq[q], q);
+      S v = St::of_f(eq[q], q);
       f[0][q][i] = v;
       f[1][q][i] = v;
     }
@@ -269,7 +317,7 @@ template <class St> struct Sim : SimBase {
     }
     if (dir >= 0) {
       size_t i = x + y * (size_t)X;
-      S v = St::store(C(4.0), dir);
+      S v = St::of_f(C(4.0), dir);
       f[0][dir][i] = v; f[1][dir][i] = v;
     }
     set_inlet_columns();
@@ -304,6 +352,23 @@ template <class St> struct Sim : SimBase {
     std::vector<S>& origin = f[0][4];
     const C w = omega;
     const long long n = (long long)N;
+    if constexpr (St::kDev) {
+      // 16-bit storage: the engine's deviation-form collision, per cell, in place
+#pragma omp parallel for num_threads(threads) schedule(static)
+      for (long long ii = 0; ii < n; ii++) {
+        size_t i = (size_t)ii;
+        float g[9];
+        for (int q = 0; q < 9; q++) g[q] = St::load(q == 4 ? origin[i] : F[q][i], q);
+        float r, dr, jxv, jyv;
+        moments_dev(g, r, dr, jxv, jyv);
+        ux[i] = jxv;
+        uy[i] = jyv;
+        rho[i] = r;
+        if (frozen(i)) continue;
+        collide_dev(g, r, dr, jxv, jyv, (float)w);
+        for (int q = 0; q < 9; q++) (q == 4 ? origin[i] : F[q][i]) = St::store(g[q], q);
+      }
+    } else {
     // pre_collide_corner, corner_pre_collision.wgsl:19-21
 #pragma omp parallel for num_threads(threads) schedule(static)
     for (long long ii = 0; ii < n; ii++) {
@@ -377,6 +442,7 @@ template <class St> struct Sim : SimBase {
       F[5][i] = St::store(e, 5); F[3][i] = St::store(wv, 3);
       F[1][i] = St::store(nn, 1); F[7][i] = St::store(s, 7);
     }
+    }  // reference-order collision
     // stream e_w, n_s, nw_se, ne_sw (lbm.rs:1127-1134): pull from set cur into
     // set nxt with half-way bounce-back; the four passes touch disjoint planes.
     std::vector<S>* G = f[nxt];
@@ -401,7 +467,7 @@ template <class St> struct Sim : SimBase {
     const int cur = (int)(step % 2);
     for (int q = 0; q < 9; q++) {
       const std::vector<S>& src = (q == 4) ? f[0][4] : f[cur][q];
-      if (pops9) for (size_t i = 0; i < N; i++) pops9[(size_t)q * N + i] = (double)St::load(src[i], q);
+      if (pops9) for (size_t i = 0; i < N; i++) pops9[(size_t)q * N + i] = (double)St::f_of(src[i], q);
     }
     for (size_t i = 0; i < N; i++) {
       if (r) r[i] = (double)rho[i];

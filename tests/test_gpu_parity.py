@@ -24,7 +24,7 @@ def sha(a):
 
 @pytest.mark.parametrize("name", CASES)
 @pytest.mark.parametrize("rows,kernel", [(8, 0), (3, 0), (8, 1), (3, 1), (1, 1), (8, 2), (1, 2), (13, 3), (3, 4),
-                                         (40, 5)])
+                                         (40, 5), (8, 6), (3, 7), (5, 8)])
 def test_gpu_matches_reference_fixture(lbm, cuda_ok, name, rows, kernel):
     g = golden(name)
     nx, ny, steps = int(g["nx"]), int(g["ny"]), int(g["steps"])
@@ -102,7 +102,7 @@ def assert_same_state(lat, o, f64=False):
 
 
 @pytest.mark.parametrize("edge", [0, 1])
-@pytest.mark.parametrize("kernel", [0, 1, 2])
+@pytest.mark.parametrize("kernel", [0, 1, 3, 6])
 def test_gpu_config0_both_edge_modes(lbm, cuda_ok, oracle_mod, edge, kernel):
     """256 x 128, tau 0.6, ux 0.1 +- 1e-4 noise, r=12 circle at (64,64), 1000 steps."""
     from lbm_gb300 import geometry
@@ -124,7 +124,7 @@ STORAGES = [(0, 0, False), (3, 3, True), (1, 1, False), (2, 2, False)]  # (lbm s
 @pytest.mark.parametrize("edge", [0, 1])
 @pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5), (600, 37, 7),
                                         (1100, 700, 9)])
-@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5, 6, 8])
 def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, edge, nx, ny, rows, kernel):
     P = oracle_mod
     rng = np.random.default_rng(nx * 1000 + ny + 7 * storage + edge)
