@@ -167,6 +167,13 @@ int lbm_step_count(const lbm_sim* sim, uint64_t* out);
 /* Kernels launched by this handle so far (instrumentation). */
 int lbm_launch_count(const lbm_sim* sim, uint64_t* out);
 
+/* Force on the solid cells (drag out[0] along +x, lift out[1] north
+ * positive) by momentum exchange on the half-way bounce-back links of the last
+ * collision: sum over streamed cells x and directions p with a solid
+ * neighbour x + c_p of 2 f_p*(x) c_p, in f64.  LBM_ERR_STATE before the first
+ * step.  No counterpart in the reference. */
+int lbm_read_force(lbm_sim* sim, double out[2]);
+
 /* FP64 sums over fluid cells of rho, jx, jy from the last step's moments
  * (global mass and momentum; no counterpart in the reference). */
 int lbm_conservation(lbm_sim* sim, double out[3]);

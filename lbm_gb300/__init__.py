@@ -81,6 +81,7 @@ _SIGS = [
     ("lbm_step_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     ("lbm_launch_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
     ("lbm_conservation", ctypes.c_int, [_P, _P]),
+    ("lbm_read_force", ctypes.c_int, [_P, _P]),
     ("lbm_conservation_noalloc", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 _P, _P]),
 ]
@@ -257,6 +258,13 @@ class Lattice:
         _check(fn(self._h, _ptr(a)))
 
     def conservation(self):
+        """FP64 (sum rho, sum jx, sum jy) over fluid cells."""
         out = np.zeros(3, np.float64)
         _check(_lib.lbm_conservation(self._h, _ptr(out)))
+        return out
+
+    def force(self):
+        """(drag, lift) on the solid cells by momentum exchange, f64."""
+        out = np.zeros(2, np.float64)
+        _check(_lib.lbm_read_force(self._h, _ptr(out)))
         return out

@@ -644,6 +644,38 @@ static int write_pops(lbm_sim* s, const void* in, bool f64) {
 int lbm_write_populations(lbm_sim* s, const float* in) { return write_pops(s, in, false); }
 int lbm_write_populations_f64(lbm_sim* s, const double* in) { return write_pops(s, in, true); }
 
+int lbm_read_force(lbm_sim* s, double out[2]) {
+  CHECK_SIM(s);
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  if (s->steps == 0) return fail(LBM_ERR_STATE, "no collision since the last initialisation");
+  // the last post-collision state: the current buffer, or the other one once
+  // the current buffer has been materialised
+  const void* P = s->materialised ? s->f[1 - s->cur] : s->f[s->cur];
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    if (s->edge == EDGE_REF)
+      k_force_partial<St, EDGE_REF><<<kReduceBlocks, 256, 0, s->stream>>>(s->L, (const S*)P, s->mask_d, s->partial_d);
+    else
+      k_force_partial<St, EDGE_CHANNEL><<<kReduceBlocks, 256, 0, s->stream>>>(s->L, (const S*)P, s->mask_d,
+                                                                              s->partial_d);
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  double* res = (double*)s->staging_d;
+  k_conservation_final<<<1, 256, 0, s->stream>>>(s->partial_d, kReduceBlocks, res);
+  CK_LAUNCH();
+  s->launches += 2;
+  double tmp[3];
+  CK(cudaMemcpyAsync(tmp, res, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  out[0] = tmp[0];
+  out[1] = tmp[1];
+  return LBM_OK;
+}
+
 int lbm_conservation(lbm_sim* s, double out[3]) {
   CHECK_SIM(s);
   if (!out) return fail(LBM_ERR_ARG, "out is null");

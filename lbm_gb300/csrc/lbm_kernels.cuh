@@ -437,6 +437,48 @@ __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, t
   }
 }
 
+// Force on the solid cells by momentum exchange, from a post-collision state
+// P (8 planes) and the mask: every streamed cell whose upstream neighbour in
+// direction q is solid takes back its own opposite population p = 8 - q, which
+// left towards the wall with velocity c_p and returns with -c_p, so the solid
+// receives 2 f_p c_p.  Summed in f64 per thread, per block in a fixed order;
+// x is +x, y is north (row - 1) positive.
+template <class St, int EDGE>
+__global__ void __launch_bounds__(256) k_force_partial(Layout L, const typename St::S* __restrict__ P,
+                                                      const uint32_t* __restrict__ mask, double* __restrict__ partial) {
+  __shared__ double sh[2][256];
+  double fx = 0.0, fy = 0.0;
+  const long long n = (long long)L.nx * L.ny;
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(c / L.nx), x = (int)(c % L.nx);
+    if (mask_bit(mask, L.mw, x, y) || x == 0 || (EDGE == EDGE_REF && y == L.ny - 1)) continue;  // not streamed
+    const long long own = (long long)y * L.pitch + x;
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      if (q == 4) continue;
+      int ux_, uy_;
+      upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
+      if (!mask_bit(mask, L.mw, ux_, uy_)) continue;
+      const int p = 8 - q;
+      const double f = (double)St::f_of(P[(long long)slot(p) * L.ps + own], p);
+      fx += 2.0 * f * (double)cx(p);
+      fy -= 2.0 * f * (double)cy(p);
+    }
+  }
+  sh[0][threadIdx.x] = fx;
+  sh[1][threadIdx.x] = fy;
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (threadIdx.x < w) {
+      sh[0][threadIdx.x] += sh[0][threadIdx.x + w];
+      sh[1][threadIdx.x] += sh[1][threadIdx.x + w];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 2) partial[blockIdx.x * 3 + threadIdx.x] = sh[threadIdx.x][0];
+  if (threadIdx.x == 2) partial[blockIdx.x * 3 + 2] = 0.0;
+}
+
 // Moments of a materialised state (no collision), for readback before the
 // first step after an initialisation.
 template <class St>

@@ -233,6 +233,7 @@ struct SimBase {
   virtual void get_state(double* pops9, double* rho, double* jx, double* jy) = 0;
   virtual void get_raw_state(void* set0, void* set1) = 0;
   virtual void put_state(const double* pops9) = 0;
+  virtual int force(double out[2]) = 0;
 };
 
 template <class St> struct Sim : SimBase {
@@ -487,6 +488,31 @@ template <class St> struct Sim : SimBase {
     }
   }
 
+  // Momentum-exchange force on the solids from the last post-collision state
+  // (set (step-1)%2, collided in place and left untouched by the stream): each
+  // streamed cell with a solid upstream neighbour in direction q hands back its
+  // own population p = 8 - q, transferring 2 f_p c_p to the solid.  x is +x,
+  // y is north (row - 1) positive.  Returns 1 before the first step.
+  int force(double out[2]) override {
+    if (step == 0) return 1;
+    const std::vector<S>* P = f[(step - 1) % 2];
+    double fx = 0.0, fy = 0.0;
+    for (size_t i = 0; i < N; i++) {
+      if (!streamed(i)) continue;
+      for (int q = 0; q < 9; q++) {
+        if (q == 4) continue;
+        if (barrier[upstream(i, q)] != 1) continue;
+        const int p = 8 - q;
+        const double v = (double)St::f_of(P[p][i], p);
+        fx += 2.0 * v * CX[p];
+        fy -= 2.0 * v * CY[p];
+      }
+    }
+    out[0] = fx;
+    out[1] = fy;
+    return 0;
+  }
+
   void put_state(const double* pops9) override {
     for (size_t i = 0; i < N; i++) {
       C v[9];
@@ -557,6 +583,7 @@ void orc_get_state(orc_sim* h, double* pops9, double* rho, double* jx, double* j
 }
 void orc_get_raw_state(orc_sim* h, void* cur, void* other) { ((SimBase*)h)->get_raw_state(cur, other); }
 void orc_put_state(orc_sim* h, const double* pops9) { ((SimBase*)h)->put_state(pops9); }
+int orc_force(orc_sim* h, double* out2) { return ((SimBase*)h)->force(out2); }
 
 // curl.wgsl:49 on density buffers (momenta); cells in column 0 and the last
 // row are left at 0 (the reference leaves them stale).  Clamped neighbours.

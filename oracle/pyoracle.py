@@ -67,6 +67,8 @@ def lib():
         L.orc_get_raw_state.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_put_state.argtypes = [ctypes.c_void_p, _c_f64p]
         L.orc_curl_ref.argtypes = [ctypes.c_void_p, _c_f64p]
+        L.orc_force.restype = ctypes.c_int
+        L.orc_force.argtypes = [ctypes.c_void_p, _c_f64p]
         L.orc_float_to_half.restype = ctypes.c_uint16
         L.orc_float_to_half.argtypes = [ctypes.c_float]
         L.orc_half_to_float.restype = ctypes.c_float
@@ -160,6 +162,13 @@ class Oracle:
         out = np.zeros(self.n)
         lib().orc_curl_ref(self.h, _ptr(out, _c_f64p))
         return out.reshape(self.ny, self.nx)
+
+    def force(self):
+        """(drag, lift) by momentum exchange on the last post-collision state."""
+        out = np.zeros(2)
+        if lib().orc_force(self.h, _ptr(out, _c_f64p)):
+            raise RuntimeError("no collision yet")
+        return out
 
 
 _ref = None
