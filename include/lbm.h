@@ -155,6 +155,11 @@ int lbm_read_field(lbm_sim* sim, int field, float* out);
 int lbm_read_populations(lbm_sim* sim, float* out);
 int lbm_read_populations_f64(lbm_sim* sim, double* out);
 
+/* The same f32 populations into a DEVICE array of 9 * nx * ny floats, queued
+ * on the handle's stream without synchronising (for on-device consumers such
+ * as the closure's training samples).  No counterpart in the reference. */
+int lbm_read_populations_device(lbm_sim* sim, float* device_out);
+
 /* Upload populations (9 planes, reference order) to both buffer sets, as
  * custom_speed / single_cell upload states (lbm.rs:1092-1095); the step
  * count restarts at 0. */

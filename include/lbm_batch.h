@@ -1,0 +1,76 @@
+/* Batched lattices: many independent D2Q9 channel domains advanced together.
+ *
+ * No counterpart in the reference (lbm-wgpu drives one lattice per `Lbm`
+ * object, lbm.rs).  Each domain behaves exactly like an lbm_sim created with
+ * LBM_EDGE_CHANNEL and the same storage: frozen equilibrium inlet at its own
+ * u_in on column 0, zero-gradient outflow, periodic top/bottom, half-way
+ * bounce-back from its own mask, its own omega.
+ * One lbm_batch_step advances every domain by one step in ONE persistent
+ * kernel launch over a table of (domain, 256-column strip, row band) tiles;
+ * runs of 20 steps are replayed from a CUDA graph captured on first use.
+ * Results are bit-identical to advancing each domain through lbm_sim.
+ *
+ * Storage: LBM_STORE_F32, LBM_STORE_F16, LBM_STORE_BF16.  Every call is
+ * ordered on the batch's own stream; reads synchronise it.  Status codes and
+ * lbm_last_error() as in lbm.h. */
+#ifndef LBM_GB300_BATCH_H
+#define LBM_GB300_BATCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "lbm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct lbm_batch lbm_batch;
+
+/* count domains; domain d is nx[d] x ny[d] (3..65535 rows, nx*ny < 2^28) with
+ * relaxation omega[d] in (0, 2) and inlet velocity u_in[d].  All domains start
+ * at equilibrium rho = 1, ux = u_in[d], uy = 0, no solids. */
+int lbm_batch_create(uint32_t count, const uint32_t* nx, const uint32_t* ny, const float* omega, const float* u_in,
+                     int storage, lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* batch);
+
+/* Number of domains, total cells, steps since the last initialisation. */
+int lbm_batch_info(const lbm_batch* batch, uint32_t* count, uint64_t* cells, uint64_t* steps);
+
+/* Replace domain d's solid mask: nx*ny bytes, row-major, nonzero = solid. */
+int lbm_batch_set_mask(lbm_batch* batch, uint32_t domain, const uint8_t* mask);
+
+/* Every domain to equilibrium at rho = 1, ux = u_in[d], uy = 0 with seeded
+ * uniform noise of amplitude noise_amp on ux and uy (seed + d for domain d,
+ * the generator of lbm_init_equilibrium); step count back to 0. */
+int lbm_batch_init_equilibrium(lbm_batch* batch, float noise_amp, uint64_t seed);
+
+/* Advance every domain n steps (asynchronous). */
+int lbm_batch_step(lbm_batch* batch, uint32_t n);
+
+/* Wait for the batch's stream; LBM_ERR_STATE as lbm_synchronize. */
+int lbm_batch_synchronize(lbm_batch* batch);
+
+/* Domain d's LBM_FIELD_* (nx*ny floats) / populations (9 planes, reference
+ * direction order, f32). */
+int lbm_batch_read_field(lbm_batch* batch, uint32_t domain, int field, float* out);
+int lbm_batch_read_populations(lbm_batch* batch, uint32_t domain, float* out);
+
+/* Fix the schedule by hand: variant 0..3 = (ring stages, cells per thread)
+ * (4,1) (6,1) (4,2) (8,2); dynamic 0 = tiles sorted longest first and dealt
+ * round-robin to the persistent CTAs, 1 = CTAs take tiles from an atomic
+ * counter; rows_per_bucket[3] = target band height for domains of height
+ * <= 128, <= 256 and taller (NULL keeps the current ones). */
+int lbm_batch_set_schedule(lbm_batch* batch, int variant, int dynamic, const int* rows_per_bucket);
+
+/* Time the candidate schedules on this batch (each for steps_per_trial steps
+ * after a warm-up; the state advances meanwhile) and keep the fastest.  The
+ * trials and the choice are written as JSON into report (report_len bytes,
+ * truncated; may be NULL). */
+int lbm_batch_autotune(lbm_batch* batch, uint32_t steps_per_trial, char* report, size_t report_len);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_BATCH_H */

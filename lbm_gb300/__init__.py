@@ -48,7 +48,7 @@ class LBMError(RuntimeError):
 
 _lib = None
 
-# (name, restype, argtypes) of every entry point declared in include/lbm.h
+# (name, restype, argtypes) of every entry point declared in include/*.h
 _P = ctypes.c_void_p
 _SIGS = [
     ("lbm_last_error", ctypes.c_char_p, []),
@@ -76,6 +76,7 @@ _SIGS = [
     ("lbm_read_field", ctypes.c_int, [_P, ctypes.c_int, _P]),
     ("lbm_read_populations", ctypes.c_int, [_P, _P]),
     ("lbm_read_populations_f64", ctypes.c_int, [_P, _P]),
+    ("lbm_read_populations_device", ctypes.c_int, [_P, _P]),
     ("lbm_write_populations", ctypes.c_int, [_P, _P]),
     ("lbm_write_populations_f64", ctypes.c_int, [_P, _P]),
     ("lbm_step_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64)]),
@@ -84,6 +85,38 @@ _SIGS = [
     ("lbm_read_force", ctypes.c_int, [_P, _P]),
     ("lbm_conservation_noalloc", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 _P, _P]),
+    # include/lbm_cnn.h
+    ("lbm_cnn_conv_forward", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P,
+                                            ctypes.c_int, ctypes.c_int, _P, _P]),
+    ("lbm_cnn_conv_backward_data", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                  _P, ctypes.c_int, _P, _P]),
+    ("lbm_cnn_conv_backward_weight", ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                    ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_size_t, _P]),
+    ("lbm_cnn_weight_scratch_bytes", ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    ("lbm_cnn_closure_loss", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
+                                            ctypes.c_float, _P, _P, _P, _P]),
+    ("lbm_cnn_adam", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
+                                    ctypes.c_float, ctypes.c_float, _P]),
+    ("lbm_cnn_closure_sample", ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
+                                              _P, _P]),
+    ("lbm_closure_set_weights", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    ("lbm_closure_enable", ctypes.c_int, [_P, ctypes.c_float]),
+    ("lbm_closure_disable", ctypes.c_int, [_P]),
+    ("lbm_closure_infer", ctypes.c_int, [_P]),
+    ("lbm_closure_read", ctypes.c_int, [_P, _P, _P]),
+    ("lbm_closure_fallback_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]),
+    # include/lbm_batch.h
+    ("lbm_batch_create", ctypes.c_int, [ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_int, ctypes.POINTER(_P)]),
+    ("lbm_batch_destroy", ctypes.c_int, [_P]),
+    ("lbm_batch_info", ctypes.c_int, [_P, _P, _P, _P]),
+    ("lbm_batch_set_mask", ctypes.c_int, [_P, ctypes.c_uint32, _P]),
+    ("lbm_batch_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint64]),
+    ("lbm_batch_step", ctypes.c_int, [_P, ctypes.c_uint32]),
+    ("lbm_batch_synchronize", ctypes.c_int, [_P]),
+    ("lbm_batch_read_field", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_int, _P]),
+    ("lbm_batch_read_populations", ctypes.c_int, [_P, ctypes.c_uint32, _P]),
+    ("lbm_batch_set_schedule", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P]),
+    ("lbm_batch_autotune", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]),
 ]
 
 

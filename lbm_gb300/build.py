@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbm_gb300.so")
-SOURCES = ["lbm_capi.cu", "lbm_noalloc.cu"]
+SOURCES = ["lbm_capi.cu", "lbm_noalloc.cu", "lbm_batch.cu", "lbm_cnn.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC,-O2",
                      "-Xptxas", "-v", "--expt-relaxed-constexpr"]
@@ -45,8 +45,9 @@ def stale():
     if not os.path.exists(LIB):
         return True
     t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(HERE, "..", "include", "lbm.h"),
-                                                               os.path.abspath(__file__)]
+    inc = os.path.join(HERE, "..", "include")
+    deps = ([os.path.join(CSRC, f) for f in os.listdir(CSRC)] + [os.path.join(inc, f) for f in os.listdir(inc)]
+            + [os.path.abspath(__file__)])
     return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
 
 

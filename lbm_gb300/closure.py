@@ -1,0 +1,285 @@
+"""Learned closure: training data from fine-grid runs of this engine, training
+of the relaxation-time network with the engine's own CUDA kernels, and
+coarse runs that apply it (include/lbm_cnn.h).
+
+The reference has no closure; this module adds one around the engine:
+
+* `fine_samples` runs a fine channel lattice and turns snapshot pairs (t,
+  t + F fine steps) into coarse training samples on the device
+  (lbm_cnn_closure_sample): features (rho, u, solid) and the loss
+  coefficients of a one-step fit of the coarse relaxation time;
+* `ClosureNet` holds the parameters, gradients and Adam state in device
+  memory (torch tensors serve only as allocations and a stream) and runs
+  forward / backward / loss / update through the C ABI kernels;
+* `coarse_run` advances a coarse lattice, refreshing the closure every
+  `refresh` steps, and time-averages its velocity.
+
+Acoustic scaling links the grids: a coarse cell is F x F fine cells, a coarse
+step is F fine steps, the lattice velocity is unchanged and the viscosity in
+coarse units is nu_fine / F, i.e. tau_coarse = 0.5 + (tau_fine - 0.5) / F.
+"""
+import ctypes
+
+import numpy as np
+
+from . import EDGE_CHANNEL, F32, LBMError, Lattice, _check, load_library
+from .geometry import random_circles
+
+LAYERS = [(4, 32, True), (32, 32, True), (32, 32, True), (32, 1, False)]  # (cin, cout, relu)
+N_PARAMS = sum(co * ci * 9 + co for ci, co, _ in LAYERS)
+S_RHO, S_U, DT_MAX = 50.0, 10.0, 0.25
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise LBMError(2, "the closure needs a CUDA device")
+    return torch
+
+
+def _p(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def coarse_tau(tau_fine, factor):
+    return 0.5 + (tau_fine - 0.5) / factor
+
+
+def unpack(flat):
+    """Packed parameters -> [[w (cout, cin, 3, 3), b (cout)], ...]."""
+    out, o = [], 0
+    for ci, co, _ in LAYERS:
+        w = flat[o:o + co * ci * 9].reshape(co, ci, 3, 3)
+        o += co * ci * 9
+        out.append([w, flat[o:o + co]])
+        o += co
+    return out
+
+
+def pack(params):
+    return np.concatenate([np.concatenate([np.asarray(w).reshape(-1), np.asarray(b).reshape(-1)])
+                           for w, b in params]).astype(np.float32)
+
+
+def round_bf16(a):
+    """Round float32 values to the nearest bfloat16 (ties to even), as float32."""
+    u = np.ascontiguousarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return (r & 0xFFFFFFFF).astype(np.uint32).view(np.float32).reshape(np.shape(a))
+
+
+def init_params(seed):
+    """He-uniform weights from a seeded generator, zero biases; the last
+    layer scaled by 0.1."""
+    rng = np.random.default_rng(seed)
+    params = []
+    for i, (ci, co, _) in enumerate(LAYERS):
+        lim = np.sqrt(6.0 / (ci * 9)) * (0.1 if i == len(LAYERS) - 1 else 1.0)
+        params.append([rng.uniform(-lim, lim, (co, ci, 3, 3)), np.zeros(co)])
+    return pack(params)
+
+
+class ClosureNet:
+    """Network parameters and work buffers on the current CUDA device."""
+
+    def __init__(self, params=None, seed=0):
+        self.torch = torch = _torch()
+        self.lib = load_library()
+        flat = init_params(seed) if params is None else np.asarray(params, np.float32)
+        if flat.size != N_PARAMS:
+            raise ValueError("need %d parameters" % N_PARAMS)
+        dev = torch.device("cuda")
+        self.params = torch.from_numpy(flat.copy()).to(dev)
+        self.grads = torch.zeros_like(self.params)
+        self.m = torch.zeros_like(self.params)
+        self.v = torch.zeros_like(self.params)
+        self.t = 0
+        self.scratch = torch.empty(max(self.lib.lbm_cnn_weight_scratch_bytes(ci, co) for ci, co, _ in LAYERS) // 4,
+                                   dtype=torch.float32, device=dev)
+        self.loss_scratch = torch.empty(608, dtype=torch.float64, device=dev)
+        self.loss_out = torch.empty(1, dtype=torch.float64, device=dev)
+        self._acts = None
+
+    def _views(self, buf):
+        out, o = [], 0
+        for ci, co, _ in LAYERS:
+            w = buf[o:o + co * ci * 9]
+            o += co * ci * 9
+            out.append((w, buf[o:o + co]))
+            o += co
+        return out
+
+    @property
+    def stream(self):
+        return ctypes.c_void_p(self.torch.cuda.current_stream().cuda_stream)
+
+    def numpy(self):
+        return self.params.cpu().numpy()
+
+    def forward(self, feat):
+        """feat: [N, 4, H, W] float32 CUDA tensor -> z [N, 1, H, W]."""
+        torch = self.torch
+        N, _, H, W = feat.shape
+        acts = [feat.contiguous()]
+        for (w, b), (ci, co, relu) in zip(self._views(self.params), LAYERS):
+            y = torch.empty((N, co, H, W), dtype=torch.float32, device=feat.device)
+            _check(self.lib.lbm_cnn_conv_forward(_p(acts[-1]), N, ci, H, W, _p(w), _p(b), co, 1 if relu else 0, _p(y),
+                                                 self.stream))
+            acts.append(y)
+        self._acts = acts
+        return acts[-1]
+
+    def backward(self, gz):
+        """Gradients of the last forward w.r.t. the parameters, into self.grads."""
+        torch = self.torch
+        acts = self._acts
+        N, _, H, W = acts[0].shape
+        g = gz.contiguous()
+        views = self._views(self.params)
+        gviews = self._views(self.grads)
+        for l in range(len(LAYERS) - 1, -1, -1):
+            ci, co, relu = LAYERS[l]
+            out = acts[l + 1] if relu else None
+            outp = _p(out) if out is not None else None
+            _check(self.lib.lbm_cnn_conv_backward_weight(_p(acts[l]), _p(g), outp, N, ci, H, W, co, _p(gviews[l][0]),
+                                                         _p(gviews[l][1]), _p(self.scratch),
+                                                         self.scratch.numel() * 4, self.stream))
+            if l > 0:
+                gx = torch.empty((N, ci, H, W), dtype=torch.float32, device=g.device)
+                _check(self.lib.lbm_cnn_conv_backward_data(_p(g), outp, N, ci, H, W, _p(views[l][0]), co, _p(gx),
+                                                           self.stream))
+                g = gx
+
+    def loss(self, z, coef, tau0, norm, grad=True):
+        """Closure loss (a device scalar, float64) and, with grad, dL/dz."""
+        N, _, H, W = z.shape
+        gz = self.torch.empty_like(z) if grad else None
+        _check(self.lib.lbm_cnn_closure_loss(_p(z), _p(coef), N, H, W, float(tau0), float(norm),
+                                             _p(gz) if grad else None, _p(self.loss_scratch), _p(self.loss_out),
+                                             self.stream))
+        return self.loss_out, gz
+
+    def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8):
+        self.t += 1
+        _check(self.lib.lbm_cnn_adam(_p(self.params), _p(self.grads), _p(self.m), _p(self.v), N_PARAMS, self.t,
+                                     float(lr), b1, b2, eps, self.stream))
+
+
+def sample(lib, stream, pops_t, pops_t1, solid_f, factor, feat, coef, scratch, solid_c):
+    hf, wf = solid_f.shape
+    _check(lib.lbm_cnn_closure_sample(_p(pops_t), _p(pops_t1), _p(solid_f), hf, wf, factor, _p(feat), _p(coef),
+                                      _p(scratch), _p(solid_c), stream))
+
+
+def fine_samples(mask, tau, u, steps, every, factor, seed=0, noise=1e-3, start=0, storage=F32):
+    """Run a fine channel lattice with `mask` for `steps` steps and return
+    the coarse samples of every snapshot pair (t, t + factor) taken every
+    `every` steps from step `start` on: (feat [S, 4, H, W], coef [S, 3, H, W],
+    coarse solid [H, W]) as CUDA tensors."""
+    torch = _torch()
+    lib = load_library()
+    ny, nx = mask.shape
+    H, W = ny // factor, nx // factor
+    dev = torch.device("cuda")
+    times = list(range(max(start, 0), steps - factor + 1, every))
+    feat = torch.empty((len(times), 4, H, W), dtype=torch.float32, device=dev)
+    coef = torch.empty((len(times), 3, H, W), dtype=torch.float32, device=dev)
+    solid_c = torch.empty((H, W), dtype=torch.uint8, device=dev)
+    solid_f = torch.from_numpy(np.ascontiguousarray(mask, dtype=np.uint8)).to(dev)
+    pa = torch.empty((9, ny, nx), dtype=torch.float32, device=dev)
+    pb = torch.empty_like(pa)
+    scratch = torch.empty(18 * H * W, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
+        lat.set_stream(stream.cuda_stream)
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, noise, seed)
+        lat.draw_mask(mask)
+        done = 0
+        for k, t in enumerate(times):
+            if t > done:
+                lat.iterate(t - done)
+            _check(lib.lbm_read_populations_device(lat.handle, _p(pa)))
+            lat.iterate(factor)
+            _check(lib.lbm_read_populations_device(lat.handle, _p(pb)))
+            done = t + factor
+            sample(lib, ctypes.c_void_p(stream.cuda_stream), pa, pb, solid_f, factor, feat[k], coef[k], scratch,
+                   solid_c)
+        lat.synchronize()
+    return feat, coef, solid_c
+
+
+def velocity_average(lat, steps, every, factor=1, solid=None):
+    """Advance `steps` steps and return the time average of (ux, uy) sampled
+    every `every` steps, block-averaged over the fluid cells of factor x
+    factor blocks when factor > 1 (solid gives the fine mask)."""
+    acc = None
+    n = 0
+    for _ in range(steps // every):
+        lat.iterate(every)
+        u = np.stack([lat.field("ux"), lat.field("uy")]).astype(np.float64)
+        acc = u if acc is None else acc + u
+        n += 1
+    u = acc / max(n, 1)
+    if factor > 1:
+        ny, nx = u.shape[1:]
+        fl = (solid == 0).astype(np.float64)[:ny // factor * factor, :nx // factor * factor]
+        fl = fl.reshape(ny // factor, factor, nx // factor, factor)
+        uu = u[:, :ny // factor * factor, :nx // factor * factor].reshape(2, ny // factor, factor, nx // factor,
+                                                                         factor)
+        cnt = fl.sum(axis=(1, 3))
+        u = (uu * fl[None]).sum(axis=(2, 4)) / np.maximum(cnt, 1)
+    return u
+
+
+def coarse_solid(mask, factor):
+    ny, nx = mask.shape
+    fl = (mask[:ny // factor * factor, :nx // factor * factor] == 0).reshape(ny // factor, factor, nx // factor,
+                                                                             factor)
+    return (2 * fl.sum(axis=(1, 3)) < factor * factor).astype(np.uint8)
+
+
+def coarse_run(mask_c, tau_c, u, steps, every, params=None, refresh=20, drift=0.5, seed=0, noise=1e-3,
+               storage=F32, average_from=0):
+    """Coarse channel run; with params, the closure is refreshed every
+    `refresh` steps.  Returns (time-averaged velocity [2, H, W] over steps
+    average_from..steps, fallback cell-steps)."""
+    H, W = mask_c.shape
+    lib = load_library()
+    with Lattice(W, H, 1.0 / tau_c, EDGE_CHANNEL, storage) as lat:
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, noise, seed)
+        lat.draw_mask(mask_c)
+        if params is not None:
+            p = np.ascontiguousarray(params, np.float32)
+            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
+            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
+        done = 0
+        while done < average_from:
+            k = min(refresh, average_from - done)
+            if params is not None:
+                _check(lib.lbm_closure_infer(lat.handle))
+            lat.iterate(k)
+            done += k
+        acc = np.zeros((2, H, W))
+        n = 0
+        while done < steps:
+            k = min(refresh, every, steps - done)
+            if params is not None and done % refresh == 0:
+                _check(lib.lbm_closure_infer(lat.handle))
+            lat.iterate(k)
+            done += k
+            if done % every == 0:
+                acc += np.stack([lat.field("ux"), lat.field("uy")])
+                n += 1
+        fb = ctypes.c_uint64(0)
+        if params is not None:
+            _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
+        lat.synchronize()
+    return acc / max(n, 1), fb.value
+
+
+def training_layouts(count, seed, nx, ny, rmin, rmax, fraction=0.1, clearance=64):
+    """Seeded random-circle layouts for the fine runs."""
+    return [random_circles(nx, ny, 10 ** 6, rmin, rmax, seed * 1000 + i, inlet_clearance=clearance,
+                           target_fraction=fraction) for i in range(count)]

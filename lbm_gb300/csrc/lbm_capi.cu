@@ -11,6 +11,8 @@
 #include "../../include/lbm.h"
 #include "lbm_kernels.cuh"
 #include "lbm_stage.cuh"
+#include "lbm_closure.cuh"
+#include "../../include/lbm_cnn.h"
 
 using namespace lbm;
 
@@ -88,6 +90,13 @@ struct lbm_sim {
   int kernel = 2;  // step kernel variant (lbm_set_tuning)
   int sms = 0;     // multiprocessors of the device
   int staged_variant = -1, staged_bands = 0, staged_rows = 0;  // cached launch shape
+  // learned closure (include/lbm_cnn.h)
+  void* closure_base = nullptr;          // padded allocation of the per-cell records
+  __half2* closure_d = nullptr;          // (delta_tau, |u| at prediction) per cell, pitch layout
+  __nv_bfloat16* cnn_w = nullptr;        // network parameters, BF16
+  unsigned long long* fallback_d = nullptr;
+  float drift = 0.5f;
+  bool closure_on = false;
 };
 
 namespace {
@@ -191,6 +200,7 @@ int check_sim(const lbm_sim* s) {
 void release(lbm_sim* s) {
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
+  cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->fallback_d);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -523,6 +533,10 @@ int lbm_step(lbm_sim* s, uint32_t n) {
       a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
       a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
       a.flag = s->flag_d;
+      a.closure = s->closure_on ? s->closure_d : nullptr;
+      a.tau0 = 1.0f / s->omega;
+      a.drift = s->drift;
+      a.fallback = s->closure_on ? s->fallback_d : nullptr;
       if (variant >= 2) {
         return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
       } else if (variant == 1) {
@@ -582,27 +596,32 @@ int lbm_read_field(lbm_sim* s, int field, float* out) {
   return LBM_OK;
 }
 
-static int read_pops(lbm_sim* s, void* out, bool f64) {
+// Populations of the current state, plane-major, into `out`: a host array
+// (through the staging buffer, synchronising) or, with device_out, a device
+// array written directly and asynchronously on the handle's stream.
+static int read_pops(lbm_sim* s, void* out, bool f64, bool device_out = false) {
   CHECK_SIM(s);
   if (!out) return fail(LBM_ERR_ARG, "out is null");
   int rc = materialise(s);
   if (rc) return rc;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  void* dst = device_out ? out : (void*)s->staging_d;
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
     if (f64)
       k_read_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
-                                                                (double*)s->staging_d);
+                                                                (double*)dst);
     else
       k_read_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
-                                                               (float*)s->staging_d);
+                                                               (float*)dst);
     CK_LAUNCH();
     return LBM_OK;
   };
   rc = dispatch_storage(s->storage, launch);
   if (rc) return rc;
   s->launches++;
+  if (device_out) return LBM_OK;
   CK(cudaMemcpyAsync(out, s->staging_d, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyDeviceToHost,
                      s->stream));
   CK(cudaStreamSynchronize(s->stream));
@@ -611,6 +630,7 @@ static int read_pops(lbm_sim* s, void* out, bool f64) {
 
 int lbm_read_populations(lbm_sim* s, float* out) { return read_pops(s, out, false); }
 int lbm_read_populations_f64(lbm_sim* s, double* out) { return read_pops(s, out, true); }
+int lbm_read_populations_device(lbm_sim* s, float* device_out) { return read_pops(s, device_out, false, true); }
 
 static int write_pops(lbm_sim* s, const void* in, bool f64) {
   CHECK_SIM(s);
@@ -712,6 +732,94 @@ int lbm_step_count(const lbm_sim* s, uint64_t* out) {
 int lbm_launch_count(const lbm_sim* s, uint64_t* out) {
   if (!s || !out) return fail(LBM_ERR_ARG, "null argument");
   *out = s->launches;
+  return LBM_OK;
+}
+
+
+// ---- learned closure on a lattice (include/lbm_cnn.h) ------------------------------
+
+int lbm_closure_set_weights(lbm_sim* s, const float* params, size_t n) {
+  CHECK_SIM(s);
+  if (!params || n != (size_t)kCnnParams) return fail(LBM_ERR_ARG, "closure weights: need %d parameters", kCnnParams);
+  std::vector<__nv_bfloat16> w(n);
+  for (size_t i = 0; i < n; i++) w[i] = __float2bfloat16_rn(params[i]);
+  if (!s->cnn_w) CK(cudaMalloc(&s->cnn_w, n * sizeof(__nv_bfloat16)));
+  CK(cudaMemcpyAsync(s->cnn_w, w.data(), n * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_closure_enable(lbm_sim* s, float drift) {
+  CHECK_SIM(s);
+  if (s->edge != EDGE_CHANNEL || s->storage == STORE_F64)
+    return fail(LBM_ERR_ARG, "the closure needs LBM_EDGE_CHANNEL and f32 / f16 / bf16 storage");
+  if (!(drift > 0.0f)) return fail(LBM_ERR_ARG, "drift threshold %g must be > 0", (double)drift);
+  if (!s->closure_base) {
+    const size_t bytes = (size_t)(s->L.ps + 2 * kPadCells) * sizeof(__half2);
+    CK(cudaMalloc(&s->closure_base, bytes));
+    CK(cudaMemsetAsync(s->closure_base, 0xFF, bytes, s->stream));  // NaN records: no prediction, plain BGK
+    s->closure_d = (__half2*)s->closure_base + kPadCells;
+  }
+  if (!s->fallback_d) {
+    CK(cudaMalloc(&s->fallback_d, sizeof(unsigned long long)));
+    CK(cudaMemsetAsync(s->fallback_d, 0, sizeof(unsigned long long), s->stream));
+  }
+  s->drift = drift;
+  s->closure_on = true;
+  return LBM_OK;
+}
+
+int lbm_closure_disable(lbm_sim* s) {
+  CHECK_SIM(s);
+  s->closure_on = false;
+  return LBM_OK;
+}
+
+int lbm_closure_infer(lbm_sim* s) {
+  CHECK_SIM(s);
+  if (!s->closure_on || !s->cnn_w) return fail(LBM_ERR_STATE, "closure not enabled or no weights set");
+  if (!s->moments_valid) {
+    int rc = materialise(s);
+    if (!rc) rc = compute_moments(s);
+    if (rc) return rc;
+  }
+  const size_t smem = sizeof(CnnSmem);
+  CK(cudaFuncSetAttribute(k_closure_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((s->L.nx + kCnnTile - 1) / kCnnTile, (s->L.ny + kCnnTile - 1) / kCnnTile);
+  k_closure_infer<<<grid, 256, smem, s->stream>>>(s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1),
+                                                  (const float*)mom_plane(s, 2), s->mask_d, s->cnn_w, LBM_CNN_S_RHO,
+                                                  LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d);
+  CK_LAUNCH();
+  s->launches++;
+  return LBM_OK;
+}
+
+int lbm_closure_read(lbm_sim* s, float* dtau, float* speed) {
+  CHECK_SIM(s);
+  if (!s->closure_d) return fail(LBM_ERR_STATE, "closure never enabled");
+  const size_t n = (size_t)s->L.ny * s->L.pitch;
+  std::vector<__half2> h(n);
+  CK(cudaMemcpyAsync(h.data(), s->closure_d, n * sizeof(__half2), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int y = 0; y < s->L.ny; y++)
+    for (int x = 0; x < s->L.nx; x++) {
+      const float2 v = __half22float2(h[(size_t)y * s->L.pitch + x]);
+      if (dtau) dtau[(size_t)y * s->L.nx + x] = v.x;
+      if (speed) speed[(size_t)y * s->L.nx + x] = v.y;
+    }
+  return LBM_OK;
+}
+
+int lbm_closure_fallback_count(lbm_sim* s, uint64_t* out, int reset) {
+  CHECK_SIM(s);
+  if (!out) return fail(LBM_ERR_ARG, "out is null");
+  *out = 0;
+  if (!s->fallback_d) return LBM_OK;
+  unsigned long long v = 0;
+  CK(cudaMemcpyAsync(&v, s->fallback_d, sizeof v, cudaMemcpyDeviceToHost, s->stream));
+  if (reset) CK(cudaMemsetAsync(s->fallback_d, 0, sizeof v, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  *out = v;
   return LBM_OK;
 }
 

@@ -32,7 +32,33 @@ template <class S, class C> struct StepArgs {
   C* __restrict__ jx_out;
   C* __restrict__ jy_out;
   int* __restrict__ flag;     // bit 0: non-finite density seen
+  // Learned closure (channel mode, f32 / 16-bit storage), or null: per cell
+  // (delta_tau, |u| when delta_tau was predicted).  A cell relaxes with
+  // 1 / (tau0 + delta_tau) while its speed stays within drift * max(|u|_pred,
+  // 0.01) of the predicted one, with the plain omega otherwise.
+  const __half2* __restrict__ closure;
+  float tau0, drift;
+  unsigned long long* __restrict__ fallback;  // cells that fell back to plain BGK, or null
 };
+
+// Relaxation rate of one cell: the uniform omega, or the closure's.
+// `counted`: the cell is a real fluid cell (lanes computing a discarded
+// result pass false and are not counted as fallbacks).
+template <class S, class C>
+__device__ __forceinline__ C cell_omega(const StepArgs<S, C>& a, long long own, C rho, C jx, C jy,
+                                        bool counted = true) {
+  if (!a.closure) return a.omega;
+  const float2 r = __half22float2(a.closure[own]);
+  const float fr = (float)rho, fx = (float)jx, fy = (float)jy;
+  const float sp = sqrtf(fx * fx + fy * fy) / fr;
+  const bool keep = fabsf(sp - r.y) <= a.drift * fmaxf(r.y, 0.01f) && r.x >= 0.0f && r.x <= 1.0f;
+  if (a.fallback) {
+    const unsigned am = __activemask();
+    const unsigned fb = __ballot_sync(am, !keep && counted);
+    if ((threadIdx.x & 31) == __ffs(am) - 1 && fb) atomicAdd(a.fallback, (unsigned long long)__popc(fb));
+  }
+  return keep ? (C)(1.0f / (a.tau0 + r.x)) : a.omega;
+}
 
 __device__ __forceinline__ uint32_t mask_bit(const uint32_t* __restrict__ mask, int mw, int x, int y) {
   return (__ldg(mask + (long long)y * mw + (x >> 5)) >> (x & 31)) & 1u;
@@ -138,7 +164,7 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
     a.jy_out[own] = jy;
   }
   if (frozen) return;  // channel inlet: fixed equilibrium, never collided
-  St::collide(f, rho, aux, jx, jy, a.omega);
+  St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy));
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     if (q == 4) continue;
@@ -308,7 +334,7 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
       a.jy_out[own] = jy;
     }
     if (!frozen) {
-      St::collide(f, rho, aux, jx, jy, a.omega);
+      St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy));
 #pragma unroll
       for (int q = 0; q < 9; q++) {
         if (q == 4) continue;
@@ -528,8 +554,8 @@ __global__ void __launch_bounds__(256) k_conservation_partial(Layout L, const ui
   if (threadIdx.x < 3) partial[blockIdx.x * 3 + threadIdx.x] = sh[threadIdx.x][0];
 }
 
-__global__ void __launch_bounds__(256) k_conservation_final(const double* __restrict__ partial, int nblocks,
-                                                           double* __restrict__ out) {
+static __global__ void __launch_bounds__(256) k_conservation_final(const double* __restrict__ partial, int nblocks,
+                                                                  double* __restrict__ out) {
   __shared__ double sh[3][256];
   for (int k = 0; k < 3; k++) {
     double s = 0.0;

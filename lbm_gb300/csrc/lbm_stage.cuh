@@ -34,6 +34,10 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)
 __device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
 }
+// Ends the life of a barrier so that its word can be initialised again.
+__device__ __forceinline__ void mbar_inval(uint32_t bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(bar) : "memory");
+}
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint32_t bar, uint32_t bytes) {
   asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
 }
@@ -104,33 +108,24 @@ __device__ __forceinline__ void store_pair(__nv_bfloat16* p, float a, float b) {
 // Threads per CTA: kStageW / CPT consumers (CPT cells each) + one producer warp.
 template <int CPT> constexpr int stage_threads() { return kStageW / CPT + 32; }
 
-template <class St, int EDGE, int NS, int CPT>
-__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
-    k_step_ws(StepArgs<typename St::S, typename St::C> a) {
+// One tile of the staged step: columns [xb, xb + kStageW) of rows [y0, y1) of
+// the lattice described by `a` (kernel parameters, or a copy in shared memory
+// for the batched kernel).  Every thread of the CTA calls it.  It arms the
+// ring's barriers itself, so consecutive tiles of a persistent CTA reuse the
+// ring once the CTA has synchronised between them.
+template <class St, int EDGE, int NS, int CPT, class A>
+__device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
+                                        uint64_t* empty) {
   static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL), "two cells per thread: channel mode only");
   using S = typename St::S;
   using C = typename St::C;
   using G = StageGeom<S>;
   constexpr int kConsumers = kStageW / CPT;
   constexpr int kConsumerWarps = kConsumers / 32;
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[NS];
-  __shared__ __align__(8) uint64_t empty[NS];
   const Layout& L = a.L;
   const int tid = threadIdx.x;
   const bool producer = tid >= kConsumers;
-  const int xb = blockIdx.x * kStageW;
   const int x0 = xb + CPT * tid;
-  const int y0 = blockIdx.y * a.rows;
-  const int y1 = min(y0 + a.rows, L.ny);
-  if (y0 >= y1) return;  // uniform per CTA
-  if (a.materialised) {  // uniform: collide in place, per cell, from global memory
-    if (!producer)
-      for (int y = y0; y < y1; y++)
-        for (int j = 0; j < CPT; j++)
-          if (x0 + j < L.nx) step_cell<St, EDGE>(a, x0 + j, y);
-    return;
-  }
   // stage r (r_first .. r_last) lives in ring slot (r - r_first) % NS
   const int r_first = y0 - 1, r_last = y1;
   if (tid == 0) {
@@ -284,7 +279,7 @@ __global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
             a.jy_out[own + j] = jy;
           }
         }
-        St::collide(g, rho, aux, jx, jy, a.omega);
+        St::collide(g, rho, aux, jx, jy, cell_omega(a, own + j, rho, jx, jy, act[j]));
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
       }
@@ -337,6 +332,28 @@ __global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
   }
   if (bad) atomicOr(a.flag, 1);
   if (!ok) atomicOr(a.flag, 2);
+}
+
+// The staged step over one lattice: CTA (bx, by) takes strip bx and row band by.
+template <class St, int EDGE, int NS, int CPT>
+__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
+    k_step_ws(StepArgs<typename St::S, typename St::C> a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ __align__(8) uint64_t full[NS];
+  __shared__ __align__(8) uint64_t empty[NS];
+  const int xb = blockIdx.x * kStageW;
+  const int y0 = blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, a.L.ny);
+  if (y0 >= y1) return;  // uniform per CTA
+  if (a.materialised) {  // uniform: collide in place, per cell, from global memory
+    const int x0 = xb + CPT * threadIdx.x;
+    if ((int)threadIdx.x < kStageW / CPT)
+      for (int y = y0; y < y1; y++)
+        for (int j = 0; j < CPT; j++)
+          if (x0 + j < a.L.nx) step_cell<St, EDGE>(a, x0 + j, y);
+    return;
+  }
+  ws_tile<St, EDGE, NS, CPT>(a, xb, y0, y1, smem, full, empty);
 }
 
 }  // namespace lbm

@@ -77,24 +77,30 @@ def random_circles(nx, ny, count, rmin, rmax, seed, inlet_clearance=64, target_f
     return m
 
 
-def random_layout(nx, ny, fraction, seed, rmin=2.0, rmax=None, rect_share=0.5, inlet_clearance=None):
-    """Circles and rectangles until the solid fraction reaches `fraction`."""
+def random_layout(nx, ny, fraction, seed, rmin=2.0, rmax=None, rect_share=0.5, inlet_clearance=None,
+                  outlet_clearance=0):
+    """Circles and rectangles until the solid fraction reaches `fraction`;
+    no solid within `inlet_clearance` columns of the inlet or
+    `outlet_clearance` columns of the outflow edge."""
     rng = SplitMix64(seed)
     m = np.zeros((ny, nx), np.uint8)
     rmax = rmax or max(rmin + 1.0, min(nx, ny) / 8.0)
     clear = inlet_clearance if inlet_clearance is not None else max(4, nx // 8)
+    xend = nx - 2 - outlet_clearance  # last column a shape may cover
     guard = 0
     while m.mean() < fraction and guard < 100000:
         guard += 1
         if rng.uniform() < rect_share:
             w = rng.randint(2, max(2, int(2 * rmax)))
             h = rng.randint(2, max(2, int(2 * rmax)))
-            x0 = rng.randint(clear, max(clear, nx - 2 - w))
+            x0 = rng.randint(clear, max(clear, xend - w))
             y0 = rng.randint(1, max(1, ny - 1 - h))
-            rect(m, x0, y0, x0 + w, y0 + h)
+            rect(m, x0, y0, min(x0 + w, xend + 1), y0 + h)
         else:
             r = rng.uniform(rmin, rmax)
-            cx = rng.uniform(clear + r, max(clear + r, nx - 2))
+            cx = rng.uniform(clear + r, max(clear + r, xend - r))
             cy = rng.uniform(0, ny - 1)
             disk(m, cx, cy, r)
+    if outlet_clearance:
+        m[:, max(xend + 1, 0):] = 0
     return m
