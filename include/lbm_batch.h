@@ -37,6 +37,10 @@ int lbm_batch_destroy(lbm_batch* batch);
 /* Number of domains, total cells, steps since the last initialisation. */
 int lbm_batch_info(const lbm_batch* batch, uint32_t* count, uint64_t* cells, uint64_t* steps);
 
+/* The batch's own CUDA stream (cudaStream_t as void*), for callers that
+ * order or time their work against it. */
+int lbm_batch_get_stream(const lbm_batch* batch, void** stream);
+
 /* Replace domain d's solid mask: nx*ny bytes, row-major, nonzero = solid. */
 int lbm_batch_set_mask(lbm_batch* batch, uint32_t domain, const uint8_t* mask);
 

@@ -46,30 +46,30 @@ int lbm_cnn_conv_backward_weight(const float* in, const float* grad_out, const f
 size_t lbm_cnn_weight_scratch_bytes(int cin, int cout);
 
 /* Closure loss of network outputs z [n, 1, h, w] against sample coefficients
- * coef [n, 3, h, w] (A, B, C per cell): sum over cells of
- * omega^2 A - 2 omega B + C with omega = 1 / (tau0 + delta_tau(z)), divided by
- * norm, written as one double to *loss_out; grad_z (may be NULL) receives its
- * gradient.  scratch: 608 doubles. */
-int lbm_cnn_closure_loss(const float* z, const float* coef, int n, int h, int w, float tau0, float norm,
-                         float* grad_z, double* scratch, double* loss_out, void* stream);
+ * coef [n, 3, h, w] (A, B, C per cell): the sum over cells of
+ * A dt^2 - 2 B dt + C with dt = delta_tau(z), divided by norm, written as one
+ * double to *loss_out; grad_z (may be NULL) receives its gradient.
+ * scratch: 608 doubles. */
+int lbm_cnn_closure_loss(const float* z, const float* coef, int n, int h, int w, float norm, float* grad_z,
+                         double* scratch, double* loss_out, void* stream);
 
 /* One Adam step (Kingma & Ba) on n parameters; t >= 1 is the step number. */
 int lbm_cnn_adam(float* param, const float* grad, float* m, float* v, int n, int t, float lr, float beta1,
                  float beta2, float eps, void* stream);
 
-/* Training sample of a snapshot pair of a fine run: pops_t, pops_t1 are the
- * fine populations [9, hf, wf] (reference direction order) at step t and at
- * step t + factor, solid_fine [hf, wf] its mask.  Writes, for the coarse grid
- * of (hf / factor) x (wf / factor) cells (block averages over each block's
- * fluid cells; a block is solid when fewer than half its cells are fluid):
- * feat [4, H, W] (scaled rho - 1, ux, uy and the solid flag), coef [3, H, W]
- * (A = sum a_i^2, B = sum a_i b_i, C = sum b_i^2 with a_i = f_i - feq_i and
- * b_i = f_i(x) - f_i(x + c_i) one coarse step later; zero where the cell is
- * solid, on the inlet column, or next to a solid or the outflow edge) and
- * solid_coarse [H, W].  scratch: 18 * H * W floats. */
-int lbm_cnn_closure_sample(const float* pops_t, const float* pops_t1, const uint8_t* solid_fine, int hf, int wf,
-                           int factor, float* feat, float* coef, float* scratch, uint8_t* solid_coarse,
-                           void* stream);
+/* Training sample of one snapshot of a fine run: pops [9, hf, wf] are its
+ * populations (reference direction order), solid_fine [hf, wf] its mask.
+ * For the coarse grid of (hf / factor) x (wf / factor) cells (Favre averages
+ * over each block's fluid cells; a block is solid when fewer than half its
+ * cells are fluid) it writes feat [4, H, W] (scaled rho - 1, Ux, Uy and the
+ * solid flag), coef [3, H, W] and solid_coarse [H, W].  coef holds, per cell,
+ * the eddy-viscosity fit of the subgrid stress tau_ij = <rho u_i u_j> / <rho>
+ * - U_i U_j against the coarse strain rate S (central differences of U, y
+ * periodic): the squared residual |tau^d + (2/3) dt S^d|^2 of the deviatoric
+ * parts is A dt^2 - 2 B dt + C.  Zero where the cell is solid, on the first or
+ * last column, or next to a solid.  scratch: 6 * H * W floats. */
+int lbm_cnn_closure_sample(const float* pops, const uint8_t* solid_fine, int hf, int wf, int factor, float* feat,
+                           float* coef, float* scratch, uint8_t* solid_coarse, void* stream);
 
 /* ---- the closure on a lattice (LBM_EDGE_CHANNEL, f32 / f16 / bf16 storage) ----
  *

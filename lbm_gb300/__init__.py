@@ -12,7 +12,7 @@
     reset_to_equilibrium(driver)   :1076   reset_to_equilibrium()
     single_cell(driver, index)     :1502   single_cell(index)
     iterate(driver, n)             :1065   iterate(n)  (compute part; returns nothing)
-    set_summary(stat) + draw       :1061   summary(stat) -> numpy array
+    set_summary(stat) + draw       :1061   summary(stat) -> numpy array; render(w, h) -> frame
     get_compute_num()              :1170   get_compute_num()
 
 Errors raise `LBMError` with the library's message.  The compute path is the
@@ -25,7 +25,7 @@ import os
 import numpy as np
 
 __all__ = ["Lattice", "LBMError", "load_library", "EDGE_REF", "EDGE_CHANNEL", "F32", "F16", "BF16", "F64",
-           "SummaryStat", "FIELD"]
+           "SummaryStat", "ColorMap", "FIELD"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
@@ -38,6 +38,11 @@ FIELD = {"rho": 0, "jx": 1, "jy": 2, "ux": 3, "uy": 4, "curl": 5, "vorticity": 6
 class SummaryStat:
     """The reference's SummaryStat enum (lbm.rs:10-16): Curl, Ux, Uy, Rho, Speed."""
     Curl, Ux, Uy, Rho, Speed = 0, 1, 2, 3, 4
+
+
+class ColorMap:
+    """The reference's ColorMap enum (lbm.rs:20-24): Inferno, Viridis, Jet."""
+    Inferno, Viridis, Jet = 0, 1, 2
 
 
 class LBMError(RuntimeError):
@@ -85,6 +90,11 @@ _SIGS = [
     ("lbm_read_force", ctypes.c_int, [_P, _P]),
     ("lbm_conservation_noalloc", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 _P, _P]),
+    # include/lbm_render.h
+    ("lbm_summary", ctypes.c_int, [_P, ctypes.c_int, _P]),
+    ("lbm_render", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, _P, _P,
+                                  ctypes.c_int]),
+    ("lbm_render_device", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, _P]),
     # include/lbm_cnn.h
     ("lbm_cnn_conv_forward", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P,
                                             ctypes.c_int, ctypes.c_int, _P, _P]),
@@ -94,11 +104,11 @@ _SIGS = [
                                                     ctypes.c_int, ctypes.c_int, _P, _P, _P, ctypes.c_size_t, _P]),
     ("lbm_cnn_weight_scratch_bytes", ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     ("lbm_cnn_closure_loss", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_float,
-                                            ctypes.c_float, _P, _P, _P, _P]),
+                                            _P, _P, _P, _P]),
     ("lbm_cnn_adam", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_float, ctypes.c_float,
                                     ctypes.c_float, ctypes.c_float, _P]),
-    ("lbm_cnn_closure_sample", ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P,
-                                              _P, _P]),
+    ("lbm_cnn_closure_sample", ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P, _P, _P,
+                                              _P]),
     ("lbm_closure_set_weights", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     ("lbm_closure_enable", ctypes.c_int, [_P, ctypes.c_float]),
     ("lbm_closure_disable", ctypes.c_int, [_P]),
@@ -109,6 +119,7 @@ _SIGS = [
     ("lbm_batch_create", ctypes.c_int, [ctypes.c_uint32, _P, _P, _P, _P, ctypes.c_int, ctypes.POINTER(_P)]),
     ("lbm_batch_destroy", ctypes.c_int, [_P]),
     ("lbm_batch_info", ctypes.c_int, [_P, _P, _P, _P]),
+    ("lbm_batch_get_stream", ctypes.c_int, [_P, ctypes.POINTER(_P)]),
     ("lbm_batch_set_mask", ctypes.c_int, [_P, ctypes.c_uint32, _P]),
     ("lbm_batch_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_uint64]),
     ("lbm_batch_step", ctypes.c_int, [_P, ctypes.c_uint32]),
@@ -189,6 +200,12 @@ class Lattice:
             raise ValueError("pairs must have an even number of entries")
         _check(_lib.lbm_set_barrier(self._h, _ptr(p), p.size // 2))
 
+    def draw_shape(self, shape):
+        """draw_shape (lbm.rs:1337-1339): upload a shape's (index, value) pairs."""
+        from .shapes import points_vector
+        if not shape.is_empty():
+            self.draw_points(points_vector(shape, self.x))
+
     def draw_mask(self, mask):
         """Upload a whole [y, x] mask (nonzero = solid)."""
         m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
@@ -266,11 +283,29 @@ class Lattice:
         self.summary_stat = stat
 
     def summary(self, stat=None):
-        """Raw values of a SummaryStat (momenta for Ux/Uy, like ux.wgsl:41 / uy.wgsl:41)."""
+        """The reference's summary output for a SummaryStat (summary_stats/*.wgsl):
+        curl, raw momenta for Ux / Uy, the display-scaled rho and speed."""
         stat = self.summary_stat if stat is None else stat
-        name = {SummaryStat.Curl: "curl", SummaryStat.Ux: "jx", SummaryStat.Uy: "jy", SummaryStat.Rho: "rho",
-                SummaryStat.Speed: "speed"}[stat]
-        return self.field(name)
+        out = np.zeros(self.x * self.y, np.float32)
+        _check(_lib.lbm_summary(self._h, int(stat), _ptr(out)))
+        return out.reshape(self.y, self.x)
+
+    def set_color_map(self, cmap):
+        self.color_map = cmap
+
+    def render(self, width=None, height=None, stat=None, cmap=None, rgba=False, srgb=False):
+        """Headless frame of the current state (lbm_render): [height, width, 3]
+        float32 RGB, or [height, width, 4] uint8 with rgba=True."""
+        stat = self.summary_stat if stat is None else stat
+        cmap = getattr(self, "color_map", ColorMap.Jet) if cmap is None else cmap
+        w, h = int(width or self.x), int(height or self.y)
+        if rgba:
+            out = np.zeros(w * h * 4, np.uint8)
+            _check(_lib.lbm_render(self._h, int(stat), int(cmap), w, h, None, _ptr(out), 1 if srgb else 0))
+            return out.reshape(h, w, 4)
+        out = np.zeros(w * h * 3, np.float32)
+        _check(_lib.lbm_render(self._h, int(stat), int(cmap), w, h, _ptr(out), None, 0))
+        return out.reshape(h, w, 3)
 
     def populations(self, f64=False):
         out = np.zeros(9 * self.x * self.y, np.float64 if f64 else np.float32)

@@ -53,6 +53,11 @@ class Batch:
         _check(self._lib.lbm_batch_info(self._h, ctypes.byref(c), ctypes.byref(cells), ctypes.byref(steps)))
         return c.value, cells.value, steps.value
 
+    def stream(self):
+        v = ctypes.c_void_p()
+        _check(self._lib.lbm_batch_get_stream(self._h, ctypes.byref(v)))
+        return v.value or 0
+
     def set_mask(self, d, mask):
         m = np.ascontiguousarray(mask, dtype=np.uint8).reshape(-1)
         if m.size != int(self.nx[d]) * int(self.ny[d]):

@@ -4,10 +4,10 @@ coarse runs that apply it (include/lbm_cnn.h).
 
 The reference has no closure; this module adds one around the engine:
 
-* `fine_samples` runs a fine channel lattice and turns snapshot pairs (t,
-  t + F fine steps) into coarse training samples on the device
-  (lbm_cnn_closure_sample): features (rho, u, solid) and the loss
-  coefficients of a one-step fit of the coarse relaxation time;
+* `fine_samples` runs a fine channel lattice and turns snapshots into coarse
+  training samples on the device (lbm_cnn_closure_sample): features (rho, u,
+  solid) and the coefficients of an eddy-viscosity fit of the subgrid stress
+  that block averaging removes;
 * `ClosureNet` holds the parameters, gradients and Adam state in device
   memory (torch tensors serve only as allocations and a stream) and runs
   forward / backward / loss / update through the C ABI kernels;
@@ -150,13 +150,12 @@ class ClosureNet:
                                                            self.stream))
                 g = gx
 
-    def loss(self, z, coef, tau0, norm, grad=True):
+    def loss(self, z, coef, norm, grad=True):
         """Closure loss (a device scalar, float64) and, with grad, dL/dz."""
         N, _, H, W = z.shape
         gz = self.torch.empty_like(z) if grad else None
-        _check(self.lib.lbm_cnn_closure_loss(_p(z), _p(coef), N, H, W, float(tau0), float(norm),
-                                             _p(gz) if grad else None, _p(self.loss_scratch), _p(self.loss_out),
-                                             self.stream))
+        _check(self.lib.lbm_cnn_closure_loss(_p(z), _p(coef), N, H, W, float(norm), _p(gz) if grad else None,
+                                             _p(self.loss_scratch), _p(self.loss_out), self.stream))
         return self.loss_out, gz
 
     def adam(self, lr, b1=0.9, b2=0.999, eps=1e-8):
@@ -165,30 +164,29 @@ class ClosureNet:
                                      float(lr), b1, b2, eps, self.stream))
 
 
-def sample(lib, stream, pops_t, pops_t1, solid_f, factor, feat, coef, scratch, solid_c):
+def sample(lib, stream, pops, solid_f, factor, feat, coef, scratch, solid_c):
     hf, wf = solid_f.shape
-    _check(lib.lbm_cnn_closure_sample(_p(pops_t), _p(pops_t1), _p(solid_f), hf, wf, factor, _p(feat), _p(coef),
-                                      _p(scratch), _p(solid_c), stream))
+    _check(lib.lbm_cnn_closure_sample(_p(pops), _p(solid_f), hf, wf, factor, _p(feat), _p(coef), _p(scratch),
+                                      _p(solid_c), stream))
 
 
 def fine_samples(mask, tau, u, steps, every, factor, seed=0, noise=1e-3, start=0, storage=F32):
-    """Run a fine channel lattice with `mask` for `steps` steps and return
-    the coarse samples of every snapshot pair (t, t + factor) taken every
-    `every` steps from step `start` on: (feat [S, 4, H, W], coef [S, 3, H, W],
-    coarse solid [H, W]) as CUDA tensors."""
+    """Run a fine channel lattice with `mask` for `steps` steps and return the
+    coarse samples of the snapshots taken every `every` steps from step
+    `start` on: (feat [S, 4, H, W], coef [S, 3, H, W], coarse solid [H, W]) as
+    CUDA tensors."""
     torch = _torch()
     lib = load_library()
     ny, nx = mask.shape
     H, W = ny // factor, nx // factor
     dev = torch.device("cuda")
-    times = list(range(max(start, 0), steps - factor + 1, every))
+    times = list(range(max(start, every), steps + 1, every))
     feat = torch.empty((len(times), 4, H, W), dtype=torch.float32, device=dev)
     coef = torch.empty((len(times), 3, H, W), dtype=torch.float32, device=dev)
     solid_c = torch.empty((H, W), dtype=torch.uint8, device=dev)
     solid_f = torch.from_numpy(np.ascontiguousarray(mask, dtype=np.uint8)).to(dev)
-    pa = torch.empty((9, ny, nx), dtype=torch.float32, device=dev)
-    pb = torch.empty_like(pa)
-    scratch = torch.empty(18 * H * W, dtype=torch.float32, device=dev)
+    pops = torch.empty((9, ny, nx), dtype=torch.float32, device=dev)
+    scratch = torch.empty(6 * H * W, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream()
     with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
         lat.set_stream(stream.cuda_stream)
@@ -197,13 +195,10 @@ def fine_samples(mask, tau, u, steps, every, factor, seed=0, noise=1e-3, start=0
         lat.draw_mask(mask)
         done = 0
         for k, t in enumerate(times):
-            if t > done:
-                lat.iterate(t - done)
-            _check(lib.lbm_read_populations_device(lat.handle, _p(pa)))
-            lat.iterate(factor)
-            _check(lib.lbm_read_populations_device(lat.handle, _p(pb)))
-            done = t + factor
-            sample(lib, ctypes.c_void_p(stream.cuda_stream), pa, pb, solid_f, factor, feat[k], coef[k], scratch,
+            lat.iterate(t - done)
+            done = t
+            _check(lib.lbm_read_populations_device(lat.handle, _p(pops)))
+            sample(lib, ctypes.c_void_p(stream.cuda_stream), pops, solid_f, factor, feat[k], coef[k], scratch,
                    solid_c)
         lat.synchronize()
     return feat, coef, solid_c

@@ -469,6 +469,12 @@ int lbm_batch_info(const lbm_batch* b, uint32_t* count, uint64_t* cells, uint64_
   return LBM_OK;
 }
 
+int lbm_batch_get_stream(const lbm_batch* b, void** stream) {
+  if (!b || !stream) return bfail(LBM_ERR_ARG, "null argument");
+  *stream = (void*)b->stream;
+  return LBM_OK;
+}
+
 int lbm_batch_set_mask(lbm_batch* b, uint32_t domain, const uint8_t* mask) {
   int rc = check(b, domain);
   if (rc) return rc;

@@ -12,6 +12,8 @@
 #include "lbm_kernels.cuh"
 #include "lbm_stage.cuh"
 #include "lbm_closure.cuh"
+#include "lbm_render.cuh"
+#include "../../include/lbm_render.h"
 #include "../../include/lbm_cnn.h"
 
 using namespace lbm;
@@ -821,6 +823,85 @@ int lbm_closure_fallback_count(lbm_sim* s, uint64_t* out, int reset) {
   CK(cudaStreamSynchronize(s->stream));
   *out = v;
   return LBM_OK;
+}
+
+
+}  // extern "C"
+
+// ---- headless readout (include/lbm_render.h) ---------------------------------------
+
+namespace {
+
+int ensure_moments(lbm_sim* s) {
+  if (s->moments_valid) return LBM_OK;
+  int rc = materialise(s);
+  return rc ? rc : compute_moments(s);
+}
+
+template <class F> int with_moments(lbm_sim* s, F&& f) {
+  if (s->storage == STORE_F64)
+    return f((const double*)mom_plane(s, 0), (const double*)mom_plane(s, 1), (const double*)mom_plane(s, 2));
+  return f((const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2));
+}
+
+int frame(lbm_sim* s, int stat, int cmap, uint32_t w, uint32_t h, float* rgb_dev, uint8_t* rgba_dev, int srgb) {
+  if (stat < 0 || stat > 4 || cmap < 0 || cmap > 2) return fail(LBM_ERR_ARG, "bad statistic %d or colour map %d", stat, cmap);
+  if (w < 1 || h < 1 || h > 65535 || w > (1u << 20)) return fail(LBM_ERR_ARG, "bad frame size %ux%u", w, h);
+  int rc = ensure_moments(s);
+  if (rc) return rc;
+  dim3 grid((w + kBlockX - 1) / kBlockX, h);
+  rc = with_moments(s, [&](auto r, auto x, auto y) -> int {
+    k_frame<<<grid, kBlockX, 0, s->stream>>>(s->L, stat, cmap, r, x, y, s->mask_d, (int)w, (int)h, rgb_dev, rgba_dev,
+                                             srgb);
+    CK_LAUNCH();
+    return LBM_OK;
+  });
+  if (!rc) s->launches++;
+  return rc;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_summary(lbm_sim* s, int stat, float* out) {
+  CHECK_SIM(s);
+  if (!out || stat < 0 || stat > 4) return fail(LBM_ERR_ARG, "bad summary statistic or output");
+  int rc = ensure_moments(s);
+  if (rc) return rc;
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  rc = with_moments(s, [&](auto r, auto x, auto y) -> int {
+    k_summary<<<grid, kBlockX, 0, s->stream>>>(s->L, stat, r, x, y, s->staging_d);
+    CK_LAUNCH();
+    return LBM_OK;
+  });
+  if (rc) return rc;
+  s->launches++;
+  CK(cudaMemcpyAsync(out, s->staging_d, (size_t)s->L.nx * s->L.ny * 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_render_device(lbm_sim* s, int stat, int cmap, uint32_t width, uint32_t height, float* rgb) {
+  CHECK_SIM(s);
+  if (!rgb) return fail(LBM_ERR_ARG, "rgb is null");
+  return frame(s, stat, cmap, width, height, rgb, nullptr, 0);
+}
+
+int lbm_render(lbm_sim* s, int stat, int cmap, uint32_t width, uint32_t height, float* rgb, uint8_t* rgba, int srgb) {
+  CHECK_SIM(s);
+  if (!rgb && !rgba) return fail(LBM_ERR_ARG, "no output");
+  const size_t px = (size_t)width * height;
+  void* buf = nullptr;
+  CK(cudaMallocAsync(&buf, px * (12 + 4), s->stream));
+  float* d_rgb = (float*)buf;
+  uint8_t* d_rgba = (uint8_t*)buf + px * 12;
+  int rc = frame(s, stat, cmap, width, height, d_rgb, d_rgba, srgb);
+  if (!rc && rgb) rc = cudaMemcpyAsync(rgb, d_rgb, px * 12, cudaMemcpyDeviceToHost, s->stream) ? LBM_ERR_CUDA : 0;
+  if (!rc && rgba) rc = cudaMemcpyAsync(rgba, d_rgba, px * 4, cudaMemcpyDeviceToHost, s->stream) ? LBM_ERR_CUDA : 0;
+  cudaFreeAsync(buf, s->stream);
+  CK(cudaStreamSynchronize(s->stream));
+  return rc ? fail(LBM_ERR_CUDA, "render readback failed") : LBM_OK;
 }
 
 }  // extern "C"

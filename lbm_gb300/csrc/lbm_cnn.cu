@@ -227,13 +227,14 @@ __global__ void k_sum_partials(const float* __restrict__ partial, int nblocks, i
   else gb[i - nw] = s;
 }
 
-// ---- loss --------------------------------------------------------------------------
+// ---- loss ----------------------------------------------------------------------------
 __device__ __forceinline__ float sigmoid(float z) { return 1.0f / (1.0f + expf(-z)); }
 
+// Per cell A dt^2 - 2 B dt + C with dt = dt_max * sigmoid(z): partial sums
+// per block (f64) and, when gz is given, dL/dz scaled by inv_norm.
 __global__ void __launch_bounds__(256) k_closure_loss(const float* __restrict__ z, const float* __restrict__ coef,
-                                                      long long cells_per_image, int N, float tau0, float dt_max,
-                                                      float inv_norm, float* __restrict__ gz,
-                                                      double* __restrict__ partial) {
+                                                      long long cells_per_image, int N, float dt_max, float inv_norm,
+                                                      float* __restrict__ gz, double* __restrict__ partial) {
   __shared__ double sh[256];
   double s = 0.0;
   const long long total = cells_per_image * N;
@@ -242,9 +243,9 @@ __global__ void __launch_bounds__(256) k_closure_loss(const float* __restrict__ 
     const float* cf = coef + n * 3 * cells_per_image + c;
     const float A = cf[0], B = cf[cells_per_image], C = cf[2 * cells_per_image];
     const float sg = sigmoid(z[i]);
-    const float om = 1.0f / (tau0 + dt_max * sg);
-    s += (double)fmaf(om, fmaf(om, A, -2.0f * B), C);
-    if (gz) gz[i] = (2.0f * fmaf(om, A, -B)) * inv_norm * (-om * om) * dt_max * sg * (1.0f - sg);
+    const float dt = dt_max * sg;
+    s += (double)fmaf(dt, fmaf(dt, A, -2.0f * B), C);
+    if (gz) gz[i] = (2.0f * fmaf(dt, A, -B)) * inv_norm * dt_max * sg * (1.0f - sg);
   }
   sh[threadIdx.x] = s;
   __syncthreads();
@@ -275,86 +276,92 @@ __global__ void k_adam(float* __restrict__ p, const float* __restrict__ g, float
   p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
 }
 
-// ---- coarse-grained samples of a fine run ------------------------------------------------
-// Pass 1: block averages over the fluid fine cells of each F x F block, at t
-// and t + F, and the coarse solid flag (fewer than half the cells fluid).
-__global__ void k_coarsen(const float* __restrict__ ft, const float* __restrict__ ft1,
-                          const uint8_t* __restrict__ solid_f, int Hf, int Wf, int F, float* __restrict__ fc,
-                          float* __restrict__ gc, uint8_t* __restrict__ solid_c) {
+// ---- coarse-grained samples of a fine run ------------------------------------------
+// Pass 1, per coarse cell: Favre block averages over the fluid fine cells of
+// its F x F block -> (rho, Ux, Uy, tau_xx, tau_xy, tau_yy) planes, and the
+// coarse solid flag (fewer than half the cells fluid).
+__global__ void k_coarsen(const float* __restrict__ pops, const uint8_t* __restrict__ solid_f, int Hf, int Wf, int F,
+                          float* __restrict__ avg, uint8_t* __restrict__ solid_c) {
   const int W = Wf / F, H = Hf / F;
   const int X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
   if (X >= W) return;
   const size_t planef = (size_t)Hf * Wf, planec = (size_t)H * W, oc = (size_t)Y * W + X;
-  float sf[9], sg[9];
+  auto cell = [&](size_t o, float& rho, float& jx, float& jy) {
+    rho = jx = jy = 0.0f;
 #pragma unroll
-  for (int q = 0; q < 9; q++) sf[q] = sg[q] = 0.0f;
+    for (int q = 0; q < 9; q++) {
+      const float f = pops[q * planef + o];
+      rho += f;
+      jx += (float)lbm::cx(q) * f;
+      jy -= (float)lbm::cy(q) * f;
+    }
+  };
+  // two passes: the Favre mean, then the density-weighted spread around it
+  // (no cancellation between <rho u u> and U U)
+  float R = 0.0f, Jx = 0.0f, Jy = 0.0f;
   int nf = 0;
   for (int dy = 0; dy < F; dy++)
     for (int dx = 0; dx < F; dx++) {
       const size_t o = (size_t)(Y * F + dy) * Wf + X * F + dx;
       if (solid_f[o]) continue;
       nf++;
-#pragma unroll
-      for (int q = 0; q < 9; q++) {
-        sf[q] += ft[q * planef + o];
-        sg[q] += ft1[q * planef + o];
-      }
+      float rho, jx, jy;
+      cell(o, rho, jx, jy);
+      R += rho;
+      Jx += jx;
+      Jy += jy;
     }
-  const float inv = nf > 0 ? 1.0f / (float)nf : 0.0f;
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    fc[q * planec + oc] = sf[q] * inv;
-    gc[q * planec + oc] = sg[q] * inv;
-  }
+  const float Rs = nf > 0 ? R : 1.0f;
+  const float Ux = Jx / Rs, Uy = Jy / Rs;
+  float Sxx = 0.0f, Sxy = 0.0f, Syy = 0.0f;
+  for (int dy = 0; dy < F; dy++)
+    for (int dx = 0; dx < F; dx++) {
+      const size_t o = (size_t)(Y * F + dy) * Wf + X * F + dx;
+      if (solid_f[o]) continue;
+      float rho, jx, jy;
+      cell(o, rho, jx, jy);
+      const float vx = jx / rho - Ux, vy = jy / rho - Uy;
+      Sxx = fmaf(rho * vx, vx, Sxx);
+      Sxy = fmaf(rho * vx, vy, Sxy);
+      Syy = fmaf(rho * vy, vy, Syy);
+    }
+  avg[oc] = nf > 0 ? R / (float)nf : 0.0f;
+  avg[planec + oc] = Ux;
+  avg[2 * planec + oc] = Uy;
+  avg[3 * planec + oc] = Sxx / Rs;
+  avg[4 * planec + oc] = Sxy / Rs;
+  avg[5 * planec + oc] = Syy / Rs;
   solid_c[oc] = 2 * nf < F * F ? 1 : 0;
 }
 
-// Pass 2: features and loss coefficients of each coarse cell.
-__global__ void k_sample(const float* __restrict__ fc, const float* __restrict__ gc,
-                         const uint8_t* __restrict__ solid_c, int H, int W, float* __restrict__ feat,
-                         float* __restrict__ coef) {
+// Pass 2: features and the eddy-viscosity loss coefficients of each coarse cell.
+__global__ void k_sample(const float* __restrict__ avg, const uint8_t* __restrict__ solid_c, int H, int W,
+                         float* __restrict__ feat, float* __restrict__ coef) {
   const int X = blockIdx.x * blockDim.x + threadIdx.x, Y = blockIdx.y;
   if (X >= W) return;
   const size_t plane = (size_t)H * W, o = (size_t)Y * W + X;
+  const int xl = max(X - 1, 0), xr = min(X + 1, W - 1);
+  const int yu = Y == 0 ? H - 1 : Y - 1, yd = Y == H - 1 ? 0 : Y + 1;  // north / south rows, periodic
   const bool fluid = solid_c[o] == 0;
-  float f[9];
-#pragma unroll
-  for (int q = 0; q < 9; q++) f[q] = fc[q * plane + o];
-  float rho = 0.0f, jx = 0.0f, jy = 0.0f;
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    rho += f[q];
-    jx += (float)lbm::cx(q) * f[q];
-    jy -= (float)lbm::cy(q) * f[q];
-  }
-  const float rs = fluid ? rho : 1.0f;
-  const float ux = jx / rs, uy = jy / rs, usq = ux * ux + uy * uy;
-  bool valid = fluid && X > 0;
-  float A = 0.0f, B = 0.0f, C = 0.0f;
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    const int XN = X + lbm::cx(q);
-    int YN = Y + lbm::cy(q);
-    YN = YN < 0 ? YN + H : (YN >= H ? YN - H : YN);
-    const bool inside = XN >= 0 && XN < W;
-    const size_t on = (size_t)YN * W + (inside ? XN : X);
-    valid = valid && inside && solid_c[on] == 0;
-    const float cu = (float)lbm::cx(q) * ux - (float)lbm::cy(q) * uy;
-    const float wq = q == 4 ? 4.0f / 9.0f : ((q & 1) ? 1.0f / 9.0f : 1.0f / 36.0f);
-    const float feq = wq * rs * (1.0f + 3.0f * cu + 4.5f * cu * cu - 1.5f * usq);
-    const float aq = f[q] - feq, bq = f[q] - gc[q * plane + on];
-    A = fmaf(aq, aq, A);
-    B = fmaf(aq, bq, B);
-    C = fmaf(bq, bq, C);
-  }
+  const bool valid = fluid && X > 0 && X < W - 1 && !solid_c[(size_t)Y * W + xl] && !solid_c[(size_t)Y * W + xr] &&
+                     !solid_c[(size_t)yu * W + X] && !solid_c[(size_t)yd * W + X];
+  const float* Ux = avg + plane;
+  const float* Uy = avg + 2 * plane;
+  const float dUx_dx = 0.5f * (Ux[(size_t)Y * W + xr] - Ux[(size_t)Y * W + xl]);
+  const float dUy_dx = 0.5f * (Uy[(size_t)Y * W + xr] - Uy[(size_t)Y * W + xl]);
+  const float dUx_dy = 0.5f * (Ux[(size_t)yu * W + X] - Ux[(size_t)yd * W + X]);  // y points north
+  const float dUy_dy = 0.5f * (Uy[(size_t)yu * W + X] - Uy[(size_t)yd * W + X]);
+  const float sxx = 0.5f * (dUx_dx - dUy_dy), sxy = 0.5f * (dUx_dy + dUy_dx);
+  const float txx = avg[3 * plane + o], txy = avg[4 * plane + o], tyy = avg[5 * plane + o];
+  const float dxx = 0.5f * (txx - tyy);
   const float v = valid ? 1.0f : 0.0f;
-  feat[o] = fluid ? (rho - 1.0f) * LBM_CNN_S_RHO : 0.0f;
-  feat[plane + o] = fluid ? ux * LBM_CNN_S_U : 0.0f;
-  feat[2 * plane + o] = fluid ? uy * LBM_CNN_S_U : 0.0f;
+  feat[o] = fluid ? (avg[o] - 1.0f) * LBM_CNN_S_RHO : 0.0f;
+  feat[plane + o] = fluid ? Ux[o] * LBM_CNN_S_U : 0.0f;
+  feat[2 * plane + o] = fluid ? Uy[o] * LBM_CNN_S_U : 0.0f;
   feat[3 * plane + o] = fluid ? 0.0f : 1.0f;
-  coef[o] = v * A;
-  coef[plane + o] = v * B;
-  coef[2 * plane + o] = v * C;
+  coef[o] = v * (8.0f / 9.0f) * fmaf(sxx, sxx, sxy * sxy);
+  coef[plane + o] = v * (-4.0f / 3.0f) * fmaf(dxx, sxx, txy * sxy);
+  coef[2 * plane + o] = v * 2.0f * fmaf(dxx, dxx, txy * txy);
 }
 
 bool bad_shape(int N, int C, int H, int W) { return N < 1 || C < 1 || H < 1 || W < 1 || (long long)N * H > 65535ll * 1024; }
@@ -414,12 +421,12 @@ size_t lbm_cnn_weight_scratch_bytes(int cin, int cout) {
   return (size_t)kWBlocks * (cout * cin * 9 + cout) * sizeof(float);
 }
 
-int lbm_cnn_closure_loss(const float* z, const float* coef, int n, int h, int w, float tau0, float norm,
-                         float* grad_z, double* scratch, double* loss_out, void* stream) {
+int lbm_cnn_closure_loss(const float* z, const float* coef, int n, int h, int w, float norm, float* grad_z,
+                         double* scratch, double* loss_out, void* stream) {
   if (!z || !coef || !scratch || !loss_out) return cfail(LBM_ERR_ARG, "null pointer");
-  if (bad_shape(n, 1, h, w) || !(norm > 0.0f) || !(tau0 > 0.5f)) return cfail(LBM_ERR_ARG, "closure loss: bad argument");
+  if (bad_shape(n, 1, h, w) || !(norm > 0.0f)) return cfail(LBM_ERR_ARG, "closure loss: bad argument");
   cudaStream_t s = as_stream(stream);
-  k_closure_loss<<<kLossBlocks, 256, 0, s>>>(z, coef, (long long)h * w, n, tau0, LBM_CNN_DT_MAX, 1.0f / norm, grad_z,
+  k_closure_loss<<<kLossBlocks, 256, 0, s>>>(z, coef, (long long)h * w, n, LBM_CNN_DT_MAX, 1.0f / norm, grad_z,
                                              scratch);
   CCK(cudaGetLastError());
   k_sum_double<<<1, 32, 0, s>>>(scratch, kLossBlocks, 1.0 / (double)norm, loss_out);
@@ -437,20 +444,17 @@ int lbm_cnn_adam(float* param, const float* grad, float* m, float* v, int n, int
   return LBM_OK;
 }
 
-int lbm_cnn_closure_sample(const float* pops_t, const float* pops_t1, const uint8_t* solid_fine, int hf, int wf,
-                           int factor, float* feat, float* coef, float* scratch, uint8_t* solid_coarse,
-                           void* stream) {
-  if (!pops_t || !pops_t1 || !solid_fine || !feat || !coef || !scratch || !solid_coarse)
-    return cfail(LBM_ERR_ARG, "null pointer");
-  if (factor < 1 || hf < factor || wf < factor || hf > 65535 * factor) return cfail(LBM_ERR_ARG, "closure sample: bad shape");
+int lbm_cnn_closure_sample(const float* pops, const uint8_t* solid_fine, int hf, int wf, int factor, float* feat,
+                           float* coef, float* scratch, uint8_t* solid_coarse, void* stream) {
+  if (!pops || !solid_fine || !feat || !coef || !scratch || !solid_coarse) return cfail(LBM_ERR_ARG, "null pointer");
+  if (factor < 1 || hf < 3 * factor || wf < 3 * factor || hf > 65535 * factor)
+    return cfail(LBM_ERR_ARG, "closure sample: bad shape");
   const int H = hf / factor, W = wf / factor;
-  const size_t plane = (size_t)H * W;
   cudaStream_t s = as_stream(stream);
   dim3 grid((W + kRow - 1) / kRow, H);
-  k_coarsen<<<grid, kRow, 0, s>>>(pops_t, pops_t1, solid_fine, hf, wf, factor, scratch, scratch + 9 * plane,
-                                  solid_coarse);
+  k_coarsen<<<grid, kRow, 0, s>>>(pops, solid_fine, hf, wf, factor, scratch, solid_coarse);
   CCK(cudaGetLastError());
-  k_sample<<<grid, kRow, 0, s>>>(scratch, scratch + 9 * plane, solid_coarse, H, W, feat, coef);
+  k_sample<<<grid, kRow, 0, s>>>(scratch, solid_coarse, H, W, feat, coef);
   CCK(cudaGetLastError());
   return LBM_OK;
 }

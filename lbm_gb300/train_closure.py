@@ -6,8 +6,8 @@
 
 Data: `--train` seeded random-circle layouts (radii 8-40 fine cells, ~10 %
 solid, none within 64 cells of the inlet) run on the fine grid for `--steps`
-steps at tau / u; every `--every` steps a snapshot pair (t, t + F) becomes a
-coarse training sample on the device.  Training: Adam on minibatches of
+steps at tau / u; every `--every` steps a snapshot becomes a coarse training
+sample on the device (features and the subgrid-stress fit coefficients).  Training: Adam on minibatches of
 `--batch` snapshots with the engine's own forward / backward kernels.
 Evaluation on `--test` held-out layouts: time-averaged velocity of the second
 half of each run, fine (block-averaged to the coarse grid) against coarse
@@ -152,7 +152,7 @@ def main(argv=None):
         fb, cb = feat.index_select(0, it_t), coef.index_select(0, it_t)
         lr = a.lr * (0.1 ** (it / max(a.iters, 1)))  # exponential decay to lr / 10
         z = net.forward(fb)
-        L, gz = net.loss(z, cb, tau_c, float(norms[idx].sum()))
+        L, gz = net.loss(z, cb, float(norms[idx].sum()))
         net.backward(gz)
         net.adam(lr)
         if it % max(a.iters // 20, 1) == 0 or it == a.iters - 1:
@@ -161,13 +161,12 @@ def main(argv=None):
     rep["train_seconds"] = time.perf_counter() - t0
     rep["loss_history"] = hist
     params = net.numpy()
-    # loss of the untrained baseline choices on the training data: delta_tau = 0 (plain coarse BGK)
-    with torch.no_grad():
-        zero_z = torch.full((min(S, 64), 1) + tuple(feat.shape[2:]), -30.0, device=feat.device)
-        L0, _ = net.loss(zero_z, coef[:zero_z.shape[0]], tau_c, float(norms[:zero_z.shape[0]].sum()), grad=False)
-        z = net.forward(feat[:zero_z.shape[0]])
-        L1, _ = net.loss(z, coef[:zero_z.shape[0]], tau_c, float(norms[:zero_z.shape[0]].sum()), grad=False)
+    # loss with delta_tau = 0 (plain coarse BGK: the whole subgrid stress unexplained) and trained
+    k = min(S, 64)
+    zero_z = torch.full((k, 1) + tuple(feat.shape[2:]), -30.0, device=feat.device)
+    L0, _ = net.loss(zero_z, coef[:k], float(norms[:k].sum()), grad=False)
     rep["loss_plain"] = float(L0.item())
+    L1, _ = net.loss(net.forward(feat[:k]), coef[:k], float(norms[:k].sum()), grad=False)
     rep["loss_trained"] = float(L1.item())
     del feat, coef
 

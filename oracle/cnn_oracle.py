@@ -16,13 +16,16 @@ Conventions shared with the CUDA kernels (lbm_gb300/csrc/lbm_cnn.cu):
 * input features of a cell: (rho - 1) * S_RHO, ux * S_U, uy * S_U, solid
   (1 / 0); output z -> delta tau = DT_MAX * sigmoid(z);
 * a training sample is a coarse cell of a fine run block-averaged by a
-  factor F: a_i = f_i - feq_i(rho, u) of the coarse populations at t,
-  b_i = f_i(x, t) - f_i(x + c_i, t + F fine steps); with
-  omega = 1 / (tau0 + delta tau) the cell's loss is sum_i (omega a_i - b_i)^2
-  = omega^2 A - 2 omega B + C (A = sum a^2, B = sum a b, C = sum b^2): how
-  far one coarse BGK collision at that omega is from the fine run's own
-  evolution.  Cells next to a solid, on the inlet column or whose
-  downstream neighbour leaves the grid carry no sample (A = B = C = 0).
+  factor F (Favre averages over the block's fluid cells): the subgrid stress
+  tau_ij = <rho u_i u_j> / <rho> - U_i U_j of the fine velocity around the
+  coarse velocity U, against the coarse strain rate S_ij of U (central
+  differences, per coarse cell).  An eddy viscosity nu_t = delta_tau / 3 (the
+  BGK viscosity (tau - 1/2) / 3) models the deviatoric stress as
+  -2 nu_t S^d; the cell's loss is the squared Frobenius residual
+  |tau^d + (2/3) delta_tau S^d|^2 = A dt^2 - 2 B dt + C with
+  A = (4/9)|S^d|^2, B = -(2/3) <tau^d, S^d>, C = |tau^d|^2.  Cells that are
+  solid, on the first or last column or next to a solid carry no sample
+  (A = B = C = 0).
 """
 import numpy as np
 
@@ -107,15 +110,14 @@ def delta_tau(z):
     return DT_MAX / (1.0 + np.exp(-z))
 
 
-def loss(z, coef, tau0, norm):
-    """Sum over cells of omega^2 A - 2 omega B + C, divided by norm; and its
-    gradient w.r.t. z.  coef is [N, 3, H, W]."""
+def loss(z, coef, norm):
+    """Sum over cells of A dt^2 - 2 B dt + C (dt = delta_tau(z)), divided by
+    norm; and its gradient w.r.t. z.  coef is [N, 3, H, W]."""
     s = 1.0 / (1.0 + np.exp(-z[:, 0]))
-    om = 1.0 / (tau0 + DT_MAX * s)
+    dt = DT_MAX * s
     A, B, C = coef[:, 0], coef[:, 1], coef[:, 2]
-    L = (om * om * A - 2.0 * om * B + C).sum() / norm
-    dl_dom = (2.0 * om * A - 2.0 * B) / norm
-    gz = dl_dom * (-om * om) * DT_MAX * s * (1.0 - s)
+    L = (dt * dt * A - 2.0 * dt * B + C).sum() / norm
+    gz = (2.0 * (dt * A - B) / norm) * DT_MAX * s * (1.0 - s)
     return L, gz[:, None]
 
 
@@ -150,43 +152,52 @@ def moments(f):
 
 
 def coarsen(pops, solid, F):
-    """Block-average fine populations [9, Hf, Wf] over the fluid cells of each
-    F x F block; a coarse cell is solid when fewer than half its fine cells
-    are fluid.  Returns (coarse pops [9, H, W], coarse solid [H, W])."""
+    """Favre block averages of a fine state [9, Hf, Wf] over the fluid cells
+    of each F x F block: (rho, Ux, Uy, tau_xx, tau_xy, tau_yy, coarse solid),
+    a block being solid when fewer than half its cells are fluid."""
     Hf, Wf = solid.shape
     H, W = Hf // F, Wf // F
-    fl = (solid[:H * F, :W * F] == 0).astype(np.float64).reshape(H, F, W, F)
-    n = fl.sum(axis=(1, 3))
-    p = pops[:, :H * F, :W * F].reshape(9, H, F, W, F)
-    s = (p * fl[None]).sum(axis=(2, 4))
-    out = np.where(n > 0, s / np.maximum(n, 1), 0.0)
-    return out, (2 * n < F * F).astype(np.uint8)
+    rho, jx, jy = moments(pops[:, :H * F, :W * F])
+    fl = (solid[:H * F, :W * F] == 0).astype(np.float64)
+    r = np.where(fl > 0, rho, 1.0)
+    ux, uy = jx / r, jy / r
+
+    def bsum(a):
+        return (a * fl).reshape(H, F, W, F).sum(axis=(1, 3))
+
+    n = bsum(np.ones_like(rho))
+    R = bsum(rho)
+    Rs = np.where(n > 0, R, 1.0)
+    Ux, Uy = bsum(jx) / Rs, bsum(jy) / Rs
+    txx = bsum(rho * ux * ux) / Rs - Ux * Ux
+    txy = bsum(rho * ux * uy) / Rs - Ux * Uy
+    tyy = bsum(rho * uy * uy) / Rs - Uy * Uy
+    return R / np.maximum(n, 1), Ux, Uy, txx, txy, tyy, (2 * n < F * F).astype(np.uint8)
 
 
-def sample(pops_t, pops_t1, solid_f, F):
-    """Features [4, H, W] and loss coefficients [3, H, W] of one snapshot pair."""
-    f, sc = coarsen(pops_t, solid_f, F)
-    g, _ = coarsen(pops_t1, solid_f, F)
+def sample(pops, solid_f, F):
+    """Features [4, H, W] and loss coefficients [3, H, W] of one fine snapshot."""
+    rho, Ux, Uy, txx, txy, tyy, sc = coarsen(pops, solid_f, F)
     H, W = sc.shape
-    rho, jx, jy = moments(f)
     fluid = sc == 0
-    rs = np.where(fluid, rho, 1.0)
-    ux, uy = jx / rs, jy / rs
-    feq = equilibrium(rs, ux, uy)
-    a = f - feq
-    b = np.empty_like(f)
-    valid = fluid.copy()
+    up = np.roll(np.arange(H), 1)   # row - 1 (north), periodic
+    dn = np.roll(np.arange(H), -1)  # row + 1 (south)
+    xl = np.clip(np.arange(W) - 1, 0, W - 1)
+    xr = np.clip(np.arange(W) + 1, 0, W - 1)
+    dUx_dx = (Ux[:, xr] - Ux[:, xl]) / 2
+    dUy_dx = (Uy[:, xr] - Uy[:, xl]) / 2
+    dUx_dy = (Ux[up] - Ux[dn]) / 2  # y points north: rows count southwards
+    dUy_dy = (Uy[up] - Uy[dn]) / 2
+    sxx = (dUx_dx - dUy_dy) / 2  # deviatoric parts
+    sxy = (dUx_dy + dUy_dx) / 2
+    dxx = (txx - tyy) / 2
+    valid = fluid & fluid[:, xl] & fluid[:, xr] & fluid[up] & fluid[dn]
     valid[:, 0] = False
-    yy, xx = np.mgrid[0:H, 0:W]
-    for q in range(9):
-        X = xx + CX[q]
-        Y = (yy + CY[q]) % H
-        inside = (X >= 0) & (X < W)
-        Xc = np.clip(X, 0, W - 1)
-        b[q] = f[q] - g[q][Y, Xc]
-        valid &= inside & (sc[Y, Xc] == 0)
-    feat = np.stack([np.where(fluid, (rho - 1.0) * S_RHO, 0.0), np.where(fluid, ux * S_U, 0.0),
-                     np.where(fluid, uy * S_U, 0.0), sc.astype(np.float64)])
+    valid[:, -1] = False
     v = valid.astype(np.float64)
-    coef = np.stack([v * (a * a).sum(0), v * (a * b).sum(0), v * (b * b).sum(0)])
-    return feat, coef
+    A = v * (4.0 / 9.0) * 2 * (sxx * sxx + sxy * sxy)
+    B = v * -(2.0 / 3.0) * 2 * (dxx * sxx + txy * sxy)
+    C = v * 2 * (dxx * dxx + txy * txy)
+    feat = np.stack([np.where(fluid, (rho - 1.0) * S_RHO, 0.0), np.where(fluid, Ux * S_U, 0.0),
+                     np.where(fluid, Uy * S_U, 0.0), sc.astype(np.float64)])
+    return feat, np.stack([A, B, C])

@@ -199,6 +199,7 @@ def ref_lib():
         L.ref_get_state.argtypes = [ctypes.c_void_p, _c_f32p, _c_f32p, _c_f32p, _c_f32p]
         L.ref_get_sets.argtypes = [ctypes.c_void_p, _c_f32p, _c_f32p]
         L.ref_summary.argtypes = [ctypes.c_void_p, ctypes.c_int, _c_f32p]
+        L.ref_color_map.argtypes = [ctypes.c_void_p, ctypes.c_int, _c_f32p]
         _ref = L
     return _ref
 
@@ -263,3 +264,9 @@ class RefShaders:
         out = np.zeros(self.n, np.float32)
         ref_lib().ref_summary(self.h, stat, _ptr(out, _c_f32p))
         return out.reshape(self.ny, self.nx)
+
+    def color_map(self, cmap):
+        """Colours of the current output buffer (after summary()), [ny, nx, 3]."""
+        out = np.zeros(3 * self.n, np.float32)
+        ref_lib().ref_color_map(self.h, cmap, _ptr(out, _c_f32p))
+        return out.reshape(self.ny, self.nx, 3)

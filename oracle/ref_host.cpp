@@ -209,4 +209,27 @@ void ref_summary(ref_sim* h, int stat, float* out) {
   std::memcpy(out, s->output.data(), s->N * 4);
 }
 
+// Colour map of the current output buffer (lbm.rs:1299-1335; ColorMap order
+// 0 inferno, 1 viridis, 2 jet): rgb receives N * 3 floats.
+void ref_color_map(ref_sim* h, int cmap, float* rgb) {
+  RefLBM* s = (RefLBM*)h;
+  std::vector<wgsl::vec3f> colors(s->N);
+#define CMAP(ns)                                                        \
+  ns::colors = bind(colors); ns::value = bind(s->output);               \
+  ns::barrier = bind(s->barrier); ns::size = s->N;                      \
+  dispatch(s, ns::entry);
+  switch (cmap) {
+    case 0: { CMAP(cmap_inferno) break; }
+    case 1: { CMAP(cmap_viridis) break; }
+    case 2: { CMAP(cmap_jet) break; }
+    default: return;
+  }
+#undef CMAP
+  for (uint32_t i = 0; i < s->N; i++) {
+    rgb[3 * i] = colors[i].x;
+    rgb[3 * i + 1] = colors[i].y;
+    rgb[3 * i + 2] = colors[i].z;
+  }
+}
+
 }  // extern "C"

@@ -75,49 +75,62 @@ def test_backward_matches_finite_differences():
 
 
 def test_closure_loss_gradient_and_minimum():
+    """Stresses generated by an eddy viscosity dt / 3 plus noise: the loss is the
+    squared residual, its gradient matches finite differences, and its
+    minimum over delta tau is the generating value."""
     rng = np.random.default_rng(4)
     z = rng.normal(size=(2, 1, 4, 5))
-    a = rng.normal(size=(9, 2, 4, 5))
-    om_true = 1.0 / (0.51 + 0.05)
-    b = om_true * a + 1e-3 * rng.normal(size=a.shape)
-    coef = np.stack([(a * a).sum(0), (a * b).sum(0), (b * b).sum(0)], axis=1)
-    L, gz = C.loss(z, coef, 0.51, 7.0)
-    s = 1 / (1 + np.exp(-z[:, 0]))
-    om = 1 / (0.51 + C.DT_MAX * s)
-    direct = ((om[None] * a - b) ** 2).sum() / 7.0
-    assert L == pytest.approx(direct, rel=1e-12)
+    sxx, sxy = rng.normal(size=(2, 2, 4, 5)) * 1e-2
+    dt_true = 0.05
+    dxx = -(2 / 3) * dt_true * sxx + 1e-6 * rng.normal(size=sxx.shape)
+    txy = -(2 / 3) * dt_true * sxy + 1e-6 * rng.normal(size=sxy.shape)
+    coef = np.stack([(8 / 9) * (sxx ** 2 + sxy ** 2), -(4 / 3) * (dxx * sxx + txy * sxy),
+                     2 * (dxx ** 2 + txy ** 2)], axis=1)
+    L, gz = C.loss(z, coef, 7.0)
+    dt = C.delta_tau(z[:, 0])
+    direct = 2 * (((dxx + (2 / 3) * dt * sxx) ** 2) + ((txy + (2 / 3) * dt * sxy) ** 2)).sum() / 7.0
+    assert L == pytest.approx(direct, rel=1e-9)
     eps = 1e-6
     i = (1, 0, 2, 3)
     z2 = z.copy()
     z2[i] += eps
-    lp = C.loss(z2, coef, 0.51, 7.0)[0]
+    lp = C.loss(z2, coef, 7.0)[0]
     z2[i] -= 2 * eps
-    assert gz[i] == pytest.approx((lp - C.loss(z2, coef, 0.51, 7.0)[0]) / (2 * eps), rel=1e-6)
-    # the loss of one cell is smallest at the delta tau that generated b
+    assert gz[i] == pytest.approx((lp - C.loss(z2, coef, 7.0)[0]) / (2 * eps), rel=1e-6)
     zs = np.linspace(-6, 3, 9001)
     one = coef[:1, :, :1, :1]
-    losses = [C.loss(np.full((1, 1, 1, 1), v), one, 0.51, 1.0)[0] for v in zs]
-    assert C.delta_tau(zs[int(np.argmin(losses))]) == pytest.approx(0.05, abs=1e-3)
+    losses = [C.loss(np.full((1, 1, 1, 1), v), one, 1.0)[0] for v in zs]
+    assert C.delta_tau(zs[int(np.argmin(losses))]) == pytest.approx(dt_true, abs=1e-3)
 
 
-def test_sample_of_an_equilibrium_state_has_no_nonequilibrium_part():
+def test_sample_of_a_uniform_flow_and_of_a_shear_flow():
     H, W, F = 8, 12, 4
     rng = np.random.default_rng(5)
     rho = 1 + 0.01 * rng.random((H * F, W * F))
-    ux = 0.05 + 0.0 * rho
-    uy = 0.0 * rho
-    f = C.equilibrium(rho, ux, uy)
     solid = np.zeros((H * F, W * F), np.uint8)
     solid[8:16, 20:28] = 1  # coarse blocks (2..3, 5..6)
     solid[17, 3] = 1  # one cell of sixteen: the block stays fluid
-    feat, coef = C.sample(f, f, solid, F)
-    fc, sc = C.coarsen(f, solid, F)
+    # uniform flow: no strain, no subgrid stress
+    f = C.equilibrium(rho, 0.05 + 0 * rho, 0 * rho)
+    feat, coef = C.sample(f, solid, F)
+    sc = C.coarsen(f, solid, F)[-1]
     assert sc[2:4, 5:7].all() and sc.sum() == 4
-    rc, jx, _ = C.moments(fc)
-    # block averages of equilibria are not equilibria of the averages, but close
-    assert np.abs(coef[0]).max() < 1e-8
-    assert feat[1][sc == 0] == pytest.approx(jx[sc == 0] / rc[sc == 0] * C.S_U, rel=1e-12)
-    assert (coef[:, :, 0] == 0).all()  # inlet column carries no sample
+    assert np.abs(coef).max() < 1e-14
+    assert feat[1][sc == 0] == pytest.approx(0.05 * C.S_U, rel=1e-12)
+    assert (coef[:, :, 0] == 0).all() and (coef[:, :, -1] == 0).all()
+    # linear shear ux = g * row: Favre averages of a linear profile carry a
+    # subgrid variance g^2 (F^2 - 1) / 12 in xx only, the strain is (g F) / 2 in xy
+    g = 1e-3
+    rows = np.arange(H * F)[:, None] + 0 * rho
+    f = C.equilibrium(1.0 + 0 * rho, g * rows, 0 * rho)
+    _, Ux, _, txx, txy, tyy, _ = C.coarsen(f, np.zeros_like(solid), F)
+    assert txx == pytest.approx(g * g * (F * F - 1) / 12, rel=1e-9)
+    assert np.abs(txy).max() < 1e-15 and np.abs(tyy).max() < 1e-15
+    feat, coef = C.sample(f, np.zeros_like(solid), F)
+    inner = coef[:, 2:-2, 2:-2]
+    sxy = -g * F / 2  # dUx/dy with y pointing north (rows southwards)
+    assert inner[0] == pytest.approx((8 / 9) * sxy * sxy, rel=1e-9)
+    assert inner[1] == pytest.approx(0.0, abs=1e-18)  # a normal stress against a shear: no projection
 
 
 def test_bf16_rounding_matches_torch():

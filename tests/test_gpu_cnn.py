@@ -64,14 +64,16 @@ def test_gpu_closure_loss_and_full_gradient(lbm, torch_cuda):
     rng = np.random.default_rng(2)
     N, H, W = 3, 17, 40
     feat = (rng.normal(size=(N, 4, H, W)) * 0.5).astype(np.float32)
-    a = rng.normal(size=(9, N, H, W)) * 1e-3
-    b = 1.6 * a + 1e-4 * rng.normal(size=a.shape)
-    coef = np.stack([(a * a).sum(0), (a * b).sum(0), (b * b).sum(0)], axis=1).astype(np.float32)
+    sxx, sxy = rng.normal(size=(2, N, H, W)) * 1e-2
+    dxx = -0.02 * sxx + 1e-4 * rng.normal(size=sxx.shape)
+    txy = -0.02 * sxy + 1e-4 * rng.normal(size=sxy.shape)
+    coef = np.stack([(8 / 9) * (sxx ** 2 + sxy ** 2), -(4 / 3) * (dxx * sxx + txy * sxy),
+                     2 * (dxx ** 2 + txy ** 2)], axis=1).astype(np.float32)
     norm = float(coef[:, 2].sum())
     z = net.forward(torch.from_numpy(feat).cuda())
-    L, gz = net.loss(z, torch.from_numpy(coef).cuda(), 0.505, norm)
+    L, gz = net.loss(z, torch.from_numpy(coef).cuda(), norm)
     acts = C.forward(ps, feat.astype(np.float64))
-    L64, gz64 = C.loss(acts[-1], coef.astype(np.float64), 0.505, norm)
+    L64, gz64 = C.loss(acts[-1], coef.astype(np.float64), norm)
     assert float(L.item()) == pytest.approx(L64, rel=1e-5)
     close(gz.cpu().numpy(), gz64, 1e-4)
     net.backward(gz)
@@ -99,29 +101,24 @@ def test_gpu_adam_matches_oracle(lbm, torch_cuda):
 
 
 def test_gpu_closure_samples_match_oracle(lbm, torch_cuda):
-    """Samples of a real fine run (96 x 64 channel, circle) at two snapshot pairs."""
-    torch = torch_cuda
+    """Samples of a real fine run (96 x 64 channel, circle) at three snapshots."""
     from lbm_gb300 import closure, geometry
     mask = geometry.single_circle(96, 64, 30, 31.5, 7)
-    feat, coef, solid_c = closure.fine_samples(mask, 0.55, 0.06, 48, 20, 4, seed=1)
+    feat, coef, solid_c = closure.fine_samples(mask, 0.55, 0.06, 60, 20, 4, seed=1)
     with lbm.Lattice(96, 64, 1.0 / 0.55, lbm.EDGE_CHANNEL, lbm.F32) as lat:
         lat.set_inlet_velocity(0.06)
         lat.init_equilibrium(1.0, 0.06, 0.0, 1e-3, 1)
         lat.draw_mask(mask)
-        done = 0
-        for k, t in enumerate([0, 20, 40]):
-            lat.iterate(t - done) if t > done else None
-            pa = lat.populations().astype(np.float64)
-            lat.iterate(4)
-            pb = lat.populations().astype(np.float64)
-            done = t + 4
-            f64, c64 = C.sample(pa, pb, mask, 4)
+        for k in range(3):
+            lat.iterate(20)
+            pops = lat.populations().astype(np.float64)
+            f64, c64 = C.sample(pops, mask, 4)
             close(feat[k].cpu().numpy(), f64, 1e-5)
-            # A, B, C are sums of squares of differences of O(0.1) f32 values:
-            # their f32 error is ~1e-7 of the populations' size squared
+            # the stresses are differences of O(u^2) f32 products (subgrid
+            # variances ~1e-6 of u^2 ~ 4e-3): f32 leaves ~1e-3 relative on them
             for j in range(3):
-                close(coef[k, j].cpu().numpy(), c64[j], 2e-3, atol=1e-12)
-    np.testing.assert_array_equal(solid_c.cpu().numpy(), C.coarsen(pa, mask, 4)[1])
+                close(coef[k, j].cpu().numpy(), c64[j], 5e-3, atol=1e-16)
+    np.testing.assert_array_equal(solid_c.cpu().numpy(), C.coarsen(pops, mask, 4)[-1])
 
 
 def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda):
