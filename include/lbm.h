@@ -200,6 +200,19 @@ int lbm_conservation(lbm_sim* sim, double out[3]);
 int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy, const uint8_t* solid, uint32_t nx,
                              uint32_t ny, uint32_t pitch, double* out, void* stream);
 
+/* Halo rows for a lattice split into y-slabs across devices (no counterpart
+ * in the reference, which runs one lattice on one adapter).  Copies rows
+ * y .. y + nrows - 1 of the moving-population planes selected by slot_mask
+ * (bit s = slot s: 0 nw, 1 n, 2 ne, 3 w, 4 e, 5 sw, 6 s, 7 se) of the state
+ * the next step pulls from, in the storage's own words (4, 2 or 8 bytes),
+ * planes in slot order, each nrows * nx words row-major.  on_device != 0:
+ * `out` / `in` is device memory and the copy is queued on the lattice's
+ * stream; otherwise host memory and the call synchronises. */
+int lbm_rows_read(lbm_sim* sim, uint32_t y, uint32_t nrows, uint32_t slot_mask, void* out, int on_device);
+int lbm_rows_write(lbm_sim* sim, uint32_t y, uint32_t nrows, uint32_t slot_mask, const void* in, int on_device);
+/* Bytes per stored population (4 f32, 2 f16 / bf16, 8 f64). */
+int lbm_storage_bytes(const lbm_sim* sim, uint32_t* bytes);
+
 #ifdef __cplusplus
 }
 #endif

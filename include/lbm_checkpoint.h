@@ -1,0 +1,45 @@
+/* Checkpoint and resume of a lattice.
+ *
+ * The reference keeps no checkpoints (its state lives in GPU buffers for the
+ * life of the page, lbm.rs:32-98).  A checkpoint here holds the exact device
+ * state, so that a lattice loaded from it continues bit for bit as the saved
+ * one would have: both buffer sets and the rest plane in their storage words
+ * (f32, f64, or the 16-bit f - w words), which buffer is current and whether
+ * it is materialised, the step count, omega, the inlet velocity, the solid
+ * mask and, when the learned closure is on, its per-cell records.
+ *
+ * Layout (little-endian): a 96-byte header
+ *   char magic[8] = "LBMGB3CK"; u32 version = 1, nx, ny; i32 edge, storage;
+ *   f32 omega, u_in, drift; u64 steps; u32 cur, materialised, closure,
+ *   elem_bytes; u64 payload_bytes; u32 crc32 (of the payload, zlib's CRC-32);
+ *   u32 reserved[5]
+ * then the payload, every plane dense row-major (nx * ny, row 0 first):
+ *   mask (u8 per cell); buffer 0 (8 planes, direction slots 0..3 = nw, n, ne,
+ *   w and 4..7 = e, sw, s, se); buffer 1 (8 planes); rest plane; closure
+ *   records (2 x binary16 per cell) when closure != 0.
+ * A checkpoint loads into a lattice of the same size, edge mode and storage. */
+#ifndef LBM_GB300_CHECKPOINT_H
+#define LBM_GB300_CHECKPOINT_H
+
+#include <stddef.h>
+
+#include "lbm.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+int lbm_checkpoint_size(const lbm_sim* sim, size_t* bytes);
+/* Into a caller buffer of at least lbm_checkpoint_size bytes (synchronises). */
+int lbm_checkpoint_save(lbm_sim* sim, void* buf, size_t len);
+/* From a buffer; LBM_ERR_ARG on a size / mode mismatch or a CRC error. */
+int lbm_checkpoint_load(lbm_sim* sim, const void* buf, size_t len);
+/* The same through a file. */
+int lbm_checkpoint_write(lbm_sim* sim, const char* path);
+int lbm_checkpoint_read(lbm_sim* sim, const char* path);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_GB300_CHECKPOINT_H */

@@ -90,11 +90,20 @@ _SIGS = [
     ("lbm_read_force", ctypes.c_int, [_P, _P]),
     ("lbm_conservation_noalloc", ctypes.c_int, [_P, _P, _P, _P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32,
                                                 _P, _P]),
+    ("lbm_rows_read", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_int]),
+    ("lbm_rows_write", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _P, ctypes.c_int]),
+    ("lbm_storage_bytes", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint32)]),
     # include/lbm_render.h
     ("lbm_summary", ctypes.c_int, [_P, ctypes.c_int, _P]),
     ("lbm_render", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, _P, _P,
                                   ctypes.c_int]),
     ("lbm_render_device", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, _P]),
+    # include/lbm_checkpoint.h
+    ("lbm_checkpoint_size", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    ("lbm_checkpoint_save", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    ("lbm_checkpoint_load", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
+    ("lbm_checkpoint_write", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("lbm_checkpoint_read", ctypes.c_int, [_P, ctypes.c_char_p]),
     # include/lbm_cnn.h
     ("lbm_cnn_conv_forward", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P,
                                             ctypes.c_int, ctypes.c_int, _P, _P]),
@@ -298,7 +307,8 @@ class Lattice:
         float32 RGB, or [height, width, 4] uint8 with rgba=True."""
         stat = self.summary_stat if stat is None else stat
         cmap = getattr(self, "color_map", ColorMap.Jet) if cmap is None else cmap
-        w, h = int(width or self.x), int(height or self.y)
+        w = self.x if width is None else int(width)
+        h = self.y if height is None else int(height)
         if rgba:
             out = np.zeros(w * h * 4, np.uint8)
             _check(_lib.lbm_render(self._h, int(stat), int(cmap), w, h, None, _ptr(out), 1 if srgb else 0))
@@ -330,6 +340,45 @@ class Lattice:
         out = np.zeros(3, np.float64)
         _check(_lib.lbm_conservation(self._h, _ptr(out)))
         return out
+
+    # -- halo rows (y-slab decomposition) ------------------------------------------
+    @property
+    def storage_dtype(self):
+        return {F32: np.float32, F16: np.uint16, BF16: np.uint16, F64: np.float64}[self.storage]
+
+    def read_rows(self, y, nrows, slots):
+        """Rows y .. y+nrows-1 of the given moving-population slots of the state
+        the next step pulls from, as storage words [len(slots), nrows, x]."""
+        mask = sum(1 << s for s in slots)
+        out = np.zeros((len(slots), nrows, self.x), self.storage_dtype)
+        _check(_lib.lbm_rows_read(self._h, int(y), int(nrows), mask, _ptr(out), 0))
+        return out
+
+    def write_rows(self, y, slots, words):
+        mask = sum(1 << s for s in slots)
+        a = np.ascontiguousarray(words, dtype=self.storage_dtype)
+        if list(slots) != sorted(slots) or a.shape[0] != len(slots) or a.shape[2] != self.x:
+            raise ValueError("rows must be [len(slots) ascending, nrows, x]")
+        _check(_lib.lbm_rows_write(self._h, int(y), a.shape[1], mask, _ptr(a), 0))
+
+    # -- checkpoint / resume ------------------------------------------------------
+    def checkpoint(self):
+        """The exact device state as bytes (include/lbm_checkpoint.h layout)."""
+        n = ctypes.c_size_t()
+        _check(_lib.lbm_checkpoint_size(self._h, ctypes.byref(n)))
+        buf = np.zeros(n.value, np.uint8)
+        _check(_lib.lbm_checkpoint_save(self._h, _ptr(buf), n.value))
+        return buf.tobytes()
+
+    def restore(self, data):
+        buf = np.frombuffer(data, np.uint8)
+        _check(_lib.lbm_checkpoint_load(self._h, ctypes.c_void_p(buf.ctypes.data), buf.size))
+
+    def save(self, path):
+        _check(_lib.lbm_checkpoint_write(self._h, os.fsencode(path)))
+
+    def load(self, path):
+        _check(_lib.lbm_checkpoint_read(self._h, os.fsencode(path)))
 
     def force(self):
         """(drag, lift) on the solid cells by momentum exchange, f64."""

@@ -7,12 +7,15 @@ The reference has no closure; this module adds one around the engine:
 * `fine_samples` runs a fine channel lattice and turns snapshots into coarse
   training samples on the device (lbm_cnn_closure_sample): features (rho, u,
   solid) and the coefficients of an eddy-viscosity fit of the subgrid stress
-  that block averaging removes;
+  that block averaging removes (an a-priori target);
 * `ClosureNet` holds the parameters, gradients and Adam state in device
   memory (torch tensors serve only as allocations and a stream) and runs
   forward / backward / loss / update through the C ABI kernels;
-* `coarse_run` advances a coarse lattice, refreshing the closure every
-  `refresh` steps, and time-averages its velocity.
+* `rollout_labels` turns coarse runs at a few uniform relaxation-time
+  offsets into per-cell labels: which offset brings the coarse time-averaged
+  velocity closest to the fine run's;
+* `run_average` advances a lattice, refreshing the closure every `refresh`
+  steps, and time-averages its velocity on the device.
 
 Acoustic scaling links the grids: a coarse cell is F x F fine cells, a coarse
 step is F fine steps, the lattice velocity is unchanged and the viscosity in
@@ -204,27 +207,122 @@ def fine_samples(mask, tau, u, steps, every, factor, seed=0, noise=1e-3, start=0
     return feat, coef, solid_c
 
 
-def velocity_average(lat, steps, every, factor=1, solid=None):
-    """Advance `steps` steps and return the time average of (ux, uy) sampled
-    every `every` steps, block-averaged over the fluid cells of factor x
-    factor blocks when factor > 1 (solid gives the fine mask)."""
-    acc = None
+def _device_velocity(lat, torch, pops):
+    _check(load_library().lbm_read_populations_device(lat.handle, _p(pops)))
+    rho = pops.sum(0)
+    jx = pops[2] + pops[5] + pops[8] - pops[0] - pops[3] - pops[6]
+    jy = pops[0] + pops[1] + pops[2] - pops[6] - pops[7] - pops[8]
+    return torch.stack([jx / rho, jy / rho])
+
+
+def run_average(nx, ny, tau, u, mask, steps, every, avg_from, seed, params=None, refresh=20, drift=0.5,
+                storage=F32, noise=1e-3):
+    """Run a channel lattice; returns (time-averaged velocity [2, ny, nx] over
+    steps avg_from..steps as float64 numpy, seconds spent stepping, fallback
+    cell-steps).  With params the closure is refreshed every `refresh` steps.
+    Averaging reads stay on the device and outside the timing."""
+    import time
+    torch = _torch()
+    lib = load_library()
+    dev = torch.device("cuda")
+    pops = torch.empty((9, ny, nx), dtype=torch.float32, device=dev)
+    acc = torch.zeros((2, ny, nx), dtype=torch.float64, device=dev)
+    stream = torch.cuda.current_stream()
     n = 0
-    for _ in range(steps // every):
-        lat.iterate(every)
-        u = np.stack([lat.field("ux"), lat.field("uy")]).astype(np.float64)
-        acc = u if acc is None else acc + u
-        n += 1
-    u = acc / max(n, 1)
-    if factor > 1:
-        ny, nx = u.shape[1:]
-        fl = (solid == 0).astype(np.float64)[:ny // factor * factor, :nx // factor * factor]
-        fl = fl.reshape(ny // factor, factor, nx // factor, factor)
-        uu = u[:, :ny // factor * factor, :nx // factor * factor].reshape(2, ny // factor, factor, nx // factor,
-                                                                         factor)
-        cnt = fl.sum(axis=(1, 3))
-        u = (uu * fl[None]).sum(axis=(2, 4)) / np.maximum(cnt, 1)
-    return u
+    t_step = 0.0
+    fb = ctypes.c_uint64(0)
+    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
+        lat.set_stream(stream.cuda_stream)
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, noise, seed)
+        lat.draw_mask(mask)
+        if params is not None:
+            p = np.ascontiguousarray(params, np.float32)
+            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
+            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
+        done = 0
+        chunk = min(every, refresh) if params is not None else every
+        while done < steps:
+            k = min(chunk, steps - done)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if params is not None and done % refresh == 0:
+                _check(lib.lbm_closure_infer(lat.handle))
+            lat.iterate(k)
+            torch.cuda.synchronize()
+            t_step += time.perf_counter() - t0
+            done += k
+            if done > avg_from and done % every == 0:
+                acc += _device_velocity(lat, torch, pops).double()
+                n += 1
+        if params is not None:
+            _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
+        try:
+            lat.synchronize()
+        except LBMError:
+            pass  # a run that went non-finite shows up as non-finite averages
+    return (acc / max(n, 1)).cpu().numpy(), t_step, fb.value
+
+
+def time_run(nx, ny, tau, u, mask, steps, seed, params=None, refresh=20, drift=0.5, storage=F32, noise=1e-3,
+             warmup=40):
+    """Seconds of device time for `steps` steps (plus the closure's
+    inferences every `refresh` steps), timed with CUDA events on the
+    lattice's stream after a warm-up, with no readback in between."""
+    torch = _torch()
+    lib = load_library()
+    stream = torch.cuda.Stream()
+    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
+        lat.set_stream(stream.cuda_stream)
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, noise, seed)
+        lat.draw_mask(mask)
+        if params is not None:
+            p = np.ascontiguousarray(params, np.float32)
+            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
+            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
+
+        def run(n):
+            done = 0
+            while done < n:
+                k = min(refresh, n - done) if params is not None else n - done
+                if params is not None:
+                    _check(lib.lbm_closure_infer(lat.handle))
+                lat.iterate(k)
+                done += k
+
+        run(warmup)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        run(steps)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        try:
+            lat.synchronize()
+        except LBMError:
+            pass
+        return e0.elapsed_time(e1) * 1e-3
+
+
+def block_average(u, mask, F):
+    """Average [2, ny, nx] over the fluid cells of F x F blocks."""
+    ny, nx = mask.shape
+    fl = (mask == 0).astype(np.float64)[:ny // F * F, :nx // F * F].reshape(ny // F, F, nx // F, F)
+    uu = u[:, :ny // F * F, :nx // F * F].reshape(2, ny // F, F, nx // F, F)
+    with np.errstate(invalid="ignore"):
+        return (uu * fl[None]).sum(axis=(2, 4)) / np.maximum(fl.sum(axis=(1, 3)), 1)
+
+
+def rel_error(uc, uf, solid_c):
+    """Relative L2 error of a coarse time-averaged velocity over the fluid
+    cells off the inlet column (inf when the run went non-finite)."""
+    fl = solid_c == 0
+    fl[:, 0] = False
+    d = (uc - uf)[:, fl]
+    if not np.isfinite(d).all():
+        return float("inf")
+    return float(np.linalg.norm(d) / np.linalg.norm(uf[:, fl]))
 
 
 def coarse_solid(mask, factor):
@@ -234,44 +332,59 @@ def coarse_solid(mask, factor):
     return (2 * fl.sum(axis=(1, 3)) < factor * factor).astype(np.uint8)
 
 
-def coarse_run(mask_c, tau_c, u, steps, every, params=None, refresh=20, drift=0.5, seed=0, noise=1e-3,
-               storage=F32, average_from=0):
-    """Coarse channel run; with params, the closure is refreshed every
-    `refresh` steps.  Returns (time-averaged velocity [2, H, W] over steps
-    average_from..steps, fallback cell-steps)."""
+CANDIDATES = (0.0, 0.005, 0.01, 0.02, 0.04, 0.08)
+
+
+def _box(a, r):
+    """Mean over a (2r+1)^2 window (edges replicated)."""
+    p = np.pad(a, r, mode="edge")
+    c = np.cumsum(np.cumsum(p, 0), 1)
+    c = np.pad(c, ((1, 0), (1, 0)))
+    k = 2 * r + 1
+    return (c[k:, k:] - c[:-k, k:] - c[k:, :-k] + c[:-k, :-k]) / (k * k)
+
+
+def rollout_labels(mask_c, tau_c, u, steps_c, every_c, uf_c, seed, candidates=CANDIDATES, smooth=2):
+    """Per-cell relaxation-time labels from candidate rollouts: the coarse
+    lattice is run at each uniform delta_tau candidate, its time-averaged
+    velocity compared with the block-averaged fine one, the squared error
+    smoothed over a (2 smooth + 1)^2 window and fitted per cell by a parabola
+    in delta_tau (least squares over the candidates that stayed finite).  The
+    label is the parabola's minimum clipped to the range of those candidates
+    (the best candidate where the fit is not convex) and the weight is how much the error varies
+    across the candidates.  Returns (label [H, W], weight [H, W], errors
+    per candidate as relative L2)."""
     H, W = mask_c.shape
-    lib = load_library()
-    with Lattice(W, H, 1.0 / tau_c, EDGE_CHANNEL, storage) as lat:
-        lat.set_inlet_velocity(u)
-        lat.init_equilibrium(1.0, u, 0.0, noise, seed)
-        lat.draw_mask(mask_c)
-        if params is not None:
-            p = np.ascontiguousarray(params, np.float32)
-            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
-            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
-        done = 0
-        while done < average_from:
-            k = min(refresh, average_from - done)
-            if params is not None:
-                _check(lib.lbm_closure_infer(lat.handle))
-            lat.iterate(k)
-            done += k
-        acc = np.zeros((2, H, W))
-        n = 0
-        while done < steps:
-            k = min(refresh, every, steps - done)
-            if params is not None and done % refresh == 0:
-                _check(lib.lbm_closure_infer(lat.handle))
-            lat.iterate(k)
-            done += k
-            if done % every == 0:
-                acc += np.stack([lat.field("ux"), lat.field("uy")])
-                n += 1
-        fb = ctypes.c_uint64(0)
-        if params is not None:
-            _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
-        lat.synchronize()
-    return acc / max(n, 1), fb.value
+    errs, rels = [], []
+    for dt in candidates:
+        uc, _, _ = run_average(W, H, tau_c + dt, u, mask_c, steps_c, every_c, steps_c // 2, seed)
+        e = ((uc - uf_c) ** 2).sum(0)
+        errs.append(_box(e, smooth) if np.isfinite(e).all() else np.full((H, W), np.inf))
+        rels.append(rel_error(uc, uf_c, mask_c))
+    E = np.stack(errs)  # [K, H, W]
+    x = np.asarray(candidates, np.float64)
+    ok = np.isfinite(E).all(axis=(1, 2))
+    label = np.zeros((H, W))
+    weight = np.zeros((H, W))
+    if ok.sum() >= 1:
+        Ek, xk = E[ok], x[ok]
+        best = xk[np.argmin(Ek, axis=0)]
+        label = best.copy()
+        if ok.sum() >= 3:
+            V = np.stack([xk * xk, xk, np.ones_like(xk)], 1)  # e ~ a x^2 + b x + c
+            coef, *_ = np.linalg.lstsq(V, Ek.reshape(len(xk), -1), rcond=None)
+            a, b = coef[0].reshape(H, W), coef[1].reshape(H, W)
+            with np.errstate(divide="ignore", invalid="ignore"):
+                vert = np.clip(-b / (2 * a), xk.min(), xk.max())  # never below a candidate that diverged
+            label = np.where(a > 0, vert, best)
+        weight = Ek.max(0) - Ek.min(0)
+        if not ok.all():  # diverged candidates: low delta_tau is unsafe, weigh the choice fully
+            weight = np.maximum(weight, np.nanmax(weight))
+    fl = mask_c == 0
+    fl[:, 0] = False
+    weight = np.where(fl, weight, 0.0)
+    s = weight[fl].mean() if fl.any() and weight[fl].mean() > 0 else 1.0
+    return label, weight / s, rels
 
 
 def training_layouts(count, seed, nx, ny, rmin, rmax, fraction=0.1, clearance=64):

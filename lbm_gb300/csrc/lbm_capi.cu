@@ -14,6 +14,7 @@
 #include "lbm_closure.cuh"
 #include "lbm_render.cuh"
 #include "../../include/lbm_render.h"
+#include "../../include/lbm_checkpoint.h"
 #include "../../include/lbm_cnn.h"
 
 using namespace lbm;
@@ -902,6 +903,220 @@ int lbm_render(lbm_sim* s, int stat, int cmap, uint32_t width, uint32_t height, 
   cudaFreeAsync(buf, s->stream);
   CK(cudaStreamSynchronize(s->stream));
   return rc ? fail(LBM_ERR_CUDA, "render readback failed") : LBM_OK;
+}
+
+
+// ---- checkpoint / resume (include/lbm_checkpoint.h) ---------------------------------
+
+}  // extern "C"
+
+namespace {
+
+constexpr char kCkMagic[8] = {'L', 'B', 'M', 'G', 'B', '3', 'C', 'K'};
+constexpr uint32_t kCkVersion = 1;
+
+struct CkHeader {  // 96 bytes, little-endian, written as is
+  char magic[8];
+  uint32_t version, nx, ny;
+  int32_t edge, storage;
+  float omega, u_in, drift;
+  uint64_t steps;
+  uint32_t cur, materialised, closure, elem_bytes;
+  uint64_t payload_bytes;
+  uint32_t crc32, reserved[5];
+};
+static_assert(sizeof(CkHeader) == 96, "checkpoint header layout");
+
+// CRC-32 (IEEE 802.3 polynomial, reflected, as in zlib), table-driven.
+uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
+  static uint32_t table[256];
+  static bool init = false;
+  if (!init) {
+    for (uint32_t i = 0; i < 256; i++) {
+      uint32_t c = i;
+      for (int k = 0; k < 8; k++) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      table[i] = c;
+    }
+    init = true;
+  }
+  crc = ~crc;
+  for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+  return ~crc;
+}
+
+size_t ck_payload_bytes(const lbm_sim* s, bool closure) {
+  const size_t cells = (size_t)s->L.nx * s->L.ny;
+  return cells + (8 * 2 + 1) * cells * s->es + (closure ? cells * sizeof(__half2) : 0);
+}
+
+// Dense copies of `rows` pitched planes (element size e) between device and host.
+int copy_planes(void* host, const void* dev, size_t e, const Layout& L, int planes, bool to_host, cudaStream_t st) {
+  for (int p = 0; p < planes; p++) {
+    char* h = (char*)host + (size_t)p * L.nx * L.ny * e;
+    char* d = (char*)dev + (size_t)p * L.ps * e;
+    cudaError_t r = to_host ? cudaMemcpy2DAsync(h, (size_t)L.nx * e, d, (size_t)L.pitch * e, (size_t)L.nx * e, L.ny,
+                                                cudaMemcpyDeviceToHost, st)
+                            : cudaMemcpy2DAsync(d, (size_t)L.pitch * e, h, (size_t)L.nx * e, (size_t)L.nx * e, L.ny,
+                                                cudaMemcpyHostToDevice, st);
+    if (r != cudaSuccess) return fail(LBM_ERR_CUDA, "checkpoint copy: %s", cudaGetErrorString(r));
+  }
+  return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_checkpoint_size(const lbm_sim* s, size_t* bytes) {
+  if (!s || !bytes) return fail(LBM_ERR_ARG, "null argument");
+  *bytes = sizeof(CkHeader) + ck_payload_bytes(s, s->closure_on && s->closure_d);
+  return LBM_OK;
+}
+
+int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
+  CHECK_SIM(s);
+  const bool closure = s->closure_on && s->closure_d;
+  const size_t need = sizeof(CkHeader) + ck_payload_bytes(s, closure);
+  if (!buf || len < need) return fail(LBM_ERR_ARG, "checkpoint needs %zu bytes", need);
+  const size_t cells = (size_t)s->L.nx * s->L.ny, e = s->es;
+  CkHeader h{};
+  std::memcpy(h.magic, kCkMagic, 8);
+  h.version = kCkVersion;
+  h.nx = (uint32_t)s->L.nx;
+  h.ny = (uint32_t)s->L.ny;
+  h.edge = s->edge;
+  h.storage = s->storage;
+  h.omega = s->omega;
+  h.u_in = s->u_in;
+  h.drift = s->drift;
+  h.steps = s->steps;
+  h.cur = (uint32_t)s->cur;
+  h.materialised = s->materialised ? 1u : 0u;
+  h.closure = closure ? 1u : 0u;
+  h.elem_bytes = (uint32_t)e;
+  h.payload_bytes = need - sizeof(CkHeader);
+  uint8_t* p = (uint8_t*)buf + sizeof(CkHeader);
+  std::memcpy(p, s->mask_h.data(), cells);
+  uint8_t* q = p + cells;
+  int rc = copy_planes(q, s->f[0], e, s->L, 8, true, s->stream);
+  if (!rc) rc = copy_planes(q + 8 * cells * e, s->f[1], e, s->L, 8, true, s->stream);
+  if (!rc) rc = copy_planes(q + 16 * cells * e, s->rest, e, s->L, 1, true, s->stream);
+  if (!rc && closure) rc = copy_planes(q + 17 * cells * e, s->closure_d, sizeof(__half2), s->L, 1, true, s->stream);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s->stream));
+  h.crc32 = crc32_update(0u, p, h.payload_bytes);
+  std::memcpy(buf, &h, sizeof h);
+  return LBM_OK;
+}
+
+int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
+  CHECK_SIM(s);
+  if (!buf || len < sizeof(CkHeader)) return fail(LBM_ERR_ARG, "checkpoint too short");
+  CkHeader h;
+  std::memcpy(&h, buf, sizeof h);
+  if (std::memcmp(h.magic, kCkMagic, 8) != 0 || h.version != kCkVersion)
+    return fail(LBM_ERR_ARG, "not a version-%u lattice checkpoint", kCkVersion);
+  if ((int)h.nx != s->L.nx || (int)h.ny != s->L.ny || h.edge != s->edge || h.storage != s->storage)
+    return fail(LBM_ERR_ARG, "checkpoint is %ux%u edge %d storage %d, the lattice %dx%d edge %d storage %d", h.nx, h.ny,
+                h.edge, h.storage, s->L.nx, s->L.ny, s->edge, s->storage);
+  const bool closure = h.closure != 0;
+  if (h.elem_bytes != s->es || h.payload_bytes != ck_payload_bytes(s, closure) ||
+      len < sizeof(CkHeader) + h.payload_bytes)
+    return fail(LBM_ERR_ARG, "checkpoint size mismatch");
+  const uint8_t* p = (const uint8_t*)buf + sizeof(CkHeader);
+  if (crc32_update(0u, p, h.payload_bytes) != h.crc32) return fail(LBM_ERR_ARG, "checkpoint CRC mismatch");
+  if (closure && !s->closure_base) {
+    int rc = lbm_closure_enable(s, h.drift);
+    if (rc) return rc;
+  }
+  const size_t cells = (size_t)s->L.nx * s->L.ny, e = s->es;
+  for (size_t i = 0; i < cells; i++) s->mask_h[i] = p[i] ? 1 : 0;
+  pack_words(s, 0, s->L.ny);
+  int rc = upload_words(s, 0, s->L.ny);
+  const uint8_t* q = p + cells;
+  if (!rc) rc = copy_planes((void*)q, s->f[0], e, s->L, 8, false, s->stream);
+  if (!rc) rc = copy_planes((void*)(q + 8 * cells * e), s->f[1], e, s->L, 8, false, s->stream);
+  if (!rc) rc = copy_planes((void*)(q + 16 * cells * e), s->rest, e, s->L, 1, false, s->stream);
+  if (!rc && closure) rc = copy_planes((void*)(q + 17 * cells * e), s->closure_d, sizeof(__half2), s->L, 1, false, s->stream);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(s->stream));
+  s->omega = h.omega;
+  s->u_in = h.u_in;
+  s->drift = h.drift;
+  s->closure_on = closure;
+  s->steps = h.steps;
+  s->cur = (int)h.cur;
+  s->materialised = h.materialised != 0;
+  s->moments_valid = false;
+  return LBM_OK;
+}
+
+int lbm_checkpoint_write(lbm_sim* s, const char* path) {
+  CHECK_SIM(s);
+  if (!path) return fail(LBM_ERR_ARG, "path is null");
+  size_t n = 0;
+  lbm_checkpoint_size(s, &n);
+  std::vector<uint8_t> buf(n);
+  int rc = lbm_checkpoint_save(s, buf.data(), n);
+  if (rc) return rc;
+  FILE* f = std::fopen(path, "wb");
+  if (!f) return fail(LBM_ERR_ARG, "cannot open %s for writing", path);
+  const size_t w = std::fwrite(buf.data(), 1, n, f);
+  const int c = std::fclose(f);
+  if (w != n || c != 0) return fail(LBM_ERR_ARG, "short write to %s", path);
+  return LBM_OK;
+}
+
+int lbm_checkpoint_read(lbm_sim* s, const char* path) {
+  CHECK_SIM(s);
+  if (!path) return fail(LBM_ERR_ARG, "path is null");
+  FILE* f = std::fopen(path, "rb");
+  if (!f) return fail(LBM_ERR_ARG, "cannot open %s", path);
+  std::vector<uint8_t> buf;
+  uint8_t tmp[1 << 16];
+  size_t r;
+  while ((r = std::fread(tmp, 1, sizeof tmp, f)) > 0) buf.insert(buf.end(), tmp, tmp + r);
+  std::fclose(f);
+  return lbm_checkpoint_load(s, buf.data(), buf.size());
+}
+
+
+// ---- halo rows (include/lbm.h) --------------------------------------------------------
+
+static int rows_io(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, void* host, bool on_device,
+                   bool read) {
+  CHECK_SIM(s);
+  if (!host) return fail(LBM_ERR_ARG, "null buffer");
+  if (nrows == 0 || y + nrows > (uint32_t)s->L.ny || slot_mask == 0 || slot_mask > 0xFFu)
+    return fail(LBM_ERR_ARG, "rows %u..%u, slot mask 0x%x", y, y + nrows, slot_mask);
+  const size_t e = s->es, row = (size_t)s->L.nx * e;
+  const cudaMemcpyKind kind = read ? (on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost)
+                                   : (on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);
+  char* buf = (char*)host;
+  for (int slot = 0; slot < 8; slot++) {
+    if (!((slot_mask >> slot) & 1u)) continue;
+    char* dev = (char*)s->f[s->cur] + ((size_t)slot * s->L.ps + (size_t)y * s->L.pitch) * e;
+    cudaError_t r = read ? cudaMemcpy2DAsync(buf, row, dev, (size_t)s->L.pitch * e, row, nrows, kind, s->stream)
+                         : cudaMemcpy2DAsync(dev, (size_t)s->L.pitch * e, buf, row, row, nrows, kind, s->stream);
+    if (r != cudaSuccess) return fail(LBM_ERR_CUDA, "row copy: %s", cudaGetErrorString(r));
+    buf += row * nrows;
+  }
+  if (!on_device) CK(cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_rows_read(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, void* out, int on_device) {
+  return rows_io(s, y, nrows, slot_mask, out, on_device != 0, true);
+}
+
+int lbm_rows_write(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, const void* in, int on_device) {
+  return rows_io(s, y, nrows, slot_mask, const_cast<void*>(in), on_device != 0, false);
+}
+
+int lbm_storage_bytes(const lbm_sim* s, uint32_t* bytes) {
+  if (!s || !bytes) return fail(LBM_ERR_ARG, "null argument");
+  *bytes = (uint32_t)s->es;
+  return LBM_OK;
 }
 
 }  // extern "C"

@@ -6,8 +6,12 @@
 
 Data: `--train` seeded random-circle layouts (radii 8-40 fine cells, ~10 %
 solid, none within 64 cells of the inlet) run on the fine grid for `--steps`
-steps at tau / u; every `--every` steps a snapshot becomes a coarse training
-sample on the device (features and the subgrid-stress fit coefficients).  Training: Adam on minibatches of
+steps at tau / u; every `--every` steps a snapshot becomes a coarse sample
+on the device (features: rho, u, solid).  Target (`--target rollout`, the
+default): per-cell relaxation-time labels from coarse runs at a few uniform
+delta_tau offsets, fitted against the fine run's time-averaged velocity
+(closure.rollout_labels); `--target sgs` fits an eddy viscosity to the
+subgrid stress of each snapshot instead (an a-priori target).  Training: Adam on minibatches of
 `--batch` snapshots with the engine's own forward / backward kernels.
 Evaluation on `--test` held-out layouts: time-averaged velocity of the second
 half of each run, fine (block-averaged to the coarse grid) against coarse
@@ -15,84 +19,12 @@ plain BGK and coarse with the closure, and the wall time of each run.
 Prints one JSON report; saves the weights and the report to `--out`.
 """
 import argparse
-import ctypes
 import json
 import time
 
 import numpy as np
 
-from . import EDGE_CHANNEL, F32, Lattice, _check, load_library
 from . import closure as cl
-
-
-def _device_velocity(lat, torch, pops):
-    _check(load_library().lbm_read_populations_device(lat.handle, ctypes.c_void_p(pops.data_ptr())))
-    rho = pops.sum(0)
-    jx = pops[2] + pops[5] + pops[8] - pops[0] - pops[3] - pops[6]
-    jy = pops[0] + pops[1] + pops[2] - pops[6] - pops[7] - pops[8]
-    return torch.stack([jx / rho, jy / rho])
-
-
-def run_average(torch, nx, ny, tau, u, mask, steps, every, avg_from, seed, params=None, refresh=20, drift=0.5,
-                storage=F32):
-    """Run a channel lattice; returns (time-averaged velocity [2, ny, nx] over
-    steps avg_from..steps as float64 numpy, seconds spent stepping, fallback
-    cell-steps).  Averaging reads stay on the device and outside the timing."""
-    lib = load_library()
-    dev = torch.device("cuda")
-    pops = torch.empty((9, ny, nx), dtype=torch.float32, device=dev)
-    acc = torch.zeros((2, ny, nx), dtype=torch.float64, device=dev)
-    stream = torch.cuda.current_stream()
-    n = 0
-    t_step = 0.0
-    fb = ctypes.c_uint64(0)
-    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
-        lat.set_stream(stream.cuda_stream)
-        lat.set_inlet_velocity(u)
-        lat.init_equilibrium(1.0, u, 0.0, 1e-3, seed)
-        lat.draw_mask(mask)
-        if params is not None:
-            p = np.ascontiguousarray(params, np.float32)
-            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
-            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
-        done = 0
-        chunk = min(every, refresh) if params is not None else every
-        while done < steps:
-            k = min(chunk, steps - done)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            if params is not None and done % refresh == 0:
-                _check(lib.lbm_closure_infer(lat.handle))
-            lat.iterate(k)
-            torch.cuda.synchronize()
-            t_step += time.perf_counter() - t0
-            done += k
-            if done > avg_from and done % every == 0:
-                acc += _device_velocity(lat, torch, pops).double()
-                n += 1
-        if params is not None:
-            _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
-        try:
-            lat.synchronize()
-        except Exception:
-            pass  # a run that went non-finite is reported through its error, not raised
-    return (acc / max(n, 1)).cpu().numpy(), t_step, fb.value
-
-
-def block_average(u, mask, F):
-    ny, nx = mask.shape
-    fl = (mask == 0).astype(np.float64)[:ny // F * F, :nx // F * F].reshape(ny // F, F, nx // F, F)
-    uu = np.nan_to_num(u[:, :ny // F * F, :nx // F * F]).reshape(2, ny // F, F, nx // F, F)
-    return (uu * fl[None]).sum(axis=(2, 4)) / np.maximum(fl.sum(axis=(1, 3)), 1)
-
-
-def rel_error(uc, uf, solid_c):
-    fl = solid_c == 0
-    fl[:, 0] = False
-    d = (uc - uf)[:, fl]
-    if not np.isfinite(d).all():
-        return float("inf")
-    return float(np.linalg.norm(d) / np.linalg.norm(uf[:, fl]))
 
 
 def main(argv=None):
@@ -112,7 +44,8 @@ def main(argv=None):
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--refresh", type=int, default=20)
-    ap.add_argument("--drift", type=float, default=0.5)
+    ap.add_argument("--drift", type=float, default=1.0)
+    ap.add_argument("--target", choices=["rollout", "sgs"], default="rollout")
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--out", default="closure.npz")
     a = ap.parse_args(argv)
@@ -126,18 +59,35 @@ def main(argv=None):
 
     # ---- data ------------------------------------------------------------------
     t0 = time.perf_counter()
-    feats, coefs = [], []
+    steps_c, every_c = a.steps // F, max(a.every // F, 1)
+    feats, coefs, label_err = [], [], []
     for i in range(a.train):
-        f, c, _ = cl.fine_samples(layouts[i], a.tau, a.u, a.steps, a.every, F, seed=a.seed * 7919 + i,
-                                  start=a.start)
+        seed = a.seed * 7919 + i
+        f, c, _ = cl.fine_samples(layouts[i], a.tau, a.u, a.steps, a.every, F, seed=seed, start=a.start)
+        if a.target == "rollout":
+            uf, _, _ = cl.run_average(nx, ny, a.tau, a.u, layouts[i], a.steps, a.every, a.steps // 2, seed)
+            sc = cl.coarse_solid(layouts[i], F)
+            label, w, rels = cl.rollout_labels(sc, tau_c, a.u, steps_c, every_c, cl.block_average(uf, layouts[i], F),
+                                               seed)
+            label_err.append(rels)
+            lab = torch.from_numpy(np.stack([w, w * label, w * label * label]).astype(np.float32)).cuda()
+            c = lab[None].expand(f.shape[0], -1, -1, -1).contiguous()
         feats.append(f)
         coefs.append(c)
     feat = torch.cat(feats)
     coef = torch.cat(coefs)
     del feats, coefs
-    norms = coef[:, 2].sum(dim=(1, 2)).double().cpu().numpy()
+    # loss normalisation per sample: the weighted mean squared delta_tau error
+    # (rollout labels) or the fraction of the subgrid stress left unexplained
+    norms = coef[:, 0 if a.target == "rollout" else 2].sum(dim=(1, 2)).double().cpu().numpy()
+    norms = np.where(norms > 0, norms, 1.0)
     torch.cuda.synchronize()
     rep["samples"] = int(feat.shape[0])
+    rep["target"] = a.target
+    if label_err:
+        rep["candidates"] = list(cl.CANDIDATES)
+        rep["candidate_rel_err_median"] = [float(np.median([r[k] for r in label_err])) for k in
+                                           range(len(cl.CANDIDATES))]
     rep["data_seconds"] = time.perf_counter() - t0
 
     # ---- training --------------------------------------------------------------
@@ -161,7 +111,7 @@ def main(argv=None):
     rep["train_seconds"] = time.perf_counter() - t0
     rep["loss_history"] = hist
     params = net.numpy()
-    # loss with delta_tau = 0 (plain coarse BGK: the whole subgrid stress unexplained) and trained
+    # loss of delta_tau = 0 (plain coarse BGK) and of the trained network on the first samples
     k = min(S, 64)
     zero_z = torch.full((k, 1) + tuple(feat.shape[2:]), -30.0, device=feat.device)
     L0, _ = net.loss(zero_z, coef[:k], float(norms[:k].sum()), grad=False)
@@ -171,28 +121,42 @@ def main(argv=None):
     del feat, coef
 
     # ---- evaluation ------------------------------------------------------------
-    steps_c = a.steps // F
+    # baselines: plain coarse BGK (delta_tau = 0) and the uniform candidate
+    # with the lowest median error over the training layouts
+    best_dt = 0.0
+    if label_err:
+        med = rep["candidate_rel_err_median"]
+        best_dt = float(cl.CANDIDATES[int(np.argmin(med))])
+    rep["best_uniform_delta_tau"] = best_dt
     per = []
     for j in range(a.test):
         m = layouts[a.train + j]
         sc = cl.coarse_solid(m, F)
         seed = a.seed * 7919 + a.train + j
-        uf, tf, _ = run_average(torch, nx, ny, a.tau, a.u, m, a.steps, a.every, a.steps // 2, seed)
-        ufc = block_average(uf, m, F)
-        up, tp, _ = run_average(torch, nx // F, ny // F, tau_c, a.u, sc, steps_c, max(a.every // F, 1), steps_c // 2,
-                                seed)
-        uc, tc, fb = run_average(torch, nx // F, ny // F, tau_c, a.u, sc, steps_c, max(a.every // F, 1),
-                                 steps_c // 2, seed, params=params, refresh=a.refresh, drift=a.drift)
+        uf, _, _ = cl.run_average(nx, ny, a.tau, a.u, m, a.steps, a.every, a.steps // 2, seed)
+        ufc = cl.block_average(uf, m, F)
+        up, _, _ = cl.run_average(nx // F, ny // F, tau_c, a.u, sc, steps_c, every_c, steps_c // 2, seed)
+        ub, _, _ = cl.run_average(nx // F, ny // F, tau_c + best_dt, a.u, sc, steps_c, every_c, steps_c // 2, seed)
+        uc, _, fb = cl.run_average(nx // F, ny // F, tau_c, a.u, sc, steps_c, every_c, steps_c // 2, seed,
+                                   params=params, refresh=a.refresh, drift=a.drift)
+        tf = cl.time_run(nx, ny, a.tau, a.u, m, a.steps, seed)
+        tc = cl.time_run(nx // F, ny // F, tau_c, a.u, sc, steps_c, seed, params=params, refresh=a.refresh,
+                         drift=a.drift)
+        tp = cl.time_run(nx // F, ny // F, tau_c + best_dt, a.u, sc, steps_c, seed)
         active = int((sc == 0)[:, 1:].sum()) * steps_c
-        per.append({"layout": a.train + j, "err_plain": rel_error(up, ufc, sc), "err_closure": rel_error(uc, ufc, sc),
-                    "fine_seconds": tf, "plain_seconds": tp, "closure_seconds": tc,
+        per.append({"layout": a.train + j, "err_plain": cl.rel_error(up, ufc, sc),
+                    "err_best_uniform": cl.rel_error(ub, ufc, sc), "err_closure": cl.rel_error(uc, ufc, sc),
+                    "fine_seconds": tf, "uniform_seconds": tp, "closure_seconds": tc,
                     "fallback_fraction": fb / max(active, 1)})
     rep["per_layout"] = per
     ep = [p["err_plain"] for p in per]
     ec = [p["err_closure"] for p in per]
     rep["median_err_plain"] = float(np.median(ep))
     rep["median_err_closure"] = float(np.median(ec))
+    rep["median_err_best_uniform"] = float(np.median([p["err_best_uniform"] for p in per]))
     rep["speedup_vs_fine"] = float(np.median([p["fine_seconds"] / p["closure_seconds"] for p in per]))
+    rep["closure_better_than_plain"] = int(sum(p["err_closure"] < p["err_plain"] for p in per))
+    rep["closure_better_than_best_uniform"] = int(sum(p["err_closure"] < p["err_best_uniform"] for p in per))
     np.savez(a.out, params=params, report=json.dumps(rep))
     print(json.dumps(rep))
     return rep
