@@ -90,6 +90,10 @@ int lbm_closure_enable(lbm_sim* sim, float drift);
 int lbm_closure_disable(lbm_sim* sim);
 /* Predict from the moments of the last step (queued on the lattice's stream). */
 int lbm_closure_infer(lbm_sim* sim);
+/* Inference kernel: 0 (default) the tensor-core kernel (tcgen05.mma, BF16
+ * operands, f32 accumulation in tensor memory), 1 the CUDA-core kernel (BF16
+ * weights widened to f32).  Both evaluate the same network. */
+int lbm_closure_set_inference(lbm_sim* sim, int kernel);
 /* Current records as nx * ny floats each (either pointer may be NULL). */
 int lbm_closure_read(lbm_sim* sim, float* dtau, float* speed);
 /* Cell-steps that fell back to plain BGK since the last reset. */

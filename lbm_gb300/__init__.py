@@ -122,6 +122,7 @@ _SIGS = [
     ("lbm_closure_enable", ctypes.c_int, [_P, ctypes.c_float]),
     ("lbm_closure_disable", ctypes.c_int, [_P]),
     ("lbm_closure_infer", ctypes.c_int, [_P]),
+    ("lbm_closure_set_inference", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_closure_read", ctypes.c_int, [_P, _P, _P]),
     ("lbm_closure_fallback_count", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_uint64), ctypes.c_int]),
     # include/lbm_batch.h

@@ -12,6 +12,7 @@
 #include "lbm_kernels.cuh"
 #include "lbm_stage.cuh"
 #include "lbm_closure.cuh"
+#include "lbm_closure_tc.cuh"
 #include "lbm_render.cuh"
 #include "../../include/lbm_render.h"
 #include "../../include/lbm_checkpoint.h"
@@ -100,6 +101,7 @@ struct lbm_sim {
   unsigned long long* fallback_d = nullptr;
   float drift = 0.5f;
   bool closure_on = false;
+  int closure_kernel = 0;  // 0: tensor cores (tcgen05), 1: CUDA cores
 };
 
 namespace {
@@ -786,14 +788,28 @@ int lbm_closure_infer(lbm_sim* s) {
     if (!rc) rc = compute_moments(s);
     if (rc) return rc;
   }
-  const size_t smem = sizeof(CnnSmem);
-  CK(cudaFuncSetAttribute(k_closure_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((s->L.nx + kCnnTile - 1) / kCnnTile, (s->L.ny + kCnnTile - 1) / kCnnTile);
-  k_closure_infer<<<grid, 256, smem, s->stream>>>(s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1),
-                                                  (const float*)mom_plane(s, 2), s->mask_d, s->cnn_w, LBM_CNN_S_RHO,
-                                                  LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d);
+  if (s->closure_kernel == 0) {
+    CK(cudaFuncSetAttribute(k_closure_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmem));
+    k_closure_infer_tc<<<grid, 256, tc::kSmem, s->stream>>>(
+        s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), s->mask_d,
+        s->cnn_w, LBM_CNN_S_RHO, LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d, s->flag_d);
+  } else {
+    const size_t smem = sizeof(CnnSmem);
+    CK(cudaFuncSetAttribute(k_closure_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_closure_infer<<<grid, 256, smem, s->stream>>>(s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1),
+                                                    (const float*)mom_plane(s, 2), s->mask_d, s->cnn_w, LBM_CNN_S_RHO,
+                                                    LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d);
+  }
   CK_LAUNCH();
   s->launches++;
+  return LBM_OK;
+}
+
+int lbm_closure_set_inference(lbm_sim* s, int kernel) {
+  CHECK_SIM(s);
+  if (kernel != 0 && kernel != 1) return fail(LBM_ERR_ARG, "inference kernel %d (0 tensor cores, 1 CUDA cores)", kernel);
+  s->closure_kernel = kernel;
   return LBM_OK;
 }
 

@@ -1,0 +1,350 @@
+// Learned closure inference on the 5th-generation tensor cores: the whole
+// network per 16 x 16 tile in shared memory, the three 32-channel layers as
+// implicit GEMMs issued with tcgen05.mma (BF16 operands from shared memory,
+// f32 accumulators in tensor memory), the 1-channel output layer on the CUDA
+// cores.
+//
+// GEMM shapes per tile (M = window pixels, N = 32 output channels):
+//   layer 1  M = 22 x 22 (4 blocks of 128), K = 9 taps x 4 channels, padded
+//            to 48; its A operand is an explicit im2col of the features;
+//   layer 2  M = 20 rows x 22 (the input window's pitch), K = 9 x 32;
+//   layer 3  M = 18 rows x 20, K = 9 x 32.
+// For layers 2 and 3 the A operand of tap (ky, kx) is the input activation
+// buffer itself viewed from row offset ky * pitch + kx: output pixel q =
+// oy * pitch + ox reads input pixel q + ky * pitch + kx, so each tap is one
+// shared-memory descriptor with a shifted start address (the two columns per
+// row with ox >= the output width are computed and dropped).
+//
+// Operand layout (no swizzle, K-major): a buffer is [K / 8][rows][8 x bf16],
+// so an 8-row x 16-byte core matrix is 128 contiguous bytes; the leading
+// byte offset (next 8 K-values) is rows * 16 B and the stride byte offset
+// (next 8 rows) is 128 B.  Weights are [K / 8][32][8] likewise.
+//
+// One thread issues the MMAs and commits them to an mbarrier; every wait is
+// bounded (a timeout sets bit 2 of the error flag).  The CTA allocates 128
+// tensor-memory columns (4 accumulator blocks of 128 lanes x 32 f32) and
+// frees them on every path.  Dynamic shared memory is the whole 227 KB
+// opt-in window, so every operand address a descriptor can form lies inside
+// the CTA's own allocation.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include "lbm_closure.cuh"
+
+namespace lbm {
+namespace tc {
+
+constexpr int kT = 16;                 // output tile
+constexpr int kW0 = kT + 8;            // feature window (24)
+constexpr int kW1 = kT + 6, kW2 = kT + 4, kW3 = kT + 2;  // layer output windows (22, 20, 18)
+constexpr int kM1 = kW1 * kW1;         // 484 rows of layer 1
+constexpr int kM2 = kW2 * kW1;         // 440 rows of layer 2 (pitch 22)
+constexpr int kM3 = kW3 * kW2;         // 360 rows of layer 3 (pitch 20)
+constexpr int kB1 = 4, kB2 = 4, kB3 = 3;   // 128-row blocks
+constexpr int kK1 = 48;                // layer-1 K (36 used)
+// rows of each activation buffer: every row a descriptor of its layer can reach
+constexpr int kR1 = kB1 * 128;                          // im2col rows
+constexpr int kRX1 = kB2 * 128 + 2 * kW1 + 2 + 6;       // layer-1 output, pitch 22 (= 564)
+constexpr int kRX2 = kB3 * 128 + 2 * kW2 + 2 + 6;       // layer-2 output, pitch 20 (= 432)
+constexpr int kRX3 = kW3 * kW3;                         // layer-3 output, pitch 18 (= 324)
+
+// byte offsets in dynamic shared memory
+constexpr uint32_t kOffA1 = 0;                                  // [6][512][8] bf16
+constexpr uint32_t kOffX1 = kOffA1 + 6u * kR1 * 16u;            // [4][564][8]
+constexpr uint32_t kOffX2 = kOffX1 + 4u * kRX1 * 16u;           // [4][432][8]
+constexpr uint32_t kOffW1 = kOffX2 + 4u * kRX2 * 16u;           // [6][32][8]
+constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8]
+constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;
+constexpr uint32_t kOffFeat = kOffW3 + 36u * 32u * 16u;         // f32 [576][4]
+constexpr uint32_t kOffW4 = kOffFeat + kW0 * kW0 * 16u;         // f32 [288] + 4 x 32 biases
+constexpr uint32_t kOffBar = kOffW4 + (288u + 128u) * 4u;   // mbarrier (8 B), tensor-memory address (4 B)
+constexpr uint32_t kUsed = kOffBar + 16u;
+constexpr uint32_t kSmem = 232448u;  // 227 KB: the whole opt-in window (see above); no static shared memory
+static_assert(kUsed <= kSmem, "closure tile does not fit in shared memory");
+// layer-3 output reuses the im2col region
+constexpr uint32_t kOffX3 = kOffA1;
+static_assert(4u * kRX3 * 16u <= 6u * kR1 * 16u, "layer-3 output overlaps");
+
+__device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t sdesc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1, no swizzle, base offset 0
+}
+
+// kind::f16 instruction descriptor: D f32, A and B bf16, both K-major, M x N.
+constexpr uint32_t idesc(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma(uint32_t dtmem, uint64_t a, uint64_t b, uint32_t id, uint32_t accum) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dtmem),
+      "l"(a), "l"(b), "r"(id), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (clock64() - t0 > (1ll << 31)) return false;
+  }
+}
+
+// 32 consecutive f32 columns of this thread's tensor-memory lane.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+        "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; i++) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Store 32 channels of one pixel row into a [4][rows][8] bf16 buffer.
+__device__ __forceinline__ void store_row(unsigned char* buf, int rows, int row, const float (&v)[32]) {
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    __nv_bfloat162 h[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) h[j] = __floats2bfloat162_rn(v[8 * c + 2 * j], v[8 * c + 2 * j + 1]);
+    *reinterpret_cast<uint4*>(buf + ((size_t)c * rows + row) * 16) = *reinterpret_cast<uint4*>(h);
+  }
+}
+
+// Weights of a 32 -> 32 layer into [36][32][8] (K = tap * 32 + ci).
+__device__ __forceinline__ void load_w32(unsigned char* dst, const __nv_bfloat16* __restrict__ w) {
+  for (int i = threadIdx.x; i < 36 * 32; i += blockDim.x) {
+    const int kc = i / 32, co = i % 32, tap = kc / 4, ci0 = (kc % 4) * 8;
+    __nv_bfloat16 e[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) e[j] = w[(co * 32 + ci0 + j) * 9 + tap];
+    *reinterpret_cast<uint4*>(dst + (size_t)i * 16) = *reinterpret_cast<uint4*>(e);
+  }
+}
+
+}  // namespace tc
+
+// grid (ceil(nx / 16), ceil(ny / 16)), 256 threads, tc::kSmem dynamic shared memory.
+__global__ void __launch_bounds__(256, 1)
+    k_closure_infer_tc(Layout L, const float* __restrict__ rho, const float* __restrict__ jx,
+                       const float* __restrict__ jy, const uint32_t* __restrict__ mask,
+                       const __nv_bfloat16* __restrict__ wts, float s_rho, float s_u, float dt_max,
+                       __half2* __restrict__ record, int* __restrict__ flag) {
+  using namespace tc;
+  extern __shared__ __align__(1024) unsigned char sm[];
+  uint32_t& tmem_slot = *reinterpret_cast<uint32_t*>(sm + kOffBar + 8);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int tx0 = blockIdx.x * kT, ty0 = blockIdx.y * kT;
+  float* feat = reinterpret_cast<float*>(sm + kOffFeat);
+  float* w4 = reinterpret_cast<float*>(sm + kOffW4);  // [ci][tap] then biases b1, b2, b3, b4
+  const uint32_t bar = saddr(sm + kOffBar);
+
+  if (warp == 0) {  // tensor memory: 128 columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(saddr(&tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // features of the 24 x 24 window; weights
+  for (int i = tid; i < kW0 * kW0; i += blockDim.x) {
+    const int gx = tx0 - 4 + i % kW0, gy = ty0 - 4 + i / kW0;
+    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
+    if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
+      const long long o = (long long)gy * L.pitch + gx;
+      if ((mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u) {
+        f3 = 1.0f;
+      } else {
+        const float r = rho[o];
+        f0 = (r - 1.0f) * s_rho;
+        f1 = jx[o] / r * s_u;
+        f2 = jy[o] / r * s_u;
+      }
+    }
+    feat[4 * i] = f0;
+    feat[4 * i + 1] = f1;
+    feat[4 * i + 2] = f2;
+    feat[4 * i + 3] = f3;
+  }
+  for (int i = tid; i < 6 * 32; i += blockDim.x) {  // layer 1: K = tap * 4 + ci (36 used of 48)
+    const int kc = i / 32, co = i % 32;
+    __nv_bfloat16 e[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
+      e[j] = k < 36 ? wts[cnn_layer_offset(0) + (co * 4 + ci) * 9 + tap] : __float2bfloat16_rn(0.0f);
+    }
+    *reinterpret_cast<uint4*>(sm + kOffW1 + (size_t)i * 16) = *reinterpret_cast<uint4*>(e);
+  }
+  load_w32(sm + kOffW2, wts + cnn_layer_offset(1));
+  load_w32(sm + kOffW3, wts + cnn_layer_offset(2));
+  for (int i = tid; i < 288; i += blockDim.x)  // layer 4: [ci][tap] in f32
+    w4[i] = __bfloat162float(wts[cnn_layer_offset(3) + (i / 9) * 9 + i % 9]);
+  for (int i = tid; i < 97; i += blockDim.x) {  // biases: each layer's come last in its block
+    constexpr int kBias0 = cnn_layer_offset(1) - 32, kBias1 = cnn_layer_offset(2) - 32;
+    constexpr int kBias2 = cnn_layer_offset(3) - 32, kBias3 = cnn_layer_offset(4) - 1;
+    const int l = i / 32, c = i % 32;
+    const int o = (l == 0 ? kBias0 : l == 1 ? kBias1 : l == 2 ? kBias2 : kBias3) + c;
+    w4[288 + i] = __bfloat162float(wts[o]);
+  }
+  __syncthreads();
+  // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci
+  for (int i = tid; i < kR1 * 6; i += blockDim.x) {
+    const int p = i / 6, kc = i % 6;
+    __nv_bfloat16 e[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+      const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
+      float v = 0.0f;
+      if (p < kM1 && k < 36) {
+        const int oy = p / kW1, ox = p % kW1;
+        v = feat[4 * ((oy + tap / 3) * kW0 + ox + tap % 3) + ci];
+      }
+      e[j] = __float2bfloat16_rn(v);
+    }
+    *reinterpret_cast<uint4*>(sm + kOffA1 + ((size_t)kc * kR1 + p) * 16) = *reinterpret_cast<uint4*>(e);
+  }
+  fence_async_smem();
+  tc_before();
+  __syncthreads();
+  tc_after();
+  const uint32_t tmem = tmem_slot;
+  const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  bool ok = true;
+
+  // Issues one layer's MMAs (thread 0) and waits for them (everyone).
+  auto run_layer = [&](int layer, int blocks, int taps, int ksteps, uint32_t a_base, uint32_t a_rows, int pitch,
+                       uint32_t w_base) {
+    if (tid == 0) {
+      const uint32_t id = idesc(128, 32);
+      for (int mb = 0; mb < blocks; mb++)
+        for (int t = 0; t < taps; t++)
+          for (int s = 0; s < ksteps; s++) {
+            const uint32_t shift = (uint32_t)(mb * 128 + (taps == 9 ? (t / 3) * pitch + t % 3 : 0));
+            const uint32_t kc = (uint32_t)(taps == 9 ? t * 4 + 2 * s : 2 * s);
+            const uint64_t a = sdesc(a_base + (uint32_t)(2 * s) * a_rows * 16u + shift * 16u, a_rows * 16u, 128u);
+            const uint64_t b = sdesc(w_base + kc * 512u, 512u, 128u);
+            mma(tmem + (uint32_t)(mb * 32), a, b, id, (t > 0 || s > 0) ? 1u : 0u);
+          }
+      commit(bar);
+    }
+    if (!bar_wait(bar, (uint32_t)(layer & 1))) ok = false;
+    tc_after();
+  };
+  const uint32_t base = saddr(sm);
+
+  // ---- layer 1 -> X1 (pitch 22) ---------------------------------------------------------
+  run_layer(0, kB1, 1, 3, base + kOffA1, kR1, 0, base + kOffW1);
+  for (int mb = warp >> 2; mb < kB1; mb += 2) {
+    float v[32];
+    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+    const int p = mb * 128 + 32 * (warp & 3) + lane;
+    if (p < kM1) {
+      const int oy = p / kW1, ox = p % kW1, gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
+      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+#pragma unroll
+      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[288 + c], 0.0f) : 0.0f;
+      store_row(sm + kOffX1, kRX1, p, v);
+    }
+  }
+  // rows of X1 beyond the window: zero (read only by dropped outputs, but keep them finite)
+  for (int i = tid; i < 4 * (kRX1 - kM1); i += blockDim.x) {
+    const int c = i / (kRX1 - kM1), r = kM1 + i % (kRX1 - kM1);
+    *reinterpret_cast<uint4*>(sm + kOffX1 + ((size_t)c * kRX1 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  fence_async_smem();
+  tc_before();
+  __syncthreads();
+  tc_after();
+
+  // ---- layer 2 -> X2 (pitch 20) ---------------------------------------------------------
+  run_layer(1, kB2, 9, 2, base + kOffX1, kRX1, kW1, base + kOffW2);
+  for (int mb = warp >> 2; mb < kB2; mb += 2) {
+    float v[32];
+    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+    const int q = mb * 128 + 32 * (warp & 3) + lane;
+    const int oy = q / kW1, ox = q % kW1;
+    if (q < kM2 && ox < kW2) {
+      const int gx = tx0 - 2 + ox, gy = ty0 - 2 + oy;
+      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+#pragma unroll
+      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[320 + c], 0.0f) : 0.0f;
+      store_row(sm + kOffX2, kRX2, oy * kW2 + ox, v);
+    }
+  }
+  for (int i = tid; i < 4 * (kRX2 - kW2 * kW2); i += blockDim.x) {
+    const int c = i / (kRX2 - kW2 * kW2), r = kW2 * kW2 + i % (kRX2 - kW2 * kW2);
+    *reinterpret_cast<uint4*>(sm + kOffX2 + ((size_t)c * kRX2 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+  }
+  fence_async_smem();
+  tc_before();
+  __syncthreads();
+  tc_after();
+
+  // ---- layer 3 -> X3 (pitch 18, in the im2col region) ------------------------------------
+  run_layer(2, kB3, 9, 2, base + kOffX2, kRX2, kW2, base + kOffW3);
+  for (int mb = warp >> 2; mb < kB3; mb += 2) {
+    float v[32];
+    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+    const int q = mb * 128 + 32 * (warp & 3) + lane;
+    const int oy = q / kW2, ox = q % kW2;
+    if (q < kM3 && ox < kW3) {
+      const int gx = tx0 - 1 + ox, gy = ty0 - 1 + oy;
+      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+#pragma unroll
+      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[352 + c], 0.0f) : 0.0f;
+      store_row(sm + kOffX3, kRX3, oy * kW3 + ox, v);
+    }
+  }
+  tc_before();
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (!ok && tid == 0) atomicOr(flag, 2);
+
+  // ---- layer 4 (32 -> 1) on the CUDA cores, record ----------------------------------------
+  {
+    const int oy = tid / kT, ox = tid % kT, gx = tx0 + ox, gy = ty0 + oy;
+    float z = w4[384];
+    for (int tap = 0; tap < 9; tap++) {
+      const int r = (oy + tap / 3) * kW3 + ox + tap % 3;
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
+#pragma unroll
+        for (int j = 0; j < 8; j++) z = fmaf(__bfloat162float(e[j]), w4[(8 * c + j) * 9 + tap], z);
+      }
+    }
+    if (gx < L.nx && gy < L.ny) {
+      const long long o = (long long)gy * L.pitch + gx;
+      const float dt = dt_max / (1.0f + expf(-z));
+      const float r = rho[o], vx = jx[o], vy = jy[o];
+      record[o] = __floats2half2_rn(dt, sqrtf(vx * vx + vy * vy) / r);
+    }
+  }
+}
+
+}  // namespace lbm

@@ -42,7 +42,7 @@ def main(argv=None):
     ap.add_argument("--rmax", type=float, default=40.0)
     ap.add_argument("--iters", type=int, default=3000)
     ap.add_argument("--batch", type=int, default=4)
-    ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--refresh", type=int, default=20)
     ap.add_argument("--drift", type=float, default=1.0)
     ap.add_argument("--target", choices=["rollout", "sgs"], default="rollout")
@@ -91,7 +91,15 @@ def main(argv=None):
     rep["data_seconds"] = time.perf_counter() - t0
 
     # ---- training --------------------------------------------------------------
-    net = cl.ClosureNet(seed=a.seed)
+    # start the output bias at the weighted mean label: the sigmoid then starts
+    # in its responsive range instead of saturating toward delta_tau = 0
+    init = cl.init_params(a.seed)
+    sw = float(coef[:, 0].sum().item())
+    mean_label = float(coef[:, 1].sum().item()) / sw if sw > 0 else 0.01
+    frac = min(max(mean_label / cl.DT_MAX, 1e-3), 0.999)
+    init[-1] = np.float32(np.log(frac / (1.0 - frac)))
+    rep["mean_label"] = mean_label
+    net = cl.ClosureNet(params=init)
     rng = np.random.default_rng(a.seed)
     S = feat.shape[0]
     t0 = time.perf_counter()

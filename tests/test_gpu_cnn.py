@@ -121,9 +121,13 @@ def test_gpu_closure_samples_match_oracle(lbm, torch_cuda):
     np.testing.assert_array_equal(solid_c.cpu().numpy(), C.coarsen(pops, mask, 4)[-1])
 
 
-def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda):
-    """The tile-fused network on a lattice's moments against the whole-image
-    oracle network with the same BF16-rounded weights."""
+@pytest.mark.parametrize("kernel", [0, 1])
+def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda, kernel):
+    """The tile-fused network on a lattice's moments (kernel 0: tcgen05 tensor
+    cores with BF16 activations; 1: CUDA cores with f32 activations) against
+    the whole-image oracle network with the same BF16-rounded weights.  The
+    tensor-core kernel rounds each layer's activations to BF16 (8-bit
+    mantissa): its delta_tau is held to 2 % of the largest value."""
     from lbm_gb300 import closure, geometry
     nx, ny = 150, 70  # ragged tiles on both axes
     mask = geometry.single_circle(nx, ny, 40, 35, 8)
@@ -138,7 +142,9 @@ def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda):
         p = flat.copy()
         lbm._check(L.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
         lbm._check(L.lbm_closure_enable(lat.handle, 0.5))
+        lbm._check(L.lbm_closure_set_inference(lat.handle, kernel))
         lbm._check(L.lbm_closure_infer(lat.handle))
+        lat.synchronize()
         dt = np.zeros(nx * ny, np.float32)
         sp = np.zeros(nx * ny, np.float32)
         lbm._check(L.lbm_closure_read(lat.handle, dt.ctypes.data_as(ctypes.c_void_p),
@@ -152,7 +158,10 @@ def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda):
     z = C.forward(ps, feat)[-1][0, 0]
     want = C.delta_tau(z)
     got = dt.reshape(ny, nx)
-    assert np.abs(got - want)[fl].max() <= 2e-3 * want.max()
+    tol = 2e-3 if kernel == 1 else 2e-2
+    err = np.abs(got - want)[fl].max() / want.max()
+    print("kernel %d: max delta_tau error %.3e of %.3e" % (kernel, err, want.max()))
+    assert err <= tol
     speed = np.hypot(jx, jy) / r
     assert np.abs(sp.reshape(ny, nx) - speed)[fl].max() <= 2e-3 * speed[fl].max()
 
