@@ -98,6 +98,7 @@ struct lbm_sim {
   void* closure_base = nullptr;          // padded allocation of the per-cell records
   __half2* closure_d = nullptr;          // (delta_tau, |u| at prediction) per cell, pitch layout
   __nv_bfloat16* cnn_w = nullptr;        // network parameters, BF16
+  unsigned char* cnn_wpack = nullptr;    // the same, packed for the tensor-core kernel
   unsigned long long* fallback_d = nullptr;
   float drift = 0.5f;
   bool closure_on = false;
@@ -205,7 +206,7 @@ int check_sim(const lbm_sim* s) {
 void release(lbm_sim* s) {
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
-  cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->fallback_d);
+  cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -748,8 +749,12 @@ int lbm_closure_set_weights(lbm_sim* s, const float* params, size_t n) {
   if (!params || n != (size_t)kCnnParams) return fail(LBM_ERR_ARG, "closure weights: need %d parameters", kCnnParams);
   std::vector<__nv_bfloat16> w(n);
   for (size_t i = 0; i < n; i++) w[i] = __float2bfloat16_rn(params[i]);
+  std::vector<unsigned char> packed(tc::kPackedBytes);
+  tc::pack_weights(params, packed.data());
   if (!s->cnn_w) CK(cudaMalloc(&s->cnn_w, n * sizeof(__nv_bfloat16)));
+  if (!s->cnn_wpack) CK(cudaMalloc(&s->cnn_wpack, tc::kPackedBytes));
   CK(cudaMemcpyAsync(s->cnn_w, w.data(), n * sizeof(__nv_bfloat16), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(s->cnn_wpack, packed.data(), tc::kPackedBytes, cudaMemcpyHostToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }
@@ -791,9 +796,11 @@ int lbm_closure_infer(lbm_sim* s) {
   dim3 grid((s->L.nx + kCnnTile - 1) / kCnnTile, (s->L.ny + kCnnTile - 1) / kCnnTile);
   if (s->closure_kernel == 0) {
     CK(cudaFuncSetAttribute(k_closure_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmem));
-    k_closure_infer_tc<<<grid, 256, tc::kSmem, s->stream>>>(
+    if (!s->sms) CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
+    const int tiles = (int)(grid.x * grid.y);
+    k_closure_infer_tc<<<std::min(tiles, s->sms), 256, tc::kSmem, s->stream>>>(
         s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), s->mask_d,
-        s->cnn_w, LBM_CNN_S_RHO, LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d, s->flag_d);
+        s->cnn_wpack, LBM_CNN_S_RHO, LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d, s->flag_d);
   } else {
     const size_t smem = sizeof(CnnSmem);
     CK(cudaFuncSetAttribute(k_closure_infer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -21,7 +21,8 @@
 // (next 8 rows) is 128 B.  Weights are [K / 8][32][8] likewise.
 //
 // One thread issues the MMAs and commits them to an mbarrier; every wait is
-// bounded (a timeout sets bit 2 of the error flag).  The CTA allocates 128
+// bounded (a timeout sets bit 2 of the error flag and the CTA stops waiting
+// for the rest of its tiles).  The CTA allocates 128
 // tensor-memory columns (4 accumulator blocks of 128 lanes x 32 f32) and
 // frees them on every path.  Dynamic shared memory is the whole 227 KB
 // opt-in window, so every operand address a descriptor can form lies inside
@@ -52,18 +53,50 @@ constexpr int kRX3 = kW3 * kW3;                         // layer-3 output, pitch
 constexpr uint32_t kOffA1 = 0;                                  // [6][512][8] bf16
 constexpr uint32_t kOffX1 = kOffA1 + 6u * kR1 * 16u;            // [4][564][8]
 constexpr uint32_t kOffX2 = kOffX1 + 4u * kRX1 * 16u;           // [4][432][8]
-constexpr uint32_t kOffW1 = kOffX2 + 4u * kRX2 * 16u;           // [6][32][8]
-constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8]
-constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;
-constexpr uint32_t kOffFeat = kOffW3 + 36u * 32u * 16u;         // f32 [576][4]
-constexpr uint32_t kOffW4 = kOffFeat + kW0 * kW0 * 16u;         // f32 [288] + 4 x 32 biases
-constexpr uint32_t kOffBar = kOffW4 + (288u + 128u) * 4u;   // mbarrier (8 B), tensor-memory address (4 B)
+// the packed parameters, in the order they are uploaded (pack_weights)
+constexpr uint32_t kOffW1 = kOffX2 + 4u * kRX2 * 16u;           // [6][32][8] bf16
+constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8] bf16
+constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;           // [36][32][8] bf16
+constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // f32 [288] layer 4 [ci][tap], then b1 b2 b3 (32 each), b4
+constexpr uint32_t kPackedBytes = kOffW4 + 1552u - kOffW1;      // 385 floats, padded to 16 B
+constexpr uint32_t kOffFeat = kOffW1 + kPackedBytes;            // f32 [576][4]
+constexpr uint32_t kOffBar = kOffFeat + kW0 * kW0 * 16u;        // mbarrier (8 B), tensor-memory address (4 B)
 constexpr uint32_t kUsed = kOffBar + 16u;
 constexpr uint32_t kSmem = 232448u;  // 227 KB: the whole opt-in window (see above); no static shared memory
 static_assert(kUsed <= kSmem, "closure tile does not fit in shared memory");
+static_assert(kPackedBytes % 16 == 0 && 385u * 4u <= 1552u, "packed parameter block");
 // layer-3 output reuses the im2col region
 constexpr uint32_t kOffX3 = kOffA1;
 static_assert(4u * kRX3 * 16u <= 6u * kR1 * 16u, "layer-3 output overlaps");
+
+// Host-side packing of the network parameters (cnn_layer_offset order, f32)
+// into the block copied verbatim into shared memory: BF16 weights in the
+// K-major operand layouts above; layer 4 and the biases as BF16-rounded f32.
+inline void pack_weights(const float* p, unsigned char* out) {
+  auto bf = [](float v) { return __float2bfloat16_rn(v); };
+  __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(out);
+  for (int kc = 0; kc < 6; kc++)
+    for (int co = 0; co < 32; co++)
+      for (int j = 0; j < 8; j++) {
+        const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
+        w1[(kc * 32 + co) * 8 + j] = bf(k < 36 ? p[cnn_layer_offset(0) + (co * 4 + ci) * 9 + tap] : 0.0f);
+      }
+  for (int l = 1; l <= 2; l++) {
+    __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(out + (l == 1 ? kOffW2 : kOffW3) - kOffW1);
+    for (int kc = 0; kc < 36; kc++)
+      for (int co = 0; co < 32; co++)
+        for (int j = 0; j < 8; j++) {
+          const int tap = kc / 4, ci = (kc % 4) * 8 + j;
+          w[(kc * 32 + co) * 8 + j] = bf(p[cnn_layer_offset(l) + (co * 32 + ci) * 9 + tap]);
+        }
+  }
+  float* w4 = reinterpret_cast<float*>(out + kOffW4 - kOffW1);
+  for (int i = 0; i < 288; i++) w4[i] = __bfloat162float(bf(p[cnn_layer_offset(3) + i]));
+  const int bias[4] = {cnn_layer_offset(1) - 32, cnn_layer_offset(2) - 32, cnn_layer_offset(3) - 32,
+                       cnn_layer_offset(4) - 1};
+  for (int i = 0; i < 97; i++) w4[288 + i] = __bfloat162float(bf(p[bias[i / 32] + i % 32]));
+  for (int i = 385; i < 388; i++) w4[i] = 0.0f;
+}
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -134,35 +167,27 @@ __device__ __forceinline__ void store_row(unsigned char* buf, int rows, int row,
   }
 }
 
-// Weights of a 32 -> 32 layer into [36][32][8] (K = tap * 32 + ci).
-__device__ __forceinline__ void load_w32(unsigned char* dst, const __nv_bfloat16* __restrict__ w) {
-  for (int i = threadIdx.x; i < 36 * 32; i += blockDim.x) {
-    const int kc = i / 32, co = i % 32, tap = kc / 4, ci0 = (kc % 4) * 8;
-    __nv_bfloat16 e[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) e[j] = w[(co * 32 + ci0 + j) * 9 + tap];
-    *reinterpret_cast<uint4*>(dst + (size_t)i * 16) = *reinterpret_cast<uint4*>(e);
-  }
-}
-
 }  // namespace tc
 
-// grid (ceil(nx / 16), ceil(ny / 16)), 256 threads, tc::kSmem dynamic shared memory.
+// Persistent: grid = min(tiles, multiprocessors), 256 threads, tc::kSmem
+// dynamic shared memory; each CTA sets up tensor memory, its mbarrier and the
+// packed parameters once and then walks tiles blockIdx.x, + gridDim.x, ...
 __global__ void __launch_bounds__(256, 1)
     k_closure_infer_tc(Layout L, const float* __restrict__ rho, const float* __restrict__ jx,
                        const float* __restrict__ jy, const uint32_t* __restrict__ mask,
-                       const __nv_bfloat16* __restrict__ wts, float s_rho, float s_u, float dt_max,
+                       const unsigned char* __restrict__ wpack, float s_rho, float s_u, float dt_max,
                        __half2* __restrict__ record, int* __restrict__ flag) {
   using namespace tc;
   extern __shared__ __align__(1024) unsigned char sm[];
   uint32_t& tmem_slot = *reinterpret_cast<uint32_t*>(sm + kOffBar + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int tx0 = blockIdx.x * kT, ty0 = blockIdx.y * kT;
   float* feat = reinterpret_cast<float*>(sm + kOffFeat);
   float* w4 = reinterpret_cast<float*>(sm + kOffW4);  // [ci][tap] then biases b1, b2, b3, b4
   const uint32_t bar = saddr(sm + kOffBar);
+  const uint32_t base = saddr(sm);
+  const int tiles_x = (L.nx + kT - 1) / kT, tiles = tiles_x * ((L.ny + kT - 1) / kT);
 
-  if (warp == 0) {  // tensor memory: 128 columns
+  if (warp == 0) {  // tensor memory: 128 columns for the CTA's lifetime
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(saddr(&tmem_slot)));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
@@ -170,74 +195,21 @@ __global__ void __launch_bounds__(256, 1)
     asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar));
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  // features of the 24 x 24 window; weights
-  for (int i = tid; i < kW0 * kW0; i += blockDim.x) {
-    const int gx = tx0 - 4 + i % kW0, gy = ty0 - 4 + i / kW0;
-    float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-    if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
-      const long long o = (long long)gy * L.pitch + gx;
-      if ((mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u) {
-        f3 = 1.0f;
-      } else {
-        const float r = rho[o];
-        f0 = (r - 1.0f) * s_rho;
-        f1 = jx[o] / r * s_u;
-        f2 = jy[o] / r * s_u;
-      }
-    }
-    feat[4 * i] = f0;
-    feat[4 * i + 1] = f1;
-    feat[4 * i + 2] = f2;
-    feat[4 * i + 3] = f3;
+  {  // packed parameters: one contiguous copy
+    const uint4* src = reinterpret_cast<const uint4*>(wpack);
+    uint4* dst = reinterpret_cast<uint4*>(sm + kOffW1);
+    for (int i = tid; i < (int)(kPackedBytes / 16); i += blockDim.x) dst[i] = src[i];
   }
-  for (int i = tid; i < 6 * 32; i += blockDim.x) {  // layer 1: K = tap * 4 + ci (36 used of 48)
-    const int kc = i / 32, co = i % 32;
-    __nv_bfloat16 e[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
-      e[j] = k < 36 ? wts[cnn_layer_offset(0) + (co * 4 + ci) * 9 + tap] : __float2bfloat16_rn(0.0f);
-    }
-    *reinterpret_cast<uint4*>(sm + kOffW1 + (size_t)i * 16) = *reinterpret_cast<uint4*>(e);
-  }
-  load_w32(sm + kOffW2, wts + cnn_layer_offset(1));
-  load_w32(sm + kOffW3, wts + cnn_layer_offset(2));
-  for (int i = tid; i < 288; i += blockDim.x)  // layer 4: [ci][tap] in f32
-    w4[i] = __bfloat162float(wts[cnn_layer_offset(3) + (i / 9) * 9 + i % 9]);
-  for (int i = tid; i < 97; i += blockDim.x) {  // biases: each layer's come last in its block
-    constexpr int kBias0 = cnn_layer_offset(1) - 32, kBias1 = cnn_layer_offset(2) - 32;
-    constexpr int kBias2 = cnn_layer_offset(3) - 32, kBias3 = cnn_layer_offset(4) - 1;
-    const int l = i / 32, c = i % 32;
-    const int o = (l == 0 ? kBias0 : l == 1 ? kBias1 : l == 2 ? kBias2 : kBias3) + c;
-    w4[288 + i] = __bfloat162float(wts[o]);
-  }
-  __syncthreads();
-  // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci
-  for (int i = tid; i < kR1 * 6; i += blockDim.x) {
-    const int p = i / 6, kc = i % 6;
-    __nv_bfloat16 e[8];
-#pragma unroll
-    for (int j = 0; j < 8; j++) {
-      const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
-      float v = 0.0f;
-      if (p < kM1 && k < 36) {
-        const int oy = p / kW1, ox = p % kW1;
-        v = feat[4 * ((oy + tap / 3) * kW0 + ox + tap % 3) + ci];
-      }
-      e[j] = __float2bfloat16_rn(v);
-    }
-    *reinterpret_cast<uint4*>(sm + kOffA1 + ((size_t)kc * kR1 + p) * 16) = *reinterpret_cast<uint4*>(e);
-  }
-  fence_async_smem();
   tc_before();
   __syncthreads();
   tc_after();
   const uint32_t tmem = tmem_slot;
   const uint32_t lane_base = (uint32_t)(32 * (warp & 3)) << 16;
+  uint32_t phase = 0;
   bool ok = true;
 
   // Issues one layer's MMAs (thread 0) and waits for them (everyone).
-  auto run_layer = [&](int layer, int blocks, int taps, int ksteps, uint32_t a_base, uint32_t a_rows, int pitch,
+  auto run_layer = [&](int blocks, int taps, int ksteps, uint32_t a_base, uint32_t a_rows, int pitch,
                        uint32_t w_base) {
     if (tid == 0) {
       const uint32_t id = idesc(128, 32);
@@ -252,99 +224,146 @@ __global__ void __launch_bounds__(256, 1)
           }
       commit(bar);
     }
-    if (!bar_wait(bar, (uint32_t)(layer & 1))) ok = false;
+    if (ok && !bar_wait(bar, phase & 1u)) ok = false;
+    phase++;
     tc_after();
   };
-  const uint32_t base = saddr(sm);
+  auto sync_async = [&]() {  // generic-proxy smem writes visible to the MMAs; TMEM reads done
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+  };
 
-  // ---- layer 1 -> X1 (pitch 22) ---------------------------------------------------------
-  run_layer(0, kB1, 1, 3, base + kOffA1, kR1, 0, base + kOffW1);
-  for (int mb = warp >> 2; mb < kB1; mb += 2) {
-    float v[32];
-    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
-    const int p = mb * 128 + 32 * (warp & 3) + lane;
-    if (p < kM1) {
-      const int oy = p / kW1, ox = p % kW1, gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
-      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
-#pragma unroll
-      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[288 + c], 0.0f) : 0.0f;
-      store_row(sm + kOffX1, kRX1, p, v);
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const int tx0 = (tile % tiles_x) * kT, ty0 = (tile / tiles_x) * kT;
+    // features of the 24 x 24 window (the previous tile's layer 4 is done reading)
+    __syncthreads();
+    for (int i = tid; i < kW0 * kW0; i += blockDim.x) {
+      const int gx = tx0 - 4 + i % kW0, gy = ty0 - 4 + i / kW0;
+      float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
+      if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
+        const long long o = (long long)gy * L.pitch + gx;
+        if ((mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u) {
+          f3 = 1.0f;
+        } else {
+          const float r = rho[o];
+          f0 = (r - 1.0f) * s_rho;
+          f1 = jx[o] / r * s_u;
+          f2 = jy[o] / r * s_u;
+        }
+      }
+      feat[4 * i] = f0;
+      feat[4 * i + 1] = f1;
+      feat[4 * i + 2] = f2;
+      feat[4 * i + 3] = f3;
     }
-  }
-  // rows of X1 beyond the window: zero (read only by dropped outputs, but keep them finite)
-  for (int i = tid; i < 4 * (kRX1 - kM1); i += blockDim.x) {
-    const int c = i / (kRX1 - kM1), r = kM1 + i % (kRX1 - kM1);
-    *reinterpret_cast<uint4*>(sm + kOffX1 + ((size_t)c * kRX1 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
-  }
-  fence_async_smem();
-  tc_before();
-  __syncthreads();
-  tc_after();
-
-  // ---- layer 2 -> X2 (pitch 20) ---------------------------------------------------------
-  run_layer(1, kB2, 9, 2, base + kOffX1, kRX1, kW1, base + kOffW2);
-  for (int mb = warp >> 2; mb < kB2; mb += 2) {
-    float v[32];
-    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
-    const int q = mb * 128 + 32 * (warp & 3) + lane;
-    const int oy = q / kW1, ox = q % kW1;
-    if (q < kM2 && ox < kW2) {
-      const int gx = tx0 - 2 + ox, gy = ty0 - 2 + oy;
-      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+    __syncthreads();
+    // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci
+    for (int i = tid; i < kR1 * 6; i += blockDim.x) {
+      const int p = i / 6, kc = i % 6;
+      __nv_bfloat16 e[8];
 #pragma unroll
-      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[320 + c], 0.0f) : 0.0f;
-      store_row(sm + kOffX2, kRX2, oy * kW2 + ox, v);
+      for (int j = 0; j < 8; j++) {
+        const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
+        float v = 0.0f;
+        if (p < kM1 && k < 36) {
+          const int oy = p / kW1, ox = p % kW1;
+          v = feat[4 * ((oy + tap / 3) * kW0 + ox + tap % 3) + ci];
+        }
+        e[j] = __float2bfloat16_rn(v);
+      }
+      *reinterpret_cast<uint4*>(sm + kOffA1 + ((size_t)kc * kR1 + p) * 16) = *reinterpret_cast<uint4*>(e);
     }
-  }
-  for (int i = tid; i < 4 * (kRX2 - kW2 * kW2); i += blockDim.x) {
-    const int c = i / (kRX2 - kW2 * kW2), r = kW2 * kW2 + i % (kRX2 - kW2 * kW2);
-    *reinterpret_cast<uint4*>(sm + kOffX2 + ((size_t)c * kRX2 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
-  }
-  fence_async_smem();
-  tc_before();
-  __syncthreads();
-  tc_after();
+    sync_async();
 
-  // ---- layer 3 -> X3 (pitch 18, in the im2col region) ------------------------------------
-  run_layer(2, kB3, 9, 2, base + kOffX2, kRX2, kW2, base + kOffW3);
-  for (int mb = warp >> 2; mb < kB3; mb += 2) {
-    float v[32];
-    tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
-    const int q = mb * 128 + 32 * (warp & 3) + lane;
-    const int oy = q / kW2, ox = q % kW2;
-    if (q < kM3 && ox < kW3) {
-      const int gx = tx0 - 1 + ox, gy = ty0 - 1 + oy;
-      const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+    // ---- layer 1 -> X1 (pitch 22) ---------------------------------------------------------
+    run_layer(kB1, 1, 3, base + kOffA1, kR1, 0, base + kOffW1);
+    for (int mb = warp >> 2; mb < kB1; mb += 2) {
+      float v[32];
+      tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+      const int p = mb * 128 + 32 * (warp & 3) + lane;
+      if (p < kM1) {
+        const int oy = p / kW1, ox = p % kW1, gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
+        const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
 #pragma unroll
-      for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[352 + c], 0.0f) : 0.0f;
-      store_row(sm + kOffX3, kRX3, oy * kW3 + ox, v);
-    }
-  }
-  tc_before();
-  __syncthreads();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
-  if (!ok && tid == 0) atomicOr(flag, 2);
-
-  // ---- layer 4 (32 -> 1) on the CUDA cores, record ----------------------------------------
-  {
-    const int oy = tid / kT, ox = tid % kT, gx = tx0 + ox, gy = ty0 + oy;
-    float z = w4[384];
-    for (int tap = 0; tap < 9; tap++) {
-      const int r = (oy + tap / 3) * kW3 + ox + tap % 3;
-#pragma unroll
-      for (int c = 0; c < 4; c++) {
-        const __nv_bfloat16* e = reinterpret_cast<const __nv_bfloat16*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
-#pragma unroll
-        for (int j = 0; j < 8; j++) z = fmaf(__bfloat162float(e[j]), w4[(8 * c + j) * 9 + tap], z);
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[288 + c], 0.0f) : 0.0f;
+        store_row(sm + kOffX1, kRX1, p, v);
       }
     }
-    if (gx < L.nx && gy < L.ny) {
-      const long long o = (long long)gy * L.pitch + gx;
-      const float dt = dt_max / (1.0f + expf(-z));
-      const float r = rho[o], vx = jx[o], vy = jy[o];
-      record[o] = __floats2half2_rn(dt, sqrtf(vx * vx + vy * vy) / r);
+    // rows of X1 beyond the window: zero (read only by dropped outputs, but keep them finite)
+    for (int i = tid; i < 4 * (kRX1 - kM1); i += blockDim.x) {
+      const int c = i / (kRX1 - kM1), r = kM1 + i % (kRX1 - kM1);
+      *reinterpret_cast<uint4*>(sm + kOffX1 + ((size_t)c * kRX1 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    sync_async();
+
+    // ---- layer 2 -> X2 (pitch 20) ---------------------------------------------------------
+    run_layer(kB2, 9, 2, base + kOffX1, kRX1, kW1, base + kOffW2);
+    for (int mb = warp >> 2; mb < kB2; mb += 2) {
+      float v[32];
+      tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+      const int q = mb * 128 + 32 * (warp & 3) + lane;
+      const int oy = q / kW1, ox = q % kW1;
+      if (q < kM2 && ox < kW2) {
+        const int gx = tx0 - 2 + ox, gy = ty0 - 2 + oy;
+        const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+#pragma unroll
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[320 + c], 0.0f) : 0.0f;
+        store_row(sm + kOffX2, kRX2, oy * kW2 + ox, v);
+      }
+    }
+    for (int i = tid; i < 4 * (kRX2 - kW2 * kW2); i += blockDim.x) {
+      const int c = i / (kRX2 - kW2 * kW2), r = kW2 * kW2 + i % (kRX2 - kW2 * kW2);
+      *reinterpret_cast<uint4*>(sm + kOffX2 + ((size_t)c * kRX2 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    sync_async();
+
+    // ---- layer 3 -> X3 (pitch 18, in the im2col region) ------------------------------------
+    run_layer(kB3, 9, 2, base + kOffX2, kRX2, kW2, base + kOffW3);
+    for (int mb = warp >> 2; mb < kB3; mb += 2) {
+      float v[32];
+      tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+      const int q = mb * 128 + 32 * (warp & 3) + lane;
+      const int oy = q / kW2, ox = q % kW2;
+      if (q < kM3 && ox < kW3) {
+        const int gx = tx0 - 1 + ox, gy = ty0 - 1 + oy;
+        const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
+#pragma unroll
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[352 + c], 0.0f) : 0.0f;
+        store_row(sm + kOffX3, kRX3, oy * kW3 + ox, v);
+      }
+    }
+    tc_before();
+    __syncthreads();
+
+    // ---- layer 4 (32 -> 1) on the CUDA cores, record ----------------------------------------
+    {
+      const int oy = tid / kT, ox = tid % kT, gx = tx0 + ox, gy = ty0 + oy;
+      float z = w4[384];
+      for (int tap = 0; tap < 9; tap++) {
+        const int r = (oy + tap / 3) * kW3 + ox + tap % 3;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const __nv_bfloat16* e =
+              reinterpret_cast<const __nv_bfloat16*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
+#pragma unroll
+          for (int j = 0; j < 8; j++) z = fmaf(__bfloat162float(e[j]), w4[(8 * c + j) * 9 + tap], z);
+        }
+      }
+      if (gx < L.nx && gy < L.ny) {
+        const long long o = (long long)gy * L.pitch + gx;
+        const float dt = dt_max / (1.0f + expf(-z));
+        const float r = rho[o], vx = jx[o], vy = jy[o];
+        record[o] = __floats2half2_rn(dt, sqrtf(vx * vx + vy * vy) / r);
+      }
     }
   }
+  tc_before();
+  __syncthreads();
+  tc_after();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (!ok && tid == 0) atomicOr(flag, 2);
 }
 
 }  // namespace lbm

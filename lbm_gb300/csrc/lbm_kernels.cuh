@@ -45,19 +45,29 @@ template <class S, class C> struct StepArgs {
 // `counted`: the cell is a real fluid cell (lanes computing a discarded
 // result pass false and are not counted as fallbacks).
 template <class S, class C>
-__device__ __forceinline__ C cell_omega(const StepArgs<S, C>& a, long long own, C rho, C jx, C jy,
-                                        bool counted = true) {
+__device__ __forceinline__ C cell_omega_rec(const StepArgs<S, C>& a, __half2 rec, C rho, C jx, C jy,
+                                            bool counted = true) {
   if (!a.closure) return a.omega;
-  const float2 r = __half22float2(a.closure[own]);
+  const float2 r = __half22float2(rec);
   const float fr = (float)rho, fx = (float)jx, fy = (float)jy;
-  const float sp = sqrtf(fx * fx + fy * fy) / fr;
-  const bool keep = fabsf(sp - r.y) <= a.drift * fmaxf(r.y, 0.01f) && r.x >= 0.0f && r.x <= 1.0f;
+  // |u| within [lo, hi] compared as |j|^2 against rho^2 [lo^2, hi^2]: no root, no division
+  const float d = a.drift * fmaxf(r.y, 0.01f);
+  const float lo = fmaxf(r.y - d, 0.0f), hi = r.y + d;
+  const float j2 = fx * fx + fy * fy, r2 = fr * fr;
+  const bool keep = j2 >= r2 * (lo * lo) && j2 <= r2 * (hi * hi) && r.x >= 0.0f && r.x <= 1.0f;
   if (a.fallback) {
     const unsigned am = __activemask();
     const unsigned fb = __ballot_sync(am, !keep && counted);
-    if ((threadIdx.x & 31) == __ffs(am) - 1 && fb) atomicAdd(a.fallback, (unsigned long long)__popc(fb));
+    if (fb && (threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(a.fallback, (unsigned long long)__popc(fb));
   }
-  return keep ? (C)(1.0f / (a.tau0 + r.x)) : a.omega;
+  // __frcp_rn is the correctly rounded reciprocal: the same value as 1.0f / x
+  return keep ? (C)__frcp_rn(a.tau0 + r.x) : a.omega;
+}
+
+template <class S, class C>
+__device__ __forceinline__ C cell_omega(const StepArgs<S, C>& a, long long own, C rho, C jx, C jy,
+                                        bool counted = true) {
+  return a.closure ? cell_omega_rec(a, a.closure[own], rho, jx, jy, counted) : a.omega;
 }
 
 __device__ __forceinline__ uint32_t mask_bit(const uint32_t* __restrict__ mask, int mw, int x, int y) {

@@ -200,7 +200,17 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   }
   bool bad = false;
   uint32_t own = (uint32_t)y0 * (uint32_t)L.pitch + (uint32_t)x0;
+  // closure records (global memory) are loaded one row ahead, so their
+  // latency overlaps the stage wait and the previous row's arithmetic
+  __half2 rec[CPT], rec_next[CPT];
+#pragma unroll
+  for (int j = 0; j < CPT; j++) rec_next[j] = a.closure && !producer ? a.closure[own + j] : __half2();
   for (int y = y0; y < y1 && ok; y++, own += (uint32_t)L.pitch) {
+#pragma unroll
+    for (int j = 0; j < CPT; j++) {
+      rec[j] = rec_next[j];
+      if (a.closure && y + 1 < y1) rec_next[j] = a.closure[own + L.pitch + j];
+    }
     if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
     const unsigned char* sm = smem + (size_t)slot_m * G::kBytes;
     const unsigned char* s0 = smem + (size_t)slot_0 * G::kBytes;
@@ -279,7 +289,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
             a.jy_out[own + j] = jy;
           }
         }
-        St::collide(g, rho, aux, jx, jy, cell_omega(a, own + j, rho, jx, jy, act[j]));
+        St::collide(g, rho, aux, jx, jy, cell_omega_rec(a, rec[j], rho, jx, jy, act[j]));
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
       }
