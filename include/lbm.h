@@ -93,10 +93,10 @@ int lbm_get_stream(const lbm_sim* sim, void** cuda_stream);
  * consumer warps per 256-column strip (rows_per_thread is then the minimum
  * band height); 6, 7, 8: the same with rings of 8, 6, 4 stages and two cells
  * per consumer thread (channel mode; reference mode runs one).  Defaults: 3
- * for f32, 8 for f16 / bf16; f64 storage always uses kernel 0.  No
- * counterpart in the
- * reference, whose dispatch is fixed at 256-wide 1-D workgroups
- * (lbm.rs:102-106). */
+ * for f32, 8 for f16 / bf16, with rows_per_thread 8 for kernels 0 / 1 and a
+ * band floor of 2 rows for the staged kernels; f64 storage always uses
+ * kernel 0.  No counterpart in the reference, whose dispatch is fixed at
+ * 256-wide 1-D workgroups (lbm.rs:102-106). */
 int lbm_set_tuning(lbm_sim* sim, int rows_per_thread, int kernel);
 
 /* draw_shape / draw_barrier_updates (lbm.rs:1337-1356, barrier_draw.wgsl:13-17):
@@ -143,12 +143,23 @@ int lbm_single_cell(lbm_sim* sim, int direction);
  * collision (the reference's density_bg after iterate). Asynchronous. */
 int lbm_step(lbm_sim* sim, uint32_t n);
 
+/* Runs of 16 steps inside one lbm_step call are replayed from a CUDA graph
+ * captured on first use (per buffer parity, recaptured when omega, the step
+ * kernel, the stream or the closure change), on by default; results are the
+ * same either way.  Not on the legacy default stream, which cannot be
+ * captured.  enable = 0 turns it off and frees the graphs. */
+int lbm_set_graphs(lbm_sim* sim, int enable);
+
 /* Wait for queued work; returns LBM_ERR_STATE if a step saw a non-finite density. */
 int lbm_synchronize(lbm_sim* sim);
 
 /* set_summary + calculate_summary (lbm.rs:1051-1063) with a real readback:
  * nx*ny floats of LBM_FIELD_* into out. */
 int lbm_read_field(lbm_sim* sim, int field, float* out);
+/* The same into a DEVICE array of nx * ny floats, queued on the handle's
+ * stream without synchronising (for on-device averaging of large grids).
+ * No counterpart in the reference. */
+int lbm_read_field_device(lbm_sim* sim, int field, float* device_out);
 
 /* Current populations (the reference's set compute_step%2 plus the rest plane
  * "origin"): 9 * nx * ny values, plane-major, reference order. */

@@ -77,8 +77,10 @@ _SIGS = [
                                             ctypes.c_uint64]),
     ("lbm_single_cell", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_step", ctypes.c_int, [_P, ctypes.c_uint32]),
+    ("lbm_set_graphs", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_synchronize", ctypes.c_int, [_P]),
     ("lbm_read_field", ctypes.c_int, [_P, ctypes.c_int, _P]),
+    ("lbm_read_field_device", ctypes.c_int, [_P, ctypes.c_int, _P]),
     ("lbm_read_populations", ctypes.c_int, [_P, _P]),
     ("lbm_read_populations_f64", ctypes.c_int, [_P, _P]),
     ("lbm_read_populations_device", ctypes.c_int, [_P, _P]),

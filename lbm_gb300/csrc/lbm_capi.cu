@@ -65,6 +65,19 @@ namespace lbm_internal {
 void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace lbm_internal
 
+constexpr int kStepGraph = 16;  // steps per captured graph (even)
+
+struct StepGraphKey {
+  float omega = 0.0f, drift = 0.0f;
+  int kernel = -1, rows = 0, bands = 0, staged_rows = 0;
+  const void* closure = nullptr;
+  cudaStream_t stream = nullptr;
+  bool operator==(const StepGraphKey& o) const {
+    return omega == o.omega && drift == o.drift && kernel == o.kernel && rows == o.rows && bands == o.bands &&
+           staged_rows == o.staged_rows && closure == o.closure && stream == o.stream;
+  }
+};
+
 struct lbm_sim {
   int device = 0;
   int edge = 0, storage = 0;
@@ -90,7 +103,7 @@ struct lbm_sim {
   bool materialised = true;  // cur holds a pre-collision state
   bool moments_valid = false;
   uint64_t steps = 0, launches = 0;
-  int rows = 8;
+  int rows = 0;    // rows per thread / band floor; 0: 8 for the per-cell kernels, 2 for the staged ones
   int kernel = 2;  // step kernel variant (lbm_set_tuning)
   int sms = 0;     // multiprocessors of the device
   int staged_variant = -1, staged_bands = 0, staged_rows = 0;  // cached launch shape
@@ -103,6 +116,10 @@ struct lbm_sim {
   float drift = 0.5f;
   bool closure_on = false;
   int closure_kernel = 0;  // 0: tensor cores (tcgen05), 1: CUDA cores
+  // captured runs of steps, one per buffer parity (lbm_step)
+  bool use_graphs = true;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  StepGraphKey graph_key[2];
 };
 
 namespace {
@@ -204,6 +221,8 @@ int check_sim(const lbm_sim* s) {
   } while (0)
 
 void release(lbm_sim* s) {
+  for (auto& g : s->graph)
+    if (g) cudaGraphExecDestroy(g);
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
   cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
@@ -228,7 +247,7 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     bands = std::max(1, std::min(bands, s->L.ny));
     // at least `rows` rows per band (the tuning value): short bands re-read
     // their two halo rows too often
-    s->staged_rows = std::max((s->L.ny + bands - 1) / bands, std::min(s->rows, s->L.ny));
+    s->staged_rows = std::max((s->L.ny + bands - 1) / bands, std::min(s->rows > 0 ? s->rows : 2, s->L.ny));
     s->staged_bands = (s->L.ny + s->staged_rows - 1) / s->staged_rows;
     s->staged_variant = s->kernel;
   }
@@ -506,63 +525,142 @@ int lbm_single_cell(lbm_sim* s, int dir) {
   return launch_init(s, 1.0, 0.0, 0.0, 0.0, 0, dir, x + y * X);
 }
 
-int lbm_step(lbm_sim* s, uint32_t n) {
-  CHECK_SIM(s);
-  if (n == 0) return LBM_OK;
-  const int rows = s->rows;
+// One step launch on the handle's stream; `last` writes the moments.
+static int launch_step(lbm_sim* s, bool last) {
+  const int rows = s->rows > 0 ? s->rows : 8;
   // f64 always runs the per-cell kernel: the pipelined and staged variants
   // would spill its doubled register footprint.
   const int variant = s->storage == STORE_F64 ? 0 : s->kernel;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, (s->L.ny + rows - 1) / rows);
-  for (uint32_t k = 0; k < n; k++) {
-    const bool last = k + 1 == n;
-    const int src = s->cur;
-    const int dst = s->materialised ? s->cur : 1 - s->cur;
-    auto launch = [&](auto tag) -> int {
-      using St = decltype(tag);
-      using S = typename St::S;
-      using C = typename St::C;
-      StepArgs<S, C> a;
-      a.L = s->L;
-      a.src = (const S*)s->f[src];
-      a.dst = (S*)s->f[dst];
-      for (int p = 0; p < 8; p++) {
-        a.srcp[p] = a.src + (long long)p * s->L.ps;
-        a.dstp[p] = a.dst + (long long)p * s->L.ps;
+  const int src = s->cur;
+  const int dst = s->materialised ? s->cur : 1 - s->cur;
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    using C = typename St::C;
+    StepArgs<S, C> a;
+    a.L = s->L;
+    a.src = (const S*)s->f[src];
+    a.dst = (S*)s->f[dst];
+    for (int p = 0; p < 8; p++) {
+      a.srcp[p] = a.src + (long long)p * s->L.ps;
+      a.dstp[p] = a.dst + (long long)p * s->L.ps;
+    }
+    a.rest = (S*)s->rest;
+    a.mask = s->mask_d;
+    a.omega = (C)s->omega;
+    a.materialised = s->materialised ? 1 : 0;
+    a.rows = rows;
+    a.rho_out = last ? (C*)mom_plane(s, 0) : nullptr;
+    a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
+    a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
+    a.flag = s->flag_d;
+    a.closure = s->closure_on ? s->closure_d : nullptr;
+    a.tau0 = 1.0f / s->omega;
+    a.drift = s->drift;
+    a.fallback = s->closure_on ? s->fallback_d : nullptr;
+    if (variant >= 2) {
+      return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
+    } else if (variant == 1) {
+      if (s->edge == EDGE_REF) k_step_pf<St, EDGE_REF, 8><<<grid, kBlockX, 0, s->stream>>>(a);
+      else k_step_pf<St, EDGE_CHANNEL, 8><<<grid, kBlockX, 0, s->stream>>>(a);
+    } else {
+      if (s->edge == EDGE_REF) k_step<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(a);
+      else k_step<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(a);
+    }
+    CK_LAUNCH();
+    return LBM_OK;
+  };
+  int rc = dispatch_storage(s->storage, launch);
+  if (rc) return rc;
+  s->launches++;
+  s->cur = dst;
+  s->materialised = false;
+  s->steps++;
+  return LBM_OK;
+}
+
+// Everything a captured run of steps depends on besides the buffers.
+static StepGraphKey graph_key(const lbm_sim* s) {
+  StepGraphKey k;
+  k.omega = s->omega;
+  k.kernel = s->kernel;
+  k.rows = s->rows;
+  k.closure = s->closure_on ? (const void*)s->closure_d : nullptr;
+  k.drift = s->drift;
+  k.stream = s->stream;
+  k.bands = s->staged_bands;
+  k.staged_rows = s->staged_rows;
+  return k;
+}
+
+static void drop_step_graphs(lbm_sim* s) {
+  for (auto& g : s->graph)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// Capture kStepGraph steps (no moments) from the current buffer parity.
+static int capture_steps(lbm_sim* s) {
+  cudaGraphExec_t& out = s->graph[s->cur];
+  if (out) {
+    cudaGraphExecDestroy(out);
+    out = nullptr;
+  }
+  const int cur0 = s->cur;
+  const uint64_t steps0 = s->steps, launches0 = s->launches;
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = LBM_OK;
+  for (int k = 0; k < kStepGraph && !rc; k++) rc = launch_step(s, false);
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  s->cur = cur0;  // the capture recorded the launches without running them
+  s->steps = steps0;
+  s->launches = launches0;
+  s->materialised = false;
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "stream capture: %s", cudaGetErrorString(e));
+  const cudaError_t ei = cudaGraphInstantiate(&out, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) return fail(LBM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
+  s->graph_key[s->cur] = graph_key(s);
+  return LBM_OK;
+}
+
+int lbm_step(lbm_sim* s, uint32_t n) {
+  CHECK_SIM(s);
+  if (n == 0) return LBM_OK;
+  for (uint32_t k = 0; k < n;) {
+    const uint32_t left = n - k;
+    // runs of kStepGraph steps replay a captured graph: launch overhead
+    // dominates small grids (the legacy default stream cannot be captured)
+    const bool steady = !s->materialised && (s->storage == STORE_F64 || s->kernel < 2 ||
+                                             s->staged_variant == s->kernel);
+    if (s->use_graphs && steady && s->stream != nullptr && left > (uint32_t)kStepGraph) {
+      if (!s->graph[s->cur] || !(s->graph_key[s->cur] == graph_key(s))) {
+        int rc = capture_steps(s);
+        if (rc) return rc;
       }
-      a.rest = (S*)s->rest;
-      a.mask = s->mask_d;
-      a.omega = (C)s->omega;
-      a.materialised = s->materialised ? 1 : 0;
-      a.rows = rows;
-      a.rho_out = last ? (C*)mom_plane(s, 0) : nullptr;
-      a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
-      a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
-      a.flag = s->flag_d;
-      a.closure = s->closure_on ? s->closure_d : nullptr;
-      a.tau0 = 1.0f / s->omega;
-      a.drift = s->drift;
-      a.fallback = s->closure_on ? s->fallback_d : nullptr;
-      if (variant >= 2) {
-        return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
-      } else if (variant == 1) {
-        if (s->edge == EDGE_REF) k_step_pf<St, EDGE_REF, 8><<<grid, kBlockX, 0, s->stream>>>(a);
-        else k_step_pf<St, EDGE_CHANNEL, 8><<<grid, kBlockX, 0, s->stream>>>(a);
-      } else {
-        if (s->edge == EDGE_REF) k_step<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(a);
-        else k_step<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(a);
-      }
-      CK_LAUNCH();
-      return LBM_OK;
-    };
-    int rc = dispatch_storage(s->storage, launch);
+      CK(cudaGraphLaunch(s->graph[s->cur], s->stream));
+      s->steps += kStepGraph;  // even: the buffer parity is unchanged
+      s->launches += kStepGraph;
+      k += kStepGraph;
+      continue;
+    }
+    int rc = launch_step(s, k + 1 == n);
     if (rc) return rc;
-    s->launches++;
-    s->cur = dst;
-    s->materialised = false;
-    s->steps++;
+    k++;
   }
   s->moments_valid = true;
+  return LBM_OK;
+}
+
+int lbm_set_graphs(lbm_sim* s, int enable) {
+  CHECK_SIM(s);
+  s->use_graphs = enable != 0;
+  if (!s->use_graphs) drop_step_graphs(s);
   return LBM_OK;
 }
 
@@ -576,7 +674,7 @@ int lbm_synchronize(lbm_sim* s) {
   return LBM_OK;
 }
 
-int lbm_read_field(lbm_sim* s, int field, float* out) {
+static int read_field(lbm_sim* s, int field, float* out, bool device_out) {
   CHECK_SIM(s);
   if (!out) return fail(LBM_ERR_ARG, "out is null");
   if (field < 0 || field > 7) return fail(LBM_ERR_ARG, "bad field %d", field);
@@ -588,7 +686,7 @@ int lbm_read_field(lbm_sim* s, int field, float* out) {
     if (rc) return rc;
   }
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
-  float* tmp = s->staging_d;
+  float* tmp = device_out ? out : s->staging_d;
   if (s->storage == STORE_F64)
     k_field<double><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const double*)mom_plane(s, 0),
                                                     (const double*)mom_plane(s, 1), (const double*)mom_plane(s, 2), tmp);
@@ -597,10 +695,14 @@ int lbm_read_field(lbm_sim* s, int field, float* out) {
                                                    (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), tmp);
   CK_LAUNCH();
   s->launches++;
+  if (device_out) return LBM_OK;
   CK(cudaMemcpyAsync(out, tmp, (size_t)s->L.nx * s->L.ny * 4, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }
+
+int lbm_read_field(lbm_sim* s, int field, float* out) { return read_field(s, field, out, false); }
+int lbm_read_field_device(lbm_sim* s, int field, float* device_out) { return read_field(s, field, device_out, true); }
 
 // Populations of the current state, plane-major, into `out`: a host array
 // (through the staging buffer, synchronising) or, with device_out, a device

@@ -259,20 +259,20 @@ __global__ void __launch_bounds__(256, 1)
       feat[4 * i + 3] = f3;
     }
     __syncthreads();
-    // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci
+    // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci; chunk kc holds
+    // taps 2 kc and 2 kc + 1.  Pixel-fastest order: a warp reads and writes
+    // consecutive 16-byte rows (no bank conflicts).
     for (int i = tid; i < kR1 * 6; i += blockDim.x) {
-      const int p = i / 6, kc = i % 6;
-      __nv_bfloat16 e[8];
-#pragma unroll
-      for (int j = 0; j < 8; j++) {
-        const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
-        float v = 0.0f;
-        if (p < kM1 && k < 36) {
-          const int oy = p / kW1, ox = p % kW1;
-          v = feat[4 * ((oy + tap / 3) * kW0 + ox + tap % 3) + ci];
-        }
-        e[j] = __float2bfloat16_rn(v);
+      const int kc = i / kR1, p = i % kR1;
+      float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
+      if (p < kM1) {
+        const int oy = p / kW1, ox = p % kW1, t0 = 2 * kc, t1 = 2 * kc + 1;
+        const float4* f4 = reinterpret_cast<const float4*>(feat);
+        if (t0 < 9) a = f4[(oy + t0 / 3) * kW0 + ox + t0 % 3];
+        if (t1 < 9) b = f4[(oy + t1 / 3) * kW0 + ox + t1 % 3];
       }
+      __nv_bfloat162 e[4] = {__floats2bfloat162_rn(a.x, a.y), __floats2bfloat162_rn(a.z, a.w),
+                             __floats2bfloat162_rn(b.x, b.y), __floats2bfloat162_rn(b.z, b.w)};
       *reinterpret_cast<uint4*>(sm + kOffA1 + ((size_t)kc * kR1 + p) * 16) = *reinterpret_cast<uint4*>(e);
     }
     sync_async();
@@ -345,10 +345,14 @@ __global__ void __launch_bounds__(256, 1)
         const int r = (oy + tap / 3) * kW3 + ox + tap % 3;
 #pragma unroll
         for (int c = 0; c < 4; c++) {
-          const __nv_bfloat16* e =
-              reinterpret_cast<const __nv_bfloat16*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
+          const uint4 raw = *reinterpret_cast<const uint4*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
+          const __nv_bfloat162* e = reinterpret_cast<const __nv_bfloat162*>(&raw);
 #pragma unroll
-          for (int j = 0; j < 8; j++) z = fmaf(__bfloat162float(e[j]), w4[(8 * c + j) * 9 + tap], z);
+          for (int j = 0; j < 4; j++) {
+            const float2 v = __bfloat1622float2(e[j]);
+            z = fmaf(v.x, w4[(8 * c + 2 * j) * 9 + tap], z);
+            z = fmaf(v.y, w4[(8 * c + 2 * j + 1) * 9 + tap], z);
+          }
         }
       }
       if (gx < L.nx && gy < L.ny) {

@@ -66,13 +66,18 @@ def random_circles(nx, ny, count, rmin, rmax, seed, inlet_clearance=64, target_f
     rng = SplitMix64(seed)
     m = np.zeros((ny, nx), np.uint8)
     placed = 0
+    solid = 0  # running count of solid cells (only the disk's bounding box changes)
     while placed < count:
         r = rng.uniform(rmin, rmax)
         cx = rng.uniform(inlet_clearance + r, nx - 1)
         cy = rng.uniform(0, ny - 1)
+        y0, y1 = max(int(np.floor(cy - r)), 0), min(int(np.ceil(cy + r)), ny - 1) + 1
+        x0, x1 = max(int(np.floor(cx - r)), 0), min(int(np.ceil(cx + r)), nx - 1) + 1
+        before = int(m[y0:y1, x0:x1].sum())
         disk(m, cx, cy, r)
+        solid += int(m[y0:y1, x0:x1].sum()) - before
         placed += 1
-        if target_fraction is not None and m.mean() >= target_fraction:
+        if target_fraction is not None and solid >= target_fraction * m.size:
             break
     return m
 

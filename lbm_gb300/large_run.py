@@ -1,0 +1,130 @@
+"""The large-grid workload: 16384 x 8192 channel, seeded circles (~8 % solid,
+radii 8-64), inlet ux 0.05, tau 0.51, run three ways on one GPU:
+
+* f32 plain BGK (the reference's arithmetic),
+* f16 (f - w) storage, plain BGK,
+* f16 storage with the learned closure (weights from a train_closure .npz),
+  refreshed every `--refresh` steps by the tensor-core inference kernel.
+
+    python -m lbm_gb300.large_run --closure closure.npz [--steps 50000] [--every 100]
+
+For each run it reports MLUPS, achieved HBM GB/s on the step kernel
+(algorithmic bytes: 72 B per active cell in f32, 36 B in f16, +4 B of
+closure records), the relative FP64 drift of the fluid mass and momentum
+sums from the first to the last step, and the time-averaged velocity over
+the second half.  The f16 runs' time-averaged velocities are compared with
+the f32 run's (relative L2 over fluid cells).  Velocity averages stay on the
+device (lbm_read_field_device); the timed region holds only steps and
+inferences.  Prints one JSON line.
+"""
+import argparse
+import ctypes
+import json
+import time
+
+import numpy as np
+
+from . import EDGE_CHANNEL, F16, F32, LBMError, Lattice, _check, load_library
+from .geometry import random_circles
+
+
+def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, drift=1.0, seed=1):
+    import torch
+    lib = load_library()
+    stream = torch.cuda.Stream()
+    dev = torch.device("cuda")
+    acc = torch.zeros((2, ny, nx), dtype=torch.float32, device=dev)
+    tmp = torch.empty((ny, nx), dtype=torch.float32, device=dev)
+    active = int((mask[:, 1:] == 0).sum())
+    out = {"storage": "f32" if storage == F32 else "f16", "closure": params is not None}
+    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
+        lat.set_stream(stream.cuda_stream)
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, 1e-4, seed)
+        lat.draw_mask(mask)
+        if params is not None:
+            p = np.ascontiguousarray(params, np.float32)
+            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
+            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
+        lat.iterate(1)
+        c0 = lat.conservation()
+        done, n_avg, dev_ms = 1, 0, 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        while done < steps:
+            k = min(every, steps - done)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            left = k
+            while left > 0:
+                c = min(left, refresh) if params is not None else left
+                if params is not None:
+                    _check(lib.lbm_closure_infer(lat.handle))
+                lat.iterate(c)
+                left -= c
+            e1.record(stream)
+            torch.cuda.synchronize()
+            dev_ms += e0.elapsed_time(e1)
+            done += k
+            if done > steps // 2:
+                for i, f in enumerate((3, 4)):  # ux, uy of the last step's moments
+                    _check(lib.lbm_read_field_device(lat.handle, f, ctypes.c_void_p(tmp.data_ptr())))
+                    acc[i] += tmp
+                n_avg += 1
+        torch.cuda.synchronize()
+        try:
+            lat.synchronize()
+            out["finite"] = True
+        except LBMError:
+            out["finite"] = False
+        c1 = lat.conservation()
+        if params is not None:
+            fb = ctypes.c_uint64(0)
+            _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
+            out["fallback_fraction"] = fb.value / max(active * (steps - 1), 1)
+    timed = steps - 1
+    bpc = (72 if storage == F32 else 36) + (4 if params is not None else 0)
+    out.update({"steps": steps, "ms_per_step": dev_ms / timed, "mlups": nx * ny * timed / (dev_ms * 1e-3) / 1e6,
+                "achieved_gbs": bpc * active * timed / (dev_ms * 1e-3) / 1e9,
+                "mass_drift": float((c1[0] - c0[0]) / c0[0]),
+                "momentum_x_drift": float((c1[1] - c0[1]) / c0[1]) if c0[1] else None})
+    return out, (acc / max(n_avg, 1)).cpu().numpy()
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--size", type=int, nargs=2, default=[16384, 8192])
+    ap.add_argument("--steps", type=int, default=50000)
+    ap.add_argument("--every", type=int, default=100)
+    ap.add_argument("--tau", type=float, default=0.51)
+    ap.add_argument("--u", type=float, default=0.05)
+    ap.add_argument("--closure", default=None, help="train_closure output (.npz)")
+    ap.add_argument("--refresh", type=int, default=20)
+    ap.add_argument("--seed", type=int, default=1)
+    a = ap.parse_args(argv)
+    nx, ny = a.size
+    mask = random_circles(nx, ny, 10 ** 7, 8, 64, a.seed, inlet_clearance=64, target_fraction=0.08)
+    rep = {"workload": "D2Q9 channel %dx%d, circles r 8-64, %.1f%% solid, tau %.2f, ux %.2f" %
+           (nx, ny, 100 * mask.mean(), a.tau, a.u)}
+    t0 = time.time()
+    r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed)
+    r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed)
+    fl = mask == 0
+    fl[:, 0] = False
+
+    def err(u):
+        d = (u - u32)[:, fl]
+        return float(np.linalg.norm(d) / np.linalg.norm(u32[:, fl])) if np.isfinite(d).all() else float("inf")
+
+    r16["vel_err_vs_f32"] = err(u16)
+    rep["runs"] = [r32, r16]
+    if a.closure:
+        params = np.load(a.closure)["params"]
+        rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh, seed=a.seed)
+        rc["vel_err_vs_f32"] = err(uc)
+        rep["runs"].append(rc)
+    rep["wall_s"] = time.time() - t0
+    print(json.dumps(rep))
+
+
+if __name__ == "__main__":
+    main()

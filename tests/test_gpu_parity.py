@@ -244,3 +244,31 @@ def test_gpu_full_size_channel_matches_oracle(lbm, cuda_ok, oracle_mod):
     np.testing.assert_array_equal(lat.field("rho"), rho.astype(np.float32))
     np.testing.assert_array_equal(lat.field("jx"), jx.astype(np.float32))
     lat.close()
+
+
+@pytest.mark.parametrize("kernel", [0, 1, 3, 8])
+def test_gpu_graph_replay_is_transparent(lbm, cuda_ok, oracle_mod, kernel):
+    """Runs of steps replayed from captured graphs (the default) give the same
+    state as plain launches, across an omega change between calls (which must
+    recapture) and against the oracle."""
+    P = oracle_mod
+    nx, ny = 130, 70
+    rng = np.random.default_rng(11)
+    mask = (rng.random((ny, nx)) < 0.06).astype(np.uint8)
+    L = lbm.load_library()
+    states = []
+    for graphs in (1, 0):
+        lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, lbm.F32 if kernel != 8 else lbm.F16,
+                          P.P_F32 if kernel != 8 else P.P_F16, 0, mask, kernel=kernel)
+        lbm._check(L.lbm_set_graphs(lat.handle, graphs))
+        lat.iterate(53)
+        o.step(53)
+        w = float(np.float32(1.0 / 0.7))
+        lat.update_omega_buffer(w)
+        o.set_omega(w)
+        lat.iterate(41)
+        o.step(41)
+        assert_same_state(lat, o)
+        states.append(lat.populations())
+        lat.close()
+    np.testing.assert_array_equal(states[0], states[1])
