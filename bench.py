@@ -421,6 +421,47 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_case(case):
+    """Small fixed workloads for ncu captures of the batched and closure kernels."""
+    import ctypes
+    import numpy as np
+    import lbm_gb300 as lbm
+    from lbm_gb300 import build as B
+    B.build()
+    lbm.load_library()
+    if case == "batched64":
+        from lbm_gb300 import batch
+        nx, ny, om, u, masks = batch.batched_workload(64, 1)
+        with batch.Batch(nx, ny, om, u, lbm.F32) as b:
+            for d, m in enumerate(masks):
+                b.set_mask(d, m)
+            b.set_schedule(0, 1, [32, 32, 32])
+            b.init_equilibrium(1e-3, 1)
+            b.step(12)
+            try:
+                b.synchronize()
+            except lbm.LBMError:
+                pass
+        print(json.dumps({"case": case, "cells": int((nx.astype(np.int64) * ny).sum())}))
+    else:
+        from lbm_gb300 import closure, geometry
+        L = lbm.load_library()
+        w = closure.init_params(3)
+        nx, ny = 2048, 1024
+        mask = geometry.random_circles(nx, ny, 10 ** 6, 8, 16, 1, target_fraction=0.08)
+        with lbm.Lattice(nx, ny, 1 / 0.51, lbm.EDGE_CHANNEL, lbm.F32) as lat:
+            lat.set_inlet_velocity(0.05)
+            lat.init_equilibrium(1, 0.05, 0, 1e-3, 1)
+            lat.draw_mask(mask)
+            lat.iterate(20)
+            lbm._check(L.lbm_closure_set_weights(lat.handle, w.ctypes.data_as(ctypes.c_void_p), w.size))
+            lbm._check(L.lbm_closure_enable(lat.handle, 1.0))
+            for _ in range(4):
+                lbm._check(L.lbm_closure_infer(lat.handle))
+            lat.synchronize()
+        print(json.dumps({"case": case, "cells": nx * ny}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -434,9 +475,15 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
                     help="time only the step kernel of one storage format (profiling runs)")
+    ap.add_argument("--case", choices=["batched64", "closure2048"], default=None,
+                    help="small fixed cases for kernel profiles: 64 batched domains (f32, 12 steps) or the "
+                         "closure inference on a 2048x1024 lattice (4 launches)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.case:
+        run_case(args.case)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:

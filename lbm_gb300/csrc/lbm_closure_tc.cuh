@@ -1,15 +1,16 @@
 // Learned closure inference on the 5th-generation tensor cores: the whole
 // network per 16 x 16 tile in shared memory, the three 32-channel layers as
 // implicit GEMMs issued with tcgen05.mma (BF16 operands from shared memory,
-// f32 accumulators in tensor memory), the 1-channel output layer on the CUDA
-// cores.
+// f32 accumulators in tensor memory), and the 1-channel output layer as a
+// fourth GEMM with its weights padded to 16 outputs.
 //
 // GEMM shapes per tile (M = window pixels, N = 32 output channels):
 //   layer 1  M = 22 x 22 (4 blocks of 128), K = 9 taps x 4 channels, padded
 //            to 48; its A operand is an explicit im2col of the features;
 //   layer 2  M = 20 rows x 22 (the input window's pitch), K = 9 x 32;
-//   layer 3  M = 18 rows x 20, K = 9 x 32.
-// For layers 2 and 3 the A operand of tap (ky, kx) is the input activation
+//   layer 3  M = 18 rows x 20, K = 9 x 32;
+//   layer 4  M = 16 rows x 18, K = 9 x 32, N = 16 (one real output).
+// For layers 2 to 4 the A operand of tap (ky, kx) is the input activation
 // buffer itself viewed from row offset ky * pitch + kx: output pixel q =
 // oy * pitch + ox reads input pixel q + ky * pitch + kx, so each tap is one
 // shared-memory descriptor with a shifted start address (the two columns per
@@ -47,7 +48,9 @@ constexpr int kK1 = 48;                // layer-1 K (36 used)
 constexpr int kR1 = kB1 * 128;                          // im2col rows
 constexpr int kRX1 = kB2 * 128 + 2 * kW1 + 2 + 6;       // layer-1 output, pitch 22 (= 564)
 constexpr int kRX2 = kB3 * 128 + 2 * kW2 + 2 + 6;       // layer-2 output, pitch 20 (= 432)
-constexpr int kRX3 = kW3 * kW3;                         // layer-3 output, pitch 18 (= 324)
+constexpr int kM4 = kT * kW3;           // 288 rows of layer 4 (pitch 18)
+constexpr int kB4 = 3;
+constexpr int kRX3 = kB4 * 128 + 2 * kW3 + 2 + 2;       // layer-3 output, pitch 18 (= 424)
 
 // byte offsets in dynamic shared memory
 constexpr uint32_t kOffA1 = 0;                                  // [6][512][8] bf16
@@ -57,14 +60,15 @@ constexpr uint32_t kOffX2 = kOffX1 + 4u * kRX1 * 16u;           // [4][432][8]
 constexpr uint32_t kOffW1 = kOffX2 + 4u * kRX2 * 16u;           // [6][32][8] bf16
 constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8] bf16
 constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;           // [36][32][8] bf16
-constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // f32 [288] layer 4 [ci][tap], then b1 b2 b3 (32 each), b4
-constexpr uint32_t kPackedBytes = kOffW4 + 1552u - kOffW1;      // 385 floats, padded to 16 B
+constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // [36][16][8] bf16: layer 4 padded to 16 outputs
+constexpr uint32_t kOffBias = kOffW4 + 36u * 16u * 16u;         // f32 b1 b2 b3 (32 each), b4
+constexpr uint32_t kPackedBytes = kOffBias + 400u - kOffW1;     // 97 floats, padded to 16 B
 constexpr uint32_t kOffFeat = kOffW1 + kPackedBytes;            // f32 [576][4]
 constexpr uint32_t kOffBar = kOffFeat + kW0 * kW0 * 16u;        // mbarrier (8 B), tensor-memory address (4 B)
 constexpr uint32_t kUsed = kOffBar + 16u;
 constexpr uint32_t kSmem = 232448u;  // 227 KB: the whole opt-in window (see above); no static shared memory
 static_assert(kUsed <= kSmem, "closure tile does not fit in shared memory");
-static_assert(kPackedBytes % 16 == 0 && 385u * 4u <= 1552u, "packed parameter block");
+static_assert(kPackedBytes % 16 == 0 && 97u * 4u <= 400u, "packed parameter block");
 // layer-3 output reuses the im2col region
 constexpr uint32_t kOffX3 = kOffA1;
 static_assert(4u * kRX3 * 16u <= 6u * kR1 * 16u, "layer-3 output overlaps");
@@ -90,12 +94,18 @@ inline void pack_weights(const float* p, unsigned char* out) {
           w[(kc * 32 + co) * 8 + j] = bf(p[cnn_layer_offset(l) + (co * 32 + ci) * 9 + tap]);
         }
   }
-  float* w4 = reinterpret_cast<float*>(out + kOffW4 - kOffW1);
-  for (int i = 0; i < 288; i++) w4[i] = __bfloat162float(bf(p[cnn_layer_offset(3) + i]));
-  const int bias[4] = {cnn_layer_offset(1) - 32, cnn_layer_offset(2) - 32, cnn_layer_offset(3) - 32,
+  __nv_bfloat16* w4 = reinterpret_cast<__nv_bfloat16*>(out + kOffW4 - kOffW1);  // output 0 real, 1..15 zero
+  for (int kc = 0; kc < 36; kc++)
+    for (int co = 0; co < 16; co++)
+      for (int j = 0; j < 8; j++) {
+        const int tap = kc / 4, ci = (kc % 4) * 8 + j;
+        w4[(kc * 16 + co) * 8 + j] = bf(co == 0 ? p[cnn_layer_offset(3) + ci * 9 + tap] : 0.0f);
+      }
+  float* bias = reinterpret_cast<float*>(out + kOffBias - kOffW1);
+  const int boff[4] = {cnn_layer_offset(1) - 32, cnn_layer_offset(2) - 32, cnn_layer_offset(3) - 32,
                        cnn_layer_offset(4) - 1};
-  for (int i = 0; i < 97; i++) w4[288 + i] = __bfloat162float(bf(p[bias[i / 32] + i % 32]));
-  for (int i = 385; i < 388; i++) w4[i] = 0.0f;
+  for (int i = 0; i < 97; i++) bias[i] = __bfloat162float(bf(p[boff[i / 32] + i % 32]));
+  for (int i = 97; i < 100; i++) bias[i] = 0.0f;
 }
 
 __device__ __forceinline__ uint32_t saddr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -182,7 +192,7 @@ __global__ void __launch_bounds__(256, 1)
   uint32_t& tmem_slot = *reinterpret_cast<uint32_t*>(sm + kOffBar + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   float* feat = reinterpret_cast<float*>(sm + kOffFeat);
-  float* w4 = reinterpret_cast<float*>(sm + kOffW4);  // [ci][tap] then biases b1, b2, b3, b4
+  const float* bias = reinterpret_cast<const float*>(sm + kOffBias);  // b1, b2, b3 (32 each), b4
   const uint32_t bar = saddr(sm + kOffBar);
   const uint32_t base = saddr(sm);
   const int tiles_x = (L.nx + kT - 1) / kT, tiles = tiles_x * ((L.ny + kT - 1) / kT);
@@ -210,16 +220,17 @@ __global__ void __launch_bounds__(256, 1)
 
   // Issues one layer's MMAs (thread 0) and waits for them (everyone).
   auto run_layer = [&](int blocks, int taps, int ksteps, uint32_t a_base, uint32_t a_rows, int pitch,
-                       uint32_t w_base) {
+                       uint32_t w_base, int n = 32) {
     if (tid == 0) {
-      const uint32_t id = idesc(128, 32);
+      const uint32_t id = idesc(128, n);
+      const uint32_t wchunk = (uint32_t)n * 16u;  // bytes of one 8-wide K chunk of the weights
       for (int mb = 0; mb < blocks; mb++)
         for (int t = 0; t < taps; t++)
           for (int s = 0; s < ksteps; s++) {
             const uint32_t shift = (uint32_t)(mb * 128 + (taps == 9 ? (t / 3) * pitch + t % 3 : 0));
             const uint32_t kc = (uint32_t)(taps == 9 ? t * 4 + 2 * s : 2 * s);
             const uint64_t a = sdesc(a_base + (uint32_t)(2 * s) * a_rows * 16u + shift * 16u, a_rows * 16u, 128u);
-            const uint64_t b = sdesc(w_base + kc * 512u, 512u, 128u);
+            const uint64_t b = sdesc(w_base + kc * wchunk, wchunk, 128u);
             mma(tmem + (uint32_t)(mb * 32), a, b, id, (t > 0 || s > 0) ? 1u : 0u);
           }
       commit(bar);
@@ -235,30 +246,55 @@ __global__ void __launch_bounds__(256, 1)
     tc_after();
   };
 
+  // The features of a tile's 24 x 24 window: each thread owns window cells
+  // tid, tid + 256, tid + 512.  The next tile's are loaded into registers
+  // while the current tile's layers run, so their latency is hidden.
+  constexpr int kFeatPer = (kW0 * kW0 + 255) / 256;
+  float4 fv[kFeatPer];
+  auto load_feats = [&](int t) {
+    const int fx0 = (t % tiles_x) * kT - 4, fy0 = (t / tiles_x) * kT - 4;
+#pragma unroll
+    for (int k = 0; k < kFeatPer; k++) {
+      const int i = tid + 256 * k;
+      float4 f = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      if (i < kW0 * kW0 && t < tiles) {
+        const int gx = fx0 + i % kW0, gy = fy0 + i / kW0;
+        if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
+          const long long o = (long long)gy * L.pitch + gx;
+          if ((mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u) {
+            f.w = 1.0f;
+          } else {  // raw moments now, scaled when stored
+            f.x = rho[o];
+            f.y = jx[o];
+            f.z = jy[o];
+            f.w = -1.0f;  // fluid marker
+          }
+        }
+      }
+      fv[k] = f;
+    }
+  };
+  load_feats(blockIdx.x);
+
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int tx0 = (tile % tiles_x) * kT, ty0 = (tile / tiles_x) * kT;
     // features of the 24 x 24 window (the previous tile's layer 4 is done reading)
     __syncthreads();
-    for (int i = tid; i < kW0 * kW0; i += blockDim.x) {
-      const int gx = tx0 - 4 + i % kW0, gy = ty0 - 4 + i / kW0;
-      float f0 = 0.0f, f1 = 0.0f, f2 = 0.0f, f3 = 0.0f;
-      if (gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny) {
-        const long long o = (long long)gy * L.pitch + gx;
-        if ((mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u) {
-          f3 = 1.0f;
-        } else {
-          const float r = rho[o];
-          f0 = (r - 1.0f) * s_rho;
-          f1 = jx[o] / r * s_u;
-          f2 = jy[o] / r * s_u;
-        }
+#pragma unroll
+    for (int k = 0; k < kFeatPer; k++) {
+      const int i = tid + 256 * k;
+      if (i >= kW0 * kW0) continue;
+      const float4 f = fv[k];
+      float4 o = make_float4(0.0f, 0.0f, 0.0f, f.w > 0.0f ? 1.0f : 0.0f);
+      if (f.w < 0.0f) {
+        o.x = (f.x - 1.0f) * s_rho;
+        o.y = f.y / f.x * s_u;
+        o.z = f.z / f.x * s_u;
       }
-      feat[4 * i] = f0;
-      feat[4 * i + 1] = f1;
-      feat[4 * i + 2] = f2;
-      feat[4 * i + 3] = f3;
+      reinterpret_cast<float4*>(feat)[i] = o;
     }
     __syncthreads();
+    load_feats(tile + gridDim.x);  // in flight while this tile's layers run
     // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci; chunk kc holds
     // taps 2 kc and 2 kc + 1.  Pixel-fastest order: a warp reads and writes
     // consecutive 16-byte rows (no bank conflicts).
@@ -287,7 +323,7 @@ __global__ void __launch_bounds__(256, 1)
         const int oy = p / kW1, ox = p % kW1, gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
         const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
 #pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[288 + c], 0.0f) : 0.0f;
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + bias[c], 0.0f) : 0.0f;
         store_row(sm + kOffX1, kRX1, p, v);
       }
     }
@@ -309,7 +345,7 @@ __global__ void __launch_bounds__(256, 1)
         const int gx = tx0 - 2 + ox, gy = ty0 - 2 + oy;
         const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
 #pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[320 + c], 0.0f) : 0.0f;
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + bias[32 + c], 0.0f) : 0.0f;
         store_row(sm + kOffX2, kRX2, oy * kW2 + ox, v);
       }
     }
@@ -330,38 +366,32 @@ __global__ void __launch_bounds__(256, 1)
         const int gx = tx0 - 1 + ox, gy = ty0 - 1 + oy;
         const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
 #pragma unroll
-        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + w4[352 + c], 0.0f) : 0.0f;
+        for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + bias[64 + c], 0.0f) : 0.0f;
         store_row(sm + kOffX3, kRX3, oy * kW3 + ox, v);
       }
     }
-    tc_before();
-    __syncthreads();
+    for (int i = tid; i < 4 * (kRX3 - kW3 * kW3); i += blockDim.x) {
+      const int c = i / (kRX3 - kW3 * kW3), r = kW3 * kW3 + i % (kRX3 - kW3 * kW3);
+      *reinterpret_cast<uint4*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    sync_async();
 
-    // ---- layer 4 (32 -> 1) on the CUDA cores, record ----------------------------------------
-    {
-      const int oy = tid / kT, ox = tid % kT, gx = tx0 + ox, gy = ty0 + oy;
-      float z = w4[384];
-      for (int tap = 0; tap < 9; tap++) {
-        const int r = (oy + tap / 3) * kW3 + ox + tap % 3;
-#pragma unroll
-        for (int c = 0; c < 4; c++) {
-          const uint4 raw = *reinterpret_cast<const uint4*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16);
-          const __nv_bfloat162* e = reinterpret_cast<const __nv_bfloat162*>(&raw);
-#pragma unroll
-          for (int j = 0; j < 4; j++) {
-            const float2 v = __bfloat1622float2(e[j]);
-            z = fmaf(v.x, w4[(8 * c + 2 * j) * 9 + tap], z);
-            z = fmaf(v.y, w4[(8 * c + 2 * j + 1) * 9 + tap], z);
-          }
-        }
-      }
-      if (gx < L.nx && gy < L.ny) {
+    // ---- layer 4 (32 -> 1, padded to N = 16) -> record ----------------------------------------
+    run_layer(kB4, 9, 2, base + kOffX3, kRX3, kW3, base + kOffW4, 16);
+    for (int mb = warp >> 2; mb < kB4; mb += 2) {
+      float v[32];
+      tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
+      const int q = mb * 128 + 32 * (warp & 3) + lane;
+      const int oy = q / kW3, ox = q % kW3, gx = tx0 + ox, gy = ty0 + oy;
+      if (q < kM4 && ox < kT && gx < L.nx && gy < L.ny) {
         const long long o = (long long)gy * L.pitch + gx;
+        const float z = v[0] + bias[96];
         const float dt = dt_max / (1.0f + expf(-z));
-        const float r = rho[o], vx = jx[o], vy = jy[o];
-        record[o] = __floats2half2_rn(dt, sqrtf(vx * vx + vy * vy) / r);
+        const float4 f = reinterpret_cast<const float4*>(feat)[(oy + 4) * kW0 + ox + 4];  // |u| from the features
+        record[o] = __floats2half2_rn(dt, sqrtf(f.y * f.y + f.z * f.z) / s_u);
       }
     }
+    tc_before();  // the next tile's MMAs reuse the tensor memory
   }
   tc_before();
   __syncthreads();

@@ -140,6 +140,12 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 
   if (producer) {
     if ((tid & 31) == 0) {
+      // a strip narrower than kStageW (the grid's last) copies only its own
+      // columns and halo, rounded up to 16 bytes; stage offsets stay fixed
+      const int w = min(kStageW, L.nx - xb);
+      const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
+      const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
+      const uint32_t stage_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes;
       int r = r_first, s = 0;
       uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
       bool ok = true;
@@ -153,12 +159,12 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         else rr = min(max(rr, 0), L.ny - 1);
         unsigned char* st = smem + (size_t)s * G::kBytes;
         const uint32_t bar = smem_addr(&full[s]);
-        mbar_arrive_expect_tx(bar, G::kBytes);
+        mbar_arrive_expect_tx(bar, stage_bytes);
         const long long row = (long long)rr * L.pitch + xb;
 #pragma unroll
         for (int p = 0; p < 8; p++)
-          bulk_g2s(smem_addr(st + p * G::kSegBytes), a.srcp[p] + row - G::kHalo, G::kSegBytes, bar);
-        bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + row, G::kRestBytes, bar);
+          bulk_g2s(smem_addr(st + p * G::kSegBytes), a.srcp[p] + row - G::kHalo, seg_bytes, bar);
+        bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + row, rest_bytes, bar);
         bulk_g2s(smem_addr(st + G::kMaskOff), a.mask + (long long)rr * L.mw + (xb >> 5) - 4, G::kMaskBytes, bar);
         if (++s == NS) { s = 0; empty_parity ^= 1u; }
       }
