@@ -243,7 +243,10 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem));
     if (occ < 1) return fail(LBM_ERR_CUDA, "staged step kernel does not fit on a multiprocessor");
     const int strips = (s->L.nx + W - 1) / W;
-    int bands = (occ * s->sms + strips - 1) / strips;
+    // as many bands as fit in ONE wave: rounding up would leave a second,
+    // nearly empty wave (e.g. 64 strips x 10 bands = 640 CTAs for 608
+    // slots), which cost 22 % at 16384 columns
+    int bands = (occ * s->sms) / strips;
     bands = std::max(1, std::min(bands, s->L.ny));
     // at least `rows` rows per band (the tuning value): short bands re-read
     // their two halo rows too often
