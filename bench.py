@@ -181,6 +181,54 @@ def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
             "nonfinite_domains": bad}
 
 
+def _finite_or_str(x, ndigits=4):
+    """A float for the JSON line; "non-finite" where the run diverged (strict
+    JSON has no Infinity or NaN)."""
+    import math
+    return round(x, ndigits) if math.isfinite(x) else "non-finite"
+
+
+def time_closure(lbm, refresh=20, seed=1):
+    """The learned-closure workload: one held-out layout of the closure
+    training setup (fine 2048x1024, tau 0.52, u 0.06, circles r 6-20 up to
+    8 % solid; coarse 4x: 512x256, tau 0.505), the fine f32 run for 8000 steps
+    against the coarse f32 run with the trained closure (tensor-core
+    inference every `refresh` steps) for the same physical time (2000
+    coarse steps).  Both are device-timed with CUDA events, every step and
+    inference included; the error is the relative L2 difference of the
+    time-averaged velocity (second half) against the block-averaged fine run,
+    for the closure and for plain coarse BGK."""
+    import numpy as np
+    from lbm_gb300 import closure as cl
+    path = os.path.join(HERE, "lbm_gb300", "models", "closure_2048x1024_f4.npz")
+    params = np.load(path)["params"]
+    nx, ny, F, tau, u, steps = 2048, 1024, 4, 0.52, 0.06, 8000
+    tau_c = cl.coarse_tau(tau, F)
+    # held-out layout 65 of the training script's seeded set (layouts 0-63 are
+    # trained on; 65's fine run stays finite), with that script's run seed
+    from lbm_gb300.geometry import random_circles
+    mask = random_circles(nx, ny, 10 ** 6, 6.0, 20.0, seed * 1000 + 65, inlet_clearance=64, target_fraction=0.08)
+    sc = cl.coarse_solid(mask, F)
+    lseed = seed * 7919 + 65
+    t_fine = cl.time_run(nx, ny, tau, u, mask, steps, lseed)
+    t_cl = cl.time_run(nx // F, ny // F, tau_c, u, sc, steps // F, lseed, params=params, refresh=refresh, drift=1.0)
+    uf, _, _ = cl.run_average(nx, ny, tau, u, mask, steps, 20, steps // 2, lseed)
+    ufc = cl.block_average(uf, mask, F)
+    uc, _, fb = cl.run_average(nx // F, ny // F, tau_c, u, sc, steps // F, 5, steps // F // 2, lseed, params=params,
+                               refresh=refresh, drift=1.0)
+    up, _, _ = cl.run_average(nx // F, ny // F, tau_c, u, sc, steps // F, 5, steps // F // 2, lseed)
+    fine_cells = nx * ny
+    return {"workload": "closure: fine 2048x1024 tau 0.52 u 0.06 vs coarse 512x256 + CNN closure (refresh %d)"
+                        % refresh,
+            "fine_ms": round(t_fine * 1e3, 3), "closure_ms": round(t_cl * 1e3, 3),
+            "speedup": round(t_fine / t_cl, 2),
+            "fine_mlups": round(fine_cells * steps / t_fine / 1e6, 1),
+            "fine_equivalent_mlups": round(fine_cells * steps / t_cl / 1e6, 1),
+            "err_closure_vs_fine": _finite_or_str(cl.rel_error(uc, ufc, sc)),
+            "err_plain_coarse_vs_fine": _finite_or_str(cl.rel_error(up, ufc, sc)),
+            "fallback_fraction": round(fb / max(int((sc == 0)[:, 1:].sum()) * (steps // F), 1), 6)}
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -291,6 +339,11 @@ def run_ours(args):
             variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
                               "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
 
+    # --- learned closure: coarse run with the trained network vs the fine run -------
+    closure_res = None
+    if not args.no_closure:
+        closure_res = time_closure(lbm)
+
     # --- batched: 512 independent domains, one persistent launch per step ----------
     batched = {}
     if not args.no_batched:
@@ -324,6 +377,7 @@ def run_ours(args):
         "mflups": round(world * active * args.steps / (dev_ms * 1e-3) / 1e6, 1),
         "variants": variants,
         "batched": batched,
+        "closure": closure_res,
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "wall_s_timed": round(wall, 4),
@@ -471,6 +525,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-closure", action="store_true")
     ap.add_argument("--batched-steps", type=int, default=5000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
