@@ -373,7 +373,7 @@ def run_ours(args):
                      "peak_source": peak_kind, "bytes_per_cell": BYTES_PER_CELL["f32"],
                      "algorithmic_bytes_per_launch": int(BYTES_PER_CELL["f32"] * active),
                      "active_cells": active,
-                     "kernel": "lbm::k_step_ws<StF32, EDGE_CHANNEL, 4>"},
+                     "kernel": "lbm::k_step_ws<StF32, EDGE_CHANNEL, NS=4, CPT=1, closure off>"},
         "mflups": round(world * active * args.steps / (dev_ms * 1e-3) / 1e6, 1),
         "variants": variants,
         "batched": batched,

@@ -231,13 +231,14 @@ void release(lbm_sim* s) {
 
 // Staged step launch: one strip of kStageW columns per grid column, row bands
 // sized so that all CTAs are resident at once (one wave, equal work).
-template <class St, int EDGE, int NS, int CPT>
+template <class St, int EDGE, int NS, int CPT, bool CL>
 int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int W = kStageW, TPB = stage_threads<CPT>();
   using G = StageGeom<typename St::S>;
   const size_t smem = (size_t)NS * G::kBytes;
-  auto kern = k_step_ws<St, EDGE, NS, CPT>;
-  if (s->staged_variant != s->kernel) {
+  auto kern = k_step_ws<St, EDGE, NS, CPT, CL>;
+  const int variant = 2 * s->kernel + (CL ? 1 : 0);
+  if (s->staged_variant != variant) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem));
@@ -252,7 +253,7 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     // their two halo rows too often
     s->staged_rows = std::max((s->L.ny + bands - 1) / bands, std::min(s->rows > 0 ? s->rows : 2, s->L.ny));
     s->staged_bands = (s->L.ny + s->staged_rows - 1) / s->staged_rows;
-    s->staged_variant = s->kernel;
+    s->staged_variant = variant;
   }
   a.rows = s->staged_rows;
   dim3 grid((s->L.nx + W - 1) / W, s->staged_bands);
@@ -262,17 +263,30 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
 }
 
 // Staged variants: ring depth and cells per consumer thread (two cells per
-// thread exist for channel mode only; reference mode runs one).
+// thread exist for channel mode only, four for channel mode with 16-bit
+// storage; elsewhere those variants run the widest that exists).  With the
+// closure on, one ring depth per cells-per-thread count runs (4 stages for one
+// or four cells, 6 for two).
 template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int C2 = EDGE == EDGE_CHANNEL ? 2 : 1;
+  constexpr int C4 = EDGE == EDGE_CHANNEL && sizeof(typename St::S) == 2 ? 4 : C2;
+  if constexpr (EDGE == EDGE_CHANNEL && sizeof(typename St::S) <= 4) {  // the closure's modes
+    if (a.closure) {
+      if (s->kernel >= 2 && s->kernel <= 5) return launch_staged<St, EDGE, 4, 1, true>(s, a);
+      if (s->kernel >= 9) return launch_staged<St, EDGE, 4, C4, true>(s, a);
+      return launch_staged<St, EDGE, 6, C2, true>(s, a);
+    }
+  }
   switch (s->kernel) {
-    case 2: return launch_staged<St, EDGE, 5, 1>(s, a);
-    case 3: return launch_staged<St, EDGE, 4, 1>(s, a);
-    case 4: return launch_staged<St, EDGE, 6, 1>(s, a);
-    case 5: return launch_staged<St, EDGE, 8, 1>(s, a);
-    case 6: return launch_staged<St, EDGE, 8, C2>(s, a);
-    case 7: return launch_staged<St, EDGE, 6, C2>(s, a);
-    default: return launch_staged<St, EDGE, 4, C2>(s, a);
+    case 2: return launch_staged<St, EDGE, 5, 1, false>(s, a);
+    case 3: return launch_staged<St, EDGE, 4, 1, false>(s, a);
+    case 4: return launch_staged<St, EDGE, 6, 1, false>(s, a);
+    case 5: return launch_staged<St, EDGE, 8, 1, false>(s, a);
+    case 6: return launch_staged<St, EDGE, 8, C2, false>(s, a);
+    case 7: return launch_staged<St, EDGE, 6, C2, false>(s, a);
+    case 9: return launch_staged<St, EDGE, 4, C4, false>(s, a);
+    case 10: return launch_staged<St, EDGE, 6, C4, false>(s, a);
+    default: return launch_staged<St, EDGE, 4, C2, false>(s, a);
   }
 }
 
@@ -316,9 +330,9 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   s->edge = edge_mode;
   s->storage = storage;
   // fastest measured variant per storage width: 4-stage ring, one cell per
-  // thread for 4-byte words; 4-stage ring, two cells per thread for 2-byte
+  // thread for 4-byte words; 6-stage ring, two cells per thread for 2-byte
   // words (reference mode runs one cell per thread); f64: the per-cell kernel
-  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 8);
+  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 7);
   s->omega = omega;
   s->es = store_bytes(storage);
   s->cs = storage == STORE_F64 ? 8 : 4;
@@ -415,7 +429,7 @@ int lbm_get_stream(const lbm_sim* s, void** stream) {
 int lbm_set_tuning(lbm_sim* s, int rows_per_thread, int kernel) {
   CHECK_SIM(s);
   if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
-  if (kernel < 0 || kernel > 8) return fail(LBM_ERR_ARG, "kernel %d", kernel);
+  if (kernel < 0 || kernel > 10) return fail(LBM_ERR_ARG, "kernel %d", kernel);
   s->rows = rows_per_thread;
   s->kernel = kernel;
   s->staged_variant = -1;  // recompute the staged launch shape
@@ -640,7 +654,7 @@ int lbm_step(lbm_sim* s, uint32_t n) {
     // runs of kStepGraph steps replay a captured graph: launch overhead
     // dominates small grids (the legacy default stream cannot be captured)
     const bool steady = !s->materialised && (s->storage == STORE_F64 || s->kernel < 2 ||
-                                             s->staged_variant == s->kernel);
+                                             s->staged_variant == 2 * s->kernel + (s->closure_on ? 1 : 0));
     if (s->use_graphs && steady && s->stream != nullptr && left > (uint32_t)kStepGraph) {
       if (!s->graph[s->cur] || !(s->graph_key[s->cur] == graph_key(s))) {
         int rc = capture_steps(s);

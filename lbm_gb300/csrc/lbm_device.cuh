@@ -32,38 +32,50 @@ template <class C> __device__ __forceinline__ void bgk(C f[9], C rho, C jx, C jy
 // Deviation-form BGK on g_i = f_i - w_i, for 16-bit storage (f32 arithmetic,
 // explicit FMA, one IEEE reciprocal).  rho = 1 + drho keeps the density
 // deviation at full precision; f_i^eq - w_i = w_i * (c0 + rho * (t + t^2/2))
-// with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho u^2, and the
-// relaxation is g_i' = (1 - omega) g_i + (omega w_i) (c0 + rho (t + t^2/2)).
+// with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho u^2.  Both
+// are written in the momentum j = rho u, so u itself is never formed:
+//   rho (t + t^2/2) = T + (T / (2 rho)) T,  T = 3 c_i.j,
+//   c0 = drho - 1.5 |j|^2 / rho.
+// The relaxation g_i' = (1 - omega) g_i + omega (f_i^eq - w_i) is evaluated as
+// g_i' = (omega w_i) X_i + ((1 - omega) g_i + b_i), X_i = T + (T / (2 rho)) T,
+// b_i = (omega w_i) c0 (two weight classes): three fused operations per
+// moving direction.  The moments sum the three columns (c_x = -1, 0, +1)
+// first, so jx and drho share them.
 __device__ __forceinline__ void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
-  const float s1 = (g[0] + g[1]) + (g[2] + g[3]);
-  const float s2 = (g[5] + g[6]) + (g[7] + g[8]);
-  drho = (s1 + g[4]) + s2;
-  jx = ((g[2] + g[5]) + g[8]) - ((g[0] + g[3]) + g[6]);
+  const float cw = (g[0] + g[3]) + g[6];  // c_x = -1
+  const float ce = (g[2] + g[5]) + g[8];  // c_x = +1
+  const float cm = (g[1] + g[7]) + g[4];  // c_x = 0
+  drho = (cw + ce) + cm;
+  jx = ce - cw;
   jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
   rho = 1.0f + drho;
 }
-__device__ __forceinline__ void relax_dev(float& g, float aw, float pt, float rho, float c0, float omw) {
-  g = __fmaf_rn(aw, __fmaf_rn(rho, pt, c0), omw * g);
+// Per-lattice constants of the relaxation (omega only): hoisted out of the
+// cell loops when omega is uniform.
+struct DevOmega {
+  float omw, aw1, aw2, aw0;
+  __device__ __forceinline__ explicit DevOmega(float omega)
+      : omw(1.0f - omega), aw1(omega * (1.0f / 9.0f)), aw2(omega * (1.0f / 36.0f)), aw0(omega * (4.0f / 9.0f)) {}
+};
+__device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, const DevOmega& o) {
+  const float h = 0.5f * __frcp_rn(rho);                  // 1 / (2 rho)
+  const float c0 = __fmaf_rn(__fmaf_rn(jx, jx, jy * jy), -3.0f * h, drho);
+  const float tx = 3.0f * jx, ty = 3.0f * jy;              // T of the axis directions
+  const float tp = tx + ty, tm = tx - ty;                  // and of the diagonals
+  const float hx = h * tx, hy = h * ty, hp = h * tp, hm = h * tm;
+  const float b1 = o.aw1 * c0, b2 = o.aw2 * c0;
+  g[5] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, tx), __fmaf_rn(o.omw, g[5], b1));   // e  (+x)
+  g[3] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, -tx), __fmaf_rn(o.omw, g[3], b1));  // w  (-x)
+  g[1] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, ty), __fmaf_rn(o.omw, g[1], b1));   // n  (+y)
+  g[7] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, -ty), __fmaf_rn(o.omw, g[7], b1));  // s  (-y)
+  g[2] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, tp), __fmaf_rn(o.omw, g[2], b2));   // ne (+x+y)
+  g[6] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, -tp), __fmaf_rn(o.omw, g[6], b2));  // sw (-x-y)
+  g[8] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, tm), __fmaf_rn(o.omw, g[8], b2));   // se (+x-y)
+  g[0] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, -tm), __fmaf_rn(o.omw, g[0], b2));  // nw (-x+y)
+  g[4] = __fmaf_rn(o.omw, g[4], o.aw0 * c0);                                    // rest (T = 0)
 }
 __device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
-  const float inv = __frcp_rn(rho);
-  const float ux = jx * inv, uy = jy * inv;
-  const float u215 = 1.5f * __fmaf_rn(ux, ux, uy * uy);
-  const float c0 = __fmaf_rn(-rho, u215, drho);
-  const float tx = 3.0f * ux, ty = 3.0f * uy;
-  const float tp = tx + ty, tm = tx - ty;
-  const float hx = 0.5f * tx, hy = 0.5f * ty, hp = 0.5f * tp, hm = 0.5f * tm;
-  const float omw = 1.0f - omega;
-  const float aw1 = omega * (1.0f / 9.0f), aw2 = omega * (1.0f / 36.0f), aw0 = omega * (4.0f / 9.0f);
-  relax_dev(g[5], aw1, __fmaf_rn(hx, tx, tx), rho, c0, omw);   // e  (+x)
-  relax_dev(g[3], aw1, __fmaf_rn(hx, tx, -tx), rho, c0, omw);  // w  (-x)
-  relax_dev(g[1], aw1, __fmaf_rn(hy, ty, ty), rho, c0, omw);   // n  (+y)
-  relax_dev(g[7], aw1, __fmaf_rn(hy, ty, -ty), rho, c0, omw);  // s  (-y)
-  relax_dev(g[2], aw2, __fmaf_rn(hp, tp, tp), rho, c0, omw);   // ne (+x+y)
-  relax_dev(g[6], aw2, __fmaf_rn(hp, tp, -tp), rho, c0, omw);  // sw (-x-y)
-  relax_dev(g[8], aw2, __fmaf_rn(hm, tm, tm), rho, c0, omw);   // se (+x-y)
-  relax_dev(g[0], aw2, __fmaf_rn(hm, tm, -tm), rho, c0, omw);  // nw (-x+y)
-  g[4] = __fmaf_rn(aw0, c0, omw * g[4]);                        // rest (t = 0)
+  collide_dev(g, rho, drho, jx, jy, DevOmega(omega));
 }
 
 // Storage policies.  S is the stored word, C the arithmetic type, and a
@@ -73,8 +85,11 @@ __device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, f
 //   f_of / of_f       stored word <-> population value f_i (readout, init)
 //   moments / collide the collision in the working representation; `aux`
 //                     carries drho between them in the deviation form
+//   Om / omega_consts what the collision derives from omega alone, computed
+//                     once per lattice where omega is uniform
 struct StF32 {
-  using S = float; using C = float;
+  using S = float; using C = float; using Om = float;
+  __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
   __device__ static C f_of(S s, int) { return s; }
@@ -83,7 +98,8 @@ struct StF32 {
   __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF64 {
-  using S = double; using C = double;
+  using S = double; using C = double; using Om = double;
+  __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
   __device__ static C f_of(S s, int) { return s; }
@@ -92,22 +108,26 @@ struct StF64 {
   __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF16 {  // binary16 deviation from the rest-state weight
-  using S = __half; using C = float;
+  using S = __half; using C = float; using Om = DevOmega;
+  __device__ static Om omega_consts(C w) { return DevOmega(w); }
   __device__ static C load(S s, int) { return __half2float(s); }
   __device__ static S store(C v, int) { return __float2half_rn(v); }
   __device__ static C f_of(S s, int q) { return weight<float>(q) + __half2float(s); }
   __device__ static S of_f(C f, int q) { return __float2half_rn(f - weight<float>(q)); }
   __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
   __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
+  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, const Om& o) { collide_dev(v, rho, aux, jx, jy, o); }
 };
 struct StBF16 {  // bfloat16 deviation from the rest-state weight
-  using S = __nv_bfloat16; using C = float;
+  using S = __nv_bfloat16; using C = float; using Om = DevOmega;
+  __device__ static Om omega_consts(C w) { return DevOmega(w); }
   __device__ static C load(S s, int) { return __bfloat162float(s); }
   __device__ static S store(C v, int) { return __float2bfloat16_rn(v); }
   __device__ static C f_of(S s, int q) { return weight<float>(q) + __bfloat162float(s); }
   __device__ static S of_f(C f, int q) { return __float2bfloat16_rn(f - weight<float>(q)); }
   __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
   __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
+  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, const Om& o) { collide_dev(v, rho, aux, jx, jy, o); }
 };
 
 // Device layout of one lattice.

@@ -53,11 +53,24 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// The same test, letting the thread sleep until the phase completes or up to
+// `ns` nanoseconds pass: a waiting warp then issues no instructions, where a
+// plain try_wait returns after a short system-dependent time and the retry
+// loop takes issue slots from the warps doing the work.
+__device__ __forceinline__ bool mbar_try_wait_sleep(uint32_t bar, uint32_t parity, uint32_t ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity), "r"(ns)
+      : "memory");
+  return ok != 0;
+}
 // Bounded wait for the completion of phase `parity`: false after ~2^31 cycles.
 __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
   if (mbar_try_wait(bar, parity)) return true;
   const long long t0 = clock64();
-  while (!mbar_try_wait(bar, parity))
+  while (!mbar_try_wait_sleep(bar, parity, 100000u))
     if (clock64() - t0 > (1ll << 31)) return false;
   return true;
 }
@@ -105,6 +118,32 @@ __device__ __forceinline__ void store_pair(__nv_bfloat16* p, float a, float b) {
   *reinterpret_cast<__nv_bfloat162*>(p) = __floats2bfloat162_rn(a, b);
 }
 
+// Four working values of 16-bit storage as one 8-byte word (p 8-byte aligned).
+template <class H2> __device__ __forceinline__ uint32_t u32_of(H2 h) {
+  uint32_t u;
+  memcpy(&u, &h, 4);
+  return u;
+}
+__device__ __forceinline__ void store_quad(__half* p, float a, float b, float c, float d) {
+  *reinterpret_cast<uint2*>(p) = make_uint2(u32_of(__floats2half2_rn(a, b)), u32_of(__floats2half2_rn(c, d)));
+}
+__device__ __forceinline__ void store_quad(__nv_bfloat16* p, float a, float b, float c, float d) {
+  *reinterpret_cast<uint2*>(p) =
+      make_uint2(u32_of(__floats2bfloat162_rn(a, b)), u32_of(__floats2bfloat162_rn(c, d)));
+}
+// Two adjacent 16-bit words (low half = lower address) as working values.
+__device__ __forceinline__ void load_pair(const __half*, uint32_t w, float& lo, float& hi) {
+  __half2 h;
+  memcpy(&h, &w, 4);
+  const float2 v = __half22float2(h);
+  lo = v.x;
+  hi = v.y;
+}
+__device__ __forceinline__ void load_pair(const __nv_bfloat16*, uint32_t w, float& lo, float& hi) {
+  lo = __uint_as_float(w << 16);  // bf16 -> f32 is exact: the high 16 bits
+  hi = __uint_as_float(w & 0xFFFF0000u);
+}
+
 // Threads per CTA: kStageW / CPT consumers (CPT cells each) + one producer warp.
 template <int CPT> constexpr int stage_threads() { return kStageW / CPT + 32; }
 
@@ -112,12 +151,16 @@ template <int CPT> constexpr int stage_threads() { return kStageW / CPT + 32; }
 // the lattice described by `a` (kernel parameters, or a copy in shared memory
 // for the batched kernel).  Every thread of the CTA calls it.  It arms the
 // ring's barriers itself, so consecutive tiles of a persistent CTA reuse the
-// ring once the CTA has synchronised between them.
-template <class St, int EDGE, int NS, int CPT, class A>
+// ring once the CTA has synchronised between them.  CL selects the per-cell
+// relaxation time of the learned closure (a.closure must then be set);
+// without it omega is uniform and its derived constants are computed once.
+template <class St, int EDGE, int NS, int CPT, bool CL, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
                                         uint64_t* empty) {
-  static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL), "two cells per thread: channel mode only");
   using S = typename St::S;
+  static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL) ||
+                    (CPT == 4 && EDGE == EDGE_CHANNEL && sizeof(S) == 2),
+                "two cells per thread: channel mode only; four: channel mode, 16-bit storage");
   using C = typename St::C;
   using G = StageGeom<S>;
   constexpr int kConsumers = kStageW / CPT;
@@ -204,18 +247,28 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     dxr[j] = (EDGE == EDGE_CHANNEL && x == L.nx - 1) ? 0 : 1;
     xin[j] = EDGE == EDGE_CHANNEL ? (x >= 1 && x <= L.nx - 1) : (x >= 1 && x <= L.nx - 2);
   }
-  bool bad = false;
+  // four cells per thread: does this thread hold the outflow column?
+  const bool has_out = CPT == 4 && x0 <= L.nx - 1 && L.nx - 1 < x0 + CPT;
+  // running sum of the densities of the cells this thread collides: it is
+  // finite exactly when they all were (inf - inf and NaN stay NaN), so one
+  // add per cell replaces a per-cell test
+  C rho_sum = C(0);
   uint32_t own = (uint32_t)y0 * (uint32_t)L.pitch + (uint32_t)x0;
   // closure records (global memory) are loaded one row ahead, so their
   // latency overlaps the stage wait and the previous row's arithmetic
   __half2 rec[CPT], rec_next[CPT];
+  if constexpr (CL) {
 #pragma unroll
-  for (int j = 0; j < CPT; j++) rec_next[j] = a.closure && !producer ? a.closure[own + j] : __half2();
+    for (int j = 0; j < CPT; j++) rec_next[j] = a.closure[own + j];
+  }
+  const typename St::Om om = St::omega_consts(a.omega);
   for (int y = y0; y < y1 && ok; y++, own += (uint32_t)L.pitch) {
+    if constexpr (CL) {
 #pragma unroll
-    for (int j = 0; j < CPT; j++) {
-      rec[j] = rec_next[j];
-      if (a.closure && y + 1 < y1) rec_next[j] = a.closure[own + L.pitch + j];
+      for (int j = 0; j < CPT; j++) {
+        rec[j] = rec_next[j];
+        if (y + 1 < y1) rec_next[j] = a.closure[own + L.pitch + j];
+      }
     }
     if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
     const unsigned char* sm = smem + (size_t)slot_m * G::kBytes;
@@ -242,7 +295,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[tid], 4);
       C rho, jx, jy, aux;
       St::moments(f, rho, aux, jx, jy);
-      bad |= !(rho - rho == C(0));
+      rho_sum += rho;
       if (a.rho_out) {
         a.rho_out[own] = rho;
         a.jx_out[own] = jx;
@@ -255,16 +308,61 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       a.rest[own] = St::store(f[4], 4);
     } else if (any_act) {
       C f[9][CPT];
+      if constexpr (CPT == 4) {
+        // 16-bit words, four consecutive cells: e is a multiple of 4, so each
+        // plane is read as aligned 8- and 4-byte words and the x-1 / x+1
+        // windows are assembled with byte permutes
 #pragma unroll
-      for (int q = 0; q < 9; q++) {  // plain pulls
-        if (q == 4) continue;
-        const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
-        const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
-#pragma unroll
-        for (int j = 0; j < CPT; j++) {
-          const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);  // pull column offset
-          f[q][j] = St::load(seg[e + j + dx], q);
+        for (int q = 0; q < 9; q++) {
+          if (q == 4) continue;
+          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+          const uint2 mid = *reinterpret_cast<const uint2*>(seg + e);  // columns x0 .. x0+3
+          uint32_t p0 = mid.x, p1 = mid.y;
+          // (the neighbour words are read as aligned 8-byte words too: a
+          // 4-byte read at an 8-byte lane stride would be 2-way bank-conflicted)
+          if (cx(q) > 0) {  // pull from x-1: columns x0-1 .. x0+2
+            const uint32_t left = reinterpret_cast<const uint2*>(seg + e - 4)->y;
+            p0 = __byte_perm(left, mid.x, 0x5432);
+            p1 = __byte_perm(mid.x, mid.y, 0x5432);
+          } else if (cx(q) < 0) {  // pull from x+1: columns x0+1 .. x0+4
+            const uint32_t right = reinterpret_cast<const uint2*>(seg + e + 4)->x;
+            p0 = __byte_perm(mid.x, mid.y, 0x5432);
+            p1 = __byte_perm(mid.y, right, 0x5432);
+          }
+          load_pair(seg, p0, f[q][0], f[q][1]);
+          load_pair(seg, p1, f[q][2], f[q][3]);
         }
+        if (has_out) {  // the outflow column pulls its x+1 populations from its own column
+#pragma unroll
+          for (int q = 0; q < 9; q++) {
+            if (cx(q) >= 0) continue;
+            const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+            const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+#pragma unroll
+            for (int j = 0; j < CPT; j++)
+              if (dxr[j] == 0) f[q][j] = St::load(seg[e + j], q);
+          }
+        }
+        const S* rest = reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes);
+        const uint2 rv = *reinterpret_cast<const uint2*>(rest + CPT * tid);
+        load_pair(rest, rv.x, f[4][0], f[4][1]);
+        load_pair(rest, rv.y, f[4][2], f[4][3]);
+      } else {
+#pragma unroll
+        for (int q = 0; q < 9; q++) {  // plain pulls
+          if (q == 4) continue;
+          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+#pragma unroll
+          for (int j = 0; j < CPT; j++) {
+            const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);  // pull column offset
+            f[q][j] = St::load(seg[e + j + dx], q);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < CPT; j++)
+          f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
       }
       if (near_solid) {  // half-way bounce-back: upstream solid -> own opposite population
 #pragma unroll
@@ -279,31 +377,57 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           }
         }
       }
+      C m_rho[CPT], m_jx[CPT], m_jy[CPT];
 #pragma unroll
       for (int j = 0; j < CPT; j++) {
-        f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
         C g[9];
 #pragma unroll
         for (int q = 0; q < 9; q++) g[q] = f[q][j];
         C rho, jx, jy, aux;
         St::moments(g, rho, aux, jx, jy);
-        if (act[j]) {
-          bad |= !(rho - rho == C(0));
-          if (a.rho_out) {
-            a.rho_out[own + j] = rho;
-            a.jx_out[own + j] = jx;
-            a.jy_out[own + j] = jy;
-          }
-        }
-        St::collide(g, rho, aux, jx, jy, cell_omega_rec(a, rec[j], rho, jx, jy, act[j]));
+        if (act[j]) rho_sum += rho;
+        m_rho[j] = rho;
+        m_jx[j] = jx;
+        m_jy[j] = jy;
+        if constexpr (CL) St::collide(g, rho, aux, jx, jy, cell_omega_rec(a, rec[j], rho, jx, jy, act[j]));
+        else St::collide(g, rho, aux, jx, jy, om);
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
       }
-      if (CPT == 2 && act[0] && act[CPT - 1]) {  // both cells: one 2-element store per plane
+      if (a.rho_out) {  // one uniform test per row, not one per cell
+#pragma unroll
+        for (int j = 0; j < CPT; j++) {
+          if (!act[j]) continue;
+          a.rho_out[own + j] = m_rho[j];
+          a.jx_out[own + j] = m_jx[j];
+          a.jy_out[own + j] = m_jy[j];
+        }
+      }
+      bool all_act = true;
+#pragma unroll
+      for (int j = 0; j < CPT; j++) all_act &= act[j];
+      if (CPT == 2 && all_act) {  // both cells: one 2-element store per plane
 #pragma unroll
         for (int q = 0; q < 9; q++) {
           S* p = q == 4 ? a.rest + own : a.dstp[slot(q)] + own;
           store_pair(p, f[q][0], f[q][CPT - 1]);
+        }
+      } else if constexpr (CPT == 4) {
+        if (all_act) {  // four cells: one 8-byte store per plane
+#pragma unroll
+          for (int q = 0; q < 9; q++) {
+            S* p = q == 4 ? a.rest + own : a.dstp[slot(q)] + own;
+            store_quad(p, f[q][0], f[q][1], f[q][2], f[q][3]);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < CPT; j++) {
+            if (!act[j]) continue;
+#pragma unroll
+            for (int q = 0; q < 9; q++)
+              if (q != 4) a.dstp[slot(q)][own + j] = St::store(f[q][j], q);
+            a.rest[own + j] = St::store(f[4][j], 4);
+          }
         }
       } else {
 #pragma unroll
@@ -316,9 +440,10 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         }
       }
     }
-    // cells outside the fast path
+    // cells outside the fast path; inert channel cells only report moments
 #pragma unroll
     for (int j = 0; j < CPT; j++) {
+      if (EDGE == EDGE_CHANNEL && !a.rho_out) break;
       if (act[j] || !in_row[j]) continue;
       if (EDGE == EDGE_CHANNEL) {  // inlet column or a solid cell: inert
         if (a.rho_out) {           // moments of its stored state
@@ -346,13 +471,13 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     slot_0 = slot_p;
     if (++slot_p == NS) { slot_p = 0; parity_p ^= 1u; }
   }
-  if (bad) atomicOr(a.flag, 1);
+  if (!(rho_sum - rho_sum == C(0))) atomicOr(a.flag, 1);
   if (!ok) atomicOr(a.flag, 2);
 }
 
 // The staged step over one lattice: CTA (bx, by) takes strip bx and row band by.
-template <class St, int EDGE, int NS, int CPT>
-__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
+template <class St, int EDGE, int NS, int CPT, bool CL>
+__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : (CPT == 2 ? (sizeof(typename St::S) == 8 ? 5 : 6) : 8))
     k_step_ws(StepArgs<typename St::S, typename St::C> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NS];
@@ -369,7 +494,7 @@ __global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 5)
           if (x0 + j < a.L.nx) step_cell<St, EDGE>(a, x0 + j, y);
     return;
   }
-  ws_tile<St, EDGE, NS, CPT>(a, xb, y0, y1, smem, full, empty);
+  ws_tile<St, EDGE, NS, CPT, CL>(a, xb, y0, y1, smem, full, empty);
 }
 
 }  // namespace lbm

@@ -144,38 +144,40 @@ struct StBF16 { using S = uint16_t; using C = float; static constexpr bool kDev 
 // Deviation-form BGK of the 16-bit storage modes, on g_q = f_q - w_q, with
 // rho = 1 + drho, one correctly rounded reciprocal and fused multiply-adds:
 // f_q^eq - w_q = w_q (c0 + rho (t + t^2/2)), t = 3 c_q.u, c0 = drho - 1.5 rho u^2,
-// relaxed as g_q' = (1 - omega) g_q + (omega w_q)(c0 + rho (t + t^2/2)).
-// Operation order is part of the definition (the GPU kernel uses the same).
+// written in j = rho u: rho (t + t^2/2) = T + (T / (2 rho)) T with T = 3 c_q.j,
+// c0 = drho - 1.5 |j|^2 / rho; relaxed as
+// g_q' = (omega w_q) X_q + ((1 - omega) g_q + (omega w_q) c0).  The moments sum
+// the columns c_x = -1, 0, +1 first.  Operation order is part of the
+// definition (the GPU kernels use the same).
 inline void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
-  const float s1 = (g[0] + g[1]) + (g[2] + g[3]);
-  const float s2 = (g[5] + g[6]) + (g[7] + g[8]);
-  drho = (s1 + g[4]) + s2;
-  jx = ((g[2] + g[5]) + g[8]) - ((g[0] + g[3]) + g[6]);
+  const float cw = (g[0] + g[3]) + g[6];
+  const float ce = (g[2] + g[5]) + g[8];
+  const float cm = (g[1] + g[7]) + g[4];
+  drho = (cw + ce) + cm;
+  jx = ce - cw;
   jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
   rho = 1.0f + drho;
 }
-inline void relax_dev(float& g, float aw, float pt, float rho, float c0, float omw) {
-  g = std::fma(aw, std::fma(rho, pt, c0), omw * g);
+inline float relax_dev(float g, float aw, float h, float t, float sign, float omw, float b) {
+  return std::fma(aw, std::fma(h * t, t, sign * t), std::fma(omw, g, b));
 }
 inline void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
-  const float inv = 1.0f / rho;
-  const float ux = jx * inv, uy = jy * inv;
-  const float u215 = 1.5f * std::fma(ux, ux, uy * uy);
-  const float c0 = std::fma(-rho, u215, drho);
-  const float tx = 3.0f * ux, ty = 3.0f * uy;
+  const float h = 0.5f * (1.0f / rho);
+  const float c0 = std::fma(std::fma(jx, jx, jy * jy), -3.0f * h, drho);
+  const float tx = 3.0f * jx, ty = 3.0f * jy;
   const float tp = tx + ty, tm = tx - ty;
-  const float hx = 0.5f * tx, hy = 0.5f * ty, hp = 0.5f * tp, hm = 0.5f * tm;
   const float omw = 1.0f - omega;
   const float aw1 = omega * (1.0f / 9.0f), aw2 = omega * (1.0f / 36.0f), aw0 = omega * (4.0f / 9.0f);
-  relax_dev(g[5], aw1, std::fma(hx, tx, tx), rho, c0, omw);
-  relax_dev(g[3], aw1, std::fma(hx, tx, -tx), rho, c0, omw);
-  relax_dev(g[1], aw1, std::fma(hy, ty, ty), rho, c0, omw);
-  relax_dev(g[7], aw1, std::fma(hy, ty, -ty), rho, c0, omw);
-  relax_dev(g[2], aw2, std::fma(hp, tp, tp), rho, c0, omw);
-  relax_dev(g[6], aw2, std::fma(hp, tp, -tp), rho, c0, omw);
-  relax_dev(g[8], aw2, std::fma(hm, tm, tm), rho, c0, omw);
-  relax_dev(g[0], aw2, std::fma(hm, tm, -tm), rho, c0, omw);
-  g[4] = std::fma(aw0, c0, omw * g[4]);
+  const float b1 = aw1 * c0, b2 = aw2 * c0;
+  g[5] = relax_dev(g[5], aw1, h, tx, 1.0f, omw, b1);
+  g[3] = relax_dev(g[3], aw1, h, tx, -1.0f, omw, b1);
+  g[1] = relax_dev(g[1], aw1, h, ty, 1.0f, omw, b1);
+  g[7] = relax_dev(g[7], aw1, h, ty, -1.0f, omw, b1);
+  g[2] = relax_dev(g[2], aw2, h, tp, 1.0f, omw, b2);
+  g[6] = relax_dev(g[6], aw2, h, tp, -1.0f, omw, b2);
+  g[8] = relax_dev(g[8], aw2, h, tm, 1.0f, omw, b2);
+  g[0] = relax_dev(g[0], aw2, h, tm, -1.0f, omw, b2);
+  g[4] = std::fma(omw, g[4], aw0 * c0);
 }
 
 // splitmix64 finaliser; the seeded per-cell noise of the initial state.

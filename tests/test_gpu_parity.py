@@ -122,9 +122,9 @@ STORAGES = [(0, 0, False), (3, 3, True), (1, 1, False), (2, 2, False)]  # (lbm s
 
 @pytest.mark.parametrize("storage,prec,f64", STORAGES)
 @pytest.mark.parametrize("edge", [0, 1])
-@pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5), (600, 37, 7),
-                                        (1100, 700, 9)])
-@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5, 6, 8])
+@pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5), (131, 20, 3),
+                                        (600, 37, 7), (1100, 700, 9)])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5, 6, 8, 9, 10])
 def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, edge, nx, ny, rows, kernel):
     P = oracle_mod
     rng = np.random.default_rng(nx * 1000 + ny + 7 * storage + edge)
@@ -246,7 +246,7 @@ def test_gpu_full_size_channel_matches_oracle(lbm, cuda_ok, oracle_mod):
     lat.close()
 
 
-@pytest.mark.parametrize("kernel", [0, 1, 3, 8])
+@pytest.mark.parametrize("kernel", [0, 1, 3, 8, 9])
 def test_gpu_graph_replay_is_transparent(lbm, cuda_ok, oracle_mod, kernel):
     """Runs of steps replayed from captured graphs (the default) give the same
     state as plain launches, across an omega change between calls (which must
@@ -258,8 +258,8 @@ def test_gpu_graph_replay_is_transparent(lbm, cuda_ok, oracle_mod, kernel):
     L = lbm.load_library()
     states = []
     for graphs in (1, 0):
-        lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, lbm.F32 if kernel != 8 else lbm.F16,
-                          P.P_F32 if kernel != 8 else P.P_F16, 0, mask, kernel=kernel)
+        lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, lbm.F32 if kernel < 8 else lbm.F16,
+                          P.P_F32 if kernel < 8 else P.P_F16, 0, mask, kernel=kernel)
         lbm._check(L.lbm_set_graphs(lat.handle, graphs))
         lat.iterate(53)
         o.step(53)
