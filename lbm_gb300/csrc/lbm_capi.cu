@@ -917,7 +917,8 @@ int lbm_closure_infer(lbm_sim* s) {
     CK(cudaFuncSetAttribute(k_closure_infer_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmem));
     if (!s->sms) CK(cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device));
     const int tiles = (int)(grid.x * grid.y);
-    k_closure_infer_tc<<<std::min(tiles, s->sms), 256, tc::kSmem, s->stream>>>(
+    // persistent: two CTAs per multiprocessor (one's epilogues overlap the other's MMAs)
+    k_closure_infer_tc<<<std::min(tiles, 2 * s->sms), 256, tc::kSmem, s->stream>>>(
         s->L, (const float*)mom_plane(s, 0), (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), s->mask_d,
         s->cnn_wpack, LBM_CNN_S_RHO, LBM_CNN_S_U, LBM_CNN_DT_MAX, s->closure_d, s->flag_d);
   } else {

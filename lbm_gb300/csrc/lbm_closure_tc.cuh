@@ -1,33 +1,41 @@
 // Learned closure inference on the 5th-generation tensor cores: the whole
-// network per 16 x 16 tile in shared memory, the three 32-channel layers as
-// implicit GEMMs issued with tcgen05.mma (BF16 operands from shared memory,
-// f32 accumulators in tensor memory), and the 1-channel output layer as a
-// fourth GEMM with its weights padded to 16 outputs.
+// network per 16 x 16 tile in shared memory, the four layers as implicit
+// GEMMs issued with tcgen05.mma (BF16 operands from shared memory, f32
+// accumulators in tensor memory); the 1-channel output layer has its weights
+// padded to 16 outputs.
 //
 // GEMM shapes per tile (M = window pixels, N = 32 output channels):
-//   layer 1  M = 22 x 22 (4 blocks of 128), K = 9 taps x 4 channels, padded
-//            to 48; its A operand is an explicit im2col of the features;
+//   layer 1  M = 22 rows x 24 (the feature window's pitch), 5 blocks of 128,
+//            K = 3 kernel rows x 16;
 //   layer 2  M = 20 rows x 22 (the input window's pitch), K = 9 x 32;
 //   layer 3  M = 18 rows x 20, K = 9 x 32;
 //   layer 4  M = 16 rows x 18, K = 9 x 32, N = 16 (one real output).
 // For layers 2 to 4 the A operand of tap (ky, kx) is the input activation
 // buffer itself viewed from row offset ky * pitch + kx: output pixel q =
 // oy * pitch + ox reads input pixel q + ky * pitch + kx, so each tap is one
-// shared-memory descriptor with a shifted start address (the two columns per
-// row with ox >= the output width are computed and dropped).
+// shared-memory descriptor with a shifted start address (the columns per
+// row with ox >= the output width are computed and dropped).  Layer 1 reads
+// a paired feature buffer: row r holds the 4 features of pixels r and r + 1
+// (16 bytes), so one K = 16 MMA per kernel row ky covers taps kx = 0, 1 (its
+// first 8-wide K chunk, rows from ky * 24) and kx = 2 (its second chunk, two
+// rows further: a leading byte offset of 32 bytes; the kx = 3 weights are 0).
 //
 // Operand layout (no swizzle, K-major): a buffer is [K / 8][rows][8 x bf16],
 // so an 8-row x 16-byte core matrix is 128 contiguous bytes; the leading
 // byte offset (next 8 K-values) is rows * 16 B and the stride byte offset
-// (next 8 rows) is 128 B.  Weights are [K / 8][32][8] likewise.
+// (next 8 rows) is 128 B.  Weights are [K / 8][N][8] likewise.
+//
+// Shared memory is 111 KB per CTA, so two CTAs share a multiprocessor and
+// one's epilogues run while the other's MMAs do.  Buffers are reused once
+// dead: the paired features and the layer-2 output share one region, the
+// layer-1 and layer-3 outputs another.  Every row a descriptor can reach
+// lies inside its region.
 //
 // One thread issues the MMAs and commits them to an mbarrier; every wait is
 // bounded (a timeout sets bit 2 of the error flag and the CTA stops waiting
-// for the rest of its tiles).  The CTA allocates 128
-// tensor-memory columns (4 accumulator blocks of 128 lanes x 32 f32) and
-// frees them on every path.  Dynamic shared memory is the whole 227 KB
-// opt-in window, so every operand address a descriptor can form lies inside
-// the CTA's own allocation.
+// for the rest of its tiles).  Each CTA allocates 256 tensor-memory columns
+// (up to 5 accumulator blocks of 128 lanes x 32 f32) and frees them on every
+// path.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -39,51 +47,49 @@ namespace tc {
 constexpr int kT = 16;                 // output tile
 constexpr int kW0 = kT + 8;            // feature window (24)
 constexpr int kW1 = kT + 6, kW2 = kT + 4, kW3 = kT + 2;  // layer output windows (22, 20, 18)
-constexpr int kM1 = kW1 * kW1;         // 484 rows of layer 1
+constexpr int kM1 = kW1 * kW0;         // 528 rows of layer 1 (pitch 24)
 constexpr int kM2 = kW2 * kW1;         // 440 rows of layer 2 (pitch 22)
 constexpr int kM3 = kW3 * kW2;         // 360 rows of layer 3 (pitch 20)
-constexpr int kB1 = 4, kB2 = 4, kB3 = 3;   // 128-row blocks
-constexpr int kK1 = 48;                // layer-1 K (36 used)
-// rows of each activation buffer: every row a descriptor of its layer can reach
-constexpr int kR1 = kB1 * 128;                          // im2col rows
+constexpr int kM4 = kT * kW3;          // 288 rows of layer 4 (pitch 18)
+constexpr int kB1 = 5, kB2 = 4, kB3 = 3, kB4 = 3;   // 128-row blocks
+// rows of each input buffer: every row a descriptor of its layer can reach
+constexpr int kRF = kB1 * 128 + 2 * kW0 + 2 + 6;        // paired features (= 696)
 constexpr int kRX1 = kB2 * 128 + 2 * kW1 + 2 + 6;       // layer-1 output, pitch 22 (= 564)
 constexpr int kRX2 = kB3 * 128 + 2 * kW2 + 2 + 6;       // layer-2 output, pitch 20 (= 432)
-constexpr int kM4 = kT * kW3;           // 288 rows of layer 4 (pitch 18)
-constexpr int kB4 = 3;
 constexpr int kRX3 = kB4 * 128 + 2 * kW3 + 2 + 2;       // layer-3 output, pitch 18 (= 424)
+static_assert(kB1 * 128 >= kM1 && kB2 * 128 >= kM2 && kB3 * 128 >= kM3 && kB4 * 128 >= kM4, "blocks");
 
 // byte offsets in dynamic shared memory
-constexpr uint32_t kOffA1 = 0;                                  // [6][512][8] bf16
-constexpr uint32_t kOffX1 = kOffA1 + 6u * kR1 * 16u;            // [4][564][8]
-constexpr uint32_t kOffX2 = kOffX1 + 4u * kRX1 * 16u;           // [4][432][8]
+constexpr uint32_t kOffP = 0;                                   // X1 [4][564][8], later X3 [4][424][8]
+constexpr uint32_t kOffQ = kOffP + 4u * kRX1 * 16u;             // paired features [696][8], later X2 [4][432][8]
+constexpr uint32_t kOffX1 = kOffP, kOffX3 = kOffP, kOffF = kOffQ, kOffX2 = kOffQ;
 // the packed parameters, in the order they are uploaded (pack_weights)
-constexpr uint32_t kOffW1 = kOffX2 + 4u * kRX2 * 16u;           // [6][32][8] bf16
+constexpr uint32_t kOffW1 = kOffQ + 4u * kRX2 * 16u;            // [6][32][8] bf16
 constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8] bf16
 constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;           // [36][32][8] bf16
 constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // [36][16][8] bf16: layer 4 padded to 16 outputs
 constexpr uint32_t kOffBias = kOffW4 + 36u * 16u * 16u;         // f32 b1 b2 b3 (32 each), b4
 constexpr uint32_t kPackedBytes = kOffBias + 400u - kOffW1;     // 97 floats, padded to 16 B
-constexpr uint32_t kOffFeat = kOffW1 + kPackedBytes;            // f32 [576][4]
-constexpr uint32_t kOffBar = kOffFeat + kW0 * kW0 * 16u;        // mbarrier (8 B), tensor-memory address (4 B)
-constexpr uint32_t kUsed = kOffBar + 16u;
-constexpr uint32_t kSmem = 232448u;  // 227 KB: the whole opt-in window (see above); no static shared memory
-static_assert(kUsed <= kSmem, "closure tile does not fit in shared memory");
+constexpr uint32_t kOffBar = kOffW1 + kPackedBytes;             // mbarrier (8 B), tensor-memory address (4 B)
+constexpr uint32_t kSmem = kOffBar + 16u;
+static_assert(4u * kRX3 <= 4u * kRX1 && kRF <= 4 * kRX2, "buffer regions");
+static_assert(2u * (kSmem + 1024u) <= 233472u, "two CTAs per multiprocessor");
 static_assert(kPackedBytes % 16 == 0 && 97u * 4u <= 400u, "packed parameter block");
-// layer-3 output reuses the im2col region
-constexpr uint32_t kOffX3 = kOffA1;
-static_assert(4u * kRX3 * 16u <= 6u * kR1 * 16u, "layer-3 output overlaps");
+constexpr uint32_t kTmemCols = 256;    // power of two >= 32 x kB1
 
 // Host-side packing of the network parameters (cnn_layer_offset order, f32)
 // into the block copied verbatim into shared memory: BF16 weights in the
 // K-major operand layouts above; layer 4 and the biases as BF16-rounded f32.
 inline void pack_weights(const float* p, unsigned char* out) {
   auto bf = [](float v) { return __float2bfloat16_rn(v); };
+  // layer 1: chunk kc = 2 ky + c holds taps kx = 2c (j < 4) and 2c + 1 (j >= 4)
+  // of kernel row ky, channel j % 4; kx = 3 is zero
   __nv_bfloat16* w1 = reinterpret_cast<__nv_bfloat16*>(out);
   for (int kc = 0; kc < 6; kc++)
     for (int co = 0; co < 32; co++)
       for (int j = 0; j < 8; j++) {
-        const int k = kc * 8 + j, tap = k / 4, ci = k % 4;
-        w1[(kc * 32 + co) * 8 + j] = bf(k < 36 ? p[cnn_layer_offset(0) + (co * 4 + ci) * 9 + tap] : 0.0f);
+        const int ky = kc / 2, kx = 2 * (kc % 2) + j / 4, ci = j % 4;
+        w1[(kc * 32 + co) * 8 + j] = bf(kx < 3 ? p[cnn_layer_offset(0) + (co * 4 + ci) * 9 + ky * 3 + kx] : 0.0f);
       }
   for (int l = 1; l <= 2; l++) {
     __nv_bfloat16* w = reinterpret_cast<__nv_bfloat16*>(out + (l == 1 ? kOffW2 : kOffW3) - kOffW1);
@@ -132,18 +138,48 @@ __device__ __forceinline__ void commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
+// Bounded wait (~2^31 cycles).  Waiting threads sleep in try_wait (suspend
+// hint) rather than spin, so they take no issue slots from the thread that
+// issues the MMAs.
 __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity) {
   const long long t0 = clock64();
   for (;;) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
-        : "r"(bar), "r"(parity)
+        : "r"(bar), "r"(parity), "r"(100000u)
         : "memory");
     if (ok) return true;
     if (clock64() - t0 > (1ll << 31)) return false;
   }
+}
+
+// One layer's MMAs, fully unrolled: BLOCKS accumulator blocks of 128 rows,
+// TAPS (3: kernel rows of the paired features, at row offset ky * PITCH;
+// 9: 3 x 3 taps at ky * PITCH + kx), KSTEPS MMAs of K = 16 per tap, A operand
+// [K / 8][A_ROWS][8] (or A_LBO bytes between its K chunks), weights
+// [K / 8][N][8].  Every descriptor is the layer's
+// base descriptor plus a compile-time offset in its 14-bit address field
+// (all operands lie below 256 KB, so the field cannot carry).
+template <int BLOCKS, int TAPS, int KSTEPS, int A_ROWS, int PITCH, int N, uint32_t A_LBO = A_ROWS * 16u>
+__device__ __forceinline__ void issue_layer(uint32_t tmem, uint32_t a_base, uint32_t w_base) {
+  constexpr uint32_t id = idesc(128, N);
+  const uint64_t a0 = sdesc(a_base, A_LBO, 128u);
+  const uint64_t b0 = sdesc(w_base, N * 16u, 128u);
+#pragma unroll
+  for (int mb = 0; mb < BLOCKS; mb++)
+#pragma unroll
+    for (int t = 0; t < TAPS; t++)
+#pragma unroll
+      for (int s = 0; s < KSTEPS; s++) {
+        static_assert(TAPS == 3 || TAPS == 9, "taps");
+        const uint32_t shift = (uint32_t)(mb * 128 + (TAPS == 9 ? (t / 3) * PITCH + t % 3 : t * PITCH));
+        const uint32_t kc = (uint32_t)(TAPS == 9 ? t * 4 + 2 * s : 2 * t + 2 * s);
+        const uint64_t a = a0 + (uint64_t)((uint32_t)(2 * s) * A_ROWS + shift);  // 16-byte units
+        const uint64_t b = b0 + (uint64_t)(kc * (uint32_t)N);
+        mma(tmem + (uint32_t)(mb * 32), a, b, id, (t > 0 || s > 0) ? 1u : 0u);
+      }
 }
 
 // 32 consecutive f32 columns of this thread's tensor-memory lane.
@@ -179,10 +215,11 @@ __device__ __forceinline__ void store_row(unsigned char* buf, int rows, int row,
 
 }  // namespace tc
 
-// Persistent: grid = min(tiles, multiprocessors), 256 threads, tc::kSmem
-// dynamic shared memory; each CTA sets up tensor memory, its mbarrier and the
-// packed parameters once and then walks tiles blockIdx.x, + gridDim.x, ...
-__global__ void __launch_bounds__(256, 1)
+// Persistent: grid = min(tiles, 2 x multiprocessors), 256 threads,
+// tc::kSmem dynamic shared memory; each CTA sets up tensor memory, its
+// mbarrier and the packed parameters once and then walks tiles blockIdx.x,
+// + gridDim.x, ...
+__global__ void __launch_bounds__(256, 2)
     k_closure_infer_tc(Layout L, const float* __restrict__ rho, const float* __restrict__ jx,
                        const float* __restrict__ jy, const uint32_t* __restrict__ mask,
                        const unsigned char* __restrict__ wpack, float s_rho, float s_u, float dt_max,
@@ -191,14 +228,14 @@ __global__ void __launch_bounds__(256, 1)
   extern __shared__ __align__(1024) unsigned char sm[];
   uint32_t& tmem_slot = *reinterpret_cast<uint32_t*>(sm + kOffBar + 8);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  float* feat = reinterpret_cast<float*>(sm + kOffFeat);
   const float* bias = reinterpret_cast<const float*>(sm + kOffBias);  // b1, b2, b3 (32 each), b4
   const uint32_t bar = saddr(sm + kOffBar);
   const uint32_t base = saddr(sm);
   const int tiles_x = (L.nx + kT - 1) / kT, tiles = tiles_x * ((L.ny + kT - 1) / kT);
 
-  if (warp == 0) {  // tensor memory: 128 columns for the CTA's lifetime
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 128;" ::"r"(saddr(&tmem_slot)));
+  if (warp == 0) {  // tensor memory for the CTA's lifetime
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(saddr(&tmem_slot)),
+                 "n"(kTmemCols));
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
   }
   if (tid == 0) {
@@ -218,23 +255,8 @@ __global__ void __launch_bounds__(256, 1)
   uint32_t phase = 0;
   bool ok = true;
 
-  // Issues one layer's MMAs (thread 0) and waits for them (everyone).
-  auto run_layer = [&](int blocks, int taps, int ksteps, uint32_t a_base, uint32_t a_rows, int pitch,
-                       uint32_t w_base, int n = 32) {
-    if (tid == 0) {
-      const uint32_t id = idesc(128, n);
-      const uint32_t wchunk = (uint32_t)n * 16u;  // bytes of one 8-wide K chunk of the weights
-      for (int mb = 0; mb < blocks; mb++)
-        for (int t = 0; t < taps; t++)
-          for (int s = 0; s < ksteps; s++) {
-            const uint32_t shift = (uint32_t)(mb * 128 + (taps == 9 ? (t / 3) * pitch + t % 3 : 0));
-            const uint32_t kc = (uint32_t)(taps == 9 ? t * 4 + 2 * s : 2 * s);
-            const uint64_t a = sdesc(a_base + (uint32_t)(2 * s) * a_rows * 16u + shift * 16u, a_rows * 16u, 128u);
-            const uint64_t b = sdesc(w_base + kc * wchunk, wchunk, 128u);
-            mma(tmem + (uint32_t)(mb * 32), a, b, id, (t > 0 || s > 0) ? 1u : 0u);
-          }
-      commit(bar);
-    }
+  // Waits for the MMAs thread 0 issued and committed (everyone).
+  auto wait_layer = [&]() {
     if (ok && !bar_wait(bar, phase & 1u)) ok = false;
     phase++;
     tc_after();
@@ -278,7 +300,9 @@ __global__ void __launch_bounds__(256, 1)
 
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     const int tx0 = (tile % tiles_x) * kT, ty0 = (tile / tiles_x) * kT;
-    // features of the 24 x 24 window (the previous tile's layer 4 is done reading)
+    // paired features (the previous tile's layer 3 is done reading X2, which
+    // shares their region): window pixel i goes to the low half of row i and
+    // the high half of row i - 1; rows from 575 on are zero beyond the window
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < kFeatPer; k++) {
@@ -291,51 +315,50 @@ __global__ void __launch_bounds__(256, 1)
         o.y = f.y / f.x * s_u;
         o.z = f.z / f.x * s_u;
       }
-      reinterpret_cast<float4*>(feat)[i] = o;
+      __nv_bfloat162 h[2] = {__floats2bfloat162_rn(o.x, o.y), __floats2bfloat162_rn(o.z, o.w)};
+      const uint2 hv = *reinterpret_cast<uint2*>(h);
+      *reinterpret_cast<uint2*>(sm + kOffF + (size_t)i * 16) = hv;
+      if (i > 0) *reinterpret_cast<uint2*>(sm + kOffF + (size_t)(i - 1) * 16 + 8) = hv;
     }
-    __syncthreads();
+    for (int i = kW0 * kW0 - 1 + tid; i < kRF; i += blockDim.x) {
+      if (i == kW0 * kW0 - 1) *reinterpret_cast<uint2*>(sm + kOffF + (size_t)i * 16 + 8) = make_uint2(0u, 0u);
+      else *reinterpret_cast<uint4*>(sm + kOffF + (size_t)i * 16) = make_uint4(0u, 0u, 0u, 0u);
+    }
     load_feats(tile + gridDim.x);  // in flight while this tile's layers run
-    // layer-1 im2col: row p = oy * 22 + ox, K = tap * 4 + ci; chunk kc holds
-    // taps 2 kc and 2 kc + 1.  Pixel-fastest order: a warp reads and writes
-    // consecutive 16-byte rows (no bank conflicts).
-    for (int i = tid; i < kR1 * 6; i += blockDim.x) {
-      const int kc = i / kR1, p = i % kR1;
-      float4 a = make_float4(0.0f, 0.0f, 0.0f, 0.0f), b = a;
-      if (p < kM1) {
-        const int oy = p / kW1, ox = p % kW1, t0 = 2 * kc, t1 = 2 * kc + 1;
-        const float4* f4 = reinterpret_cast<const float4*>(feat);
-        if (t0 < 9) a = f4[(oy + t0 / 3) * kW0 + ox + t0 % 3];
-        if (t1 < 9) b = f4[(oy + t1 / 3) * kW0 + ox + t1 % 3];
-      }
-      __nv_bfloat162 e[4] = {__floats2bfloat162_rn(a.x, a.y), __floats2bfloat162_rn(a.z, a.w),
-                             __floats2bfloat162_rn(b.x, b.y), __floats2bfloat162_rn(b.z, b.w)};
-      *reinterpret_cast<uint4*>(sm + kOffA1 + ((size_t)kc * kR1 + p) * 16) = *reinterpret_cast<uint4*>(e);
-    }
     sync_async();
 
     // ---- layer 1 -> X1 (pitch 22) ---------------------------------------------------------
-    run_layer(kB1, 1, 3, base + kOffA1, kR1, 0, base + kOffW1);
+    if (tid == 0) {
+      issue_layer<kB1, 3, 1, 0, kW0, 32, 32u>(tmem, base + kOffF, base + kOffW1);
+      commit(bar);
+    }
+    wait_layer();
     for (int mb = warp >> 2; mb < kB1; mb += 2) {
       float v[32];
       tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
       const int p = mb * 128 + 32 * (warp & 3) + lane;
-      if (p < kM1) {
-        const int oy = p / kW1, ox = p % kW1, gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
+      const int oy = p / kW0, ox = p % kW0;
+      if (p < kM1 && ox < kW1) {
+        const int gx = tx0 - 3 + ox, gy = ty0 - 3 + oy;
         const bool inside = gx >= 0 && gx < L.nx && gy >= 0 && gy < L.ny;
 #pragma unroll
         for (int c = 0; c < 32; c++) v[c] = inside ? fmaxf(v[c] + bias[c], 0.0f) : 0.0f;
-        store_row(sm + kOffX1, kRX1, p, v);
+        store_row(sm + kOffX1, kRX1, oy * kW1 + ox, v);
       }
     }
     // rows of X1 beyond the window: zero (read only by dropped outputs, but keep them finite)
-    for (int i = tid; i < 4 * (kRX1 - kM1); i += blockDim.x) {
-      const int c = i / (kRX1 - kM1), r = kM1 + i % (kRX1 - kM1);
+    for (int i = tid; i < 4 * (kRX1 - kW1 * kW1); i += blockDim.x) {
+      const int c = i / (kRX1 - kW1 * kW1), r = kW1 * kW1 + i % (kRX1 - kW1 * kW1);
       *reinterpret_cast<uint4*>(sm + kOffX1 + ((size_t)c * kRX1 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
     }
     sync_async();
 
-    // ---- layer 2 -> X2 (pitch 20) ---------------------------------------------------------
-    run_layer(kB2, 9, 2, base + kOffX1, kRX1, kW1, base + kOffW2);
+    // ---- layer 2 -> X2 (pitch 20, over the paired features) ---------------------------------
+    if (tid == 0) {
+      issue_layer<kB2, 9, 2, kRX1, kW1, 32>(tmem, base + kOffX1, base + kOffW2);
+      commit(bar);
+    }
+    wait_layer();
     for (int mb = warp >> 2; mb < kB2; mb += 2) {
       float v[32];
       tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
@@ -355,8 +378,12 @@ __global__ void __launch_bounds__(256, 1)
     }
     sync_async();
 
-    // ---- layer 3 -> X3 (pitch 18, in the im2col region) ------------------------------------
-    run_layer(kB3, 9, 2, base + kOffX2, kRX2, kW2, base + kOffW3);
+    // ---- layer 3 -> X3 (pitch 18, over X1) ----------------------------------------------------
+    if (tid == 0) {
+      issue_layer<kB3, 9, 2, kRX2, kW2, 32>(tmem, base + kOffX2, base + kOffW3);
+      commit(bar);
+    }
+    wait_layer();
     for (int mb = warp >> 2; mb < kB3; mb += 2) {
       float v[32];
       tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
@@ -377,7 +404,11 @@ __global__ void __launch_bounds__(256, 1)
     sync_async();
 
     // ---- layer 4 (32 -> 1, padded to N = 16) -> record ----------------------------------------
-    run_layer(kB4, 9, 2, base + kOffX3, kRX3, kW3, base + kOffW4, 16);
+    if (tid == 0) {
+      issue_layer<kB4, 9, 2, kRX3, kW3, 16>(tmem, base + kOffX3, base + kOffW4);
+      commit(bar);
+    }
+    wait_layer();
     for (int mb = warp >> 2; mb < kB4; mb += 2) {
       float v[32];
       tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
@@ -387,8 +418,10 @@ __global__ void __launch_bounds__(256, 1)
         const long long o = (long long)gy * L.pitch + gx;
         const float z = v[0] + bias[96];
         const float dt = dt_max / (1.0f + expf(-z));
-        const float4 f = reinterpret_cast<const float4*>(feat)[(oy + 4) * kW0 + ox + 4];  // |u| from the features
-        record[o] = __floats2half2_rn(dt, sqrtf(f.y * f.y + f.z * f.z) / s_u);
+        // |u| of the cell (solid cells: 0), from its moments
+        const bool solid = (mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u;
+        const float r = rho[o], ux = jx[o] / r, uy = jy[o] / r;
+        record[o] = __floats2half2_rn(dt, solid ? 0.0f : sqrtf(ux * ux + uy * uy));
       }
     }
     tc_before();  // the next tile's MMAs reuse the tensor memory
@@ -396,7 +429,7 @@ __global__ void __launch_bounds__(256, 1)
   tc_before();
   __syncthreads();
   tc_after();
-  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 128;" ::"r"(tmem));
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "n"(kTmemCols));
   if (!ok && tid == 0) atomicOr(flag, 2);
 }
 
