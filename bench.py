@@ -181,6 +181,83 @@ def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
             "nonfinite_domains": bad}
 
 
+def precision_check(lbm, torch, mask, steps, every=500, short=1000):
+    """Storage precision on the 4096 x 2048 workload: the same seeded run in
+    f64 (the GPU's FP64 run is the reference), f32, f16 (f - w) and bf16
+    (f - w) for `steps` steps.  For each: the relative L2 error over fluid
+    cells, against f64, of the velocity at step `short` (before the unsteady
+    wake amplifies rounding differences into different vortex trajectories),
+    of the velocity time-averaged over the second half (samples every `every`
+    steps) and of the final velocity; and the FP64 relative drift of the
+    fluid mass and x momentum sums from the first step to the last (the
+    channel is open at both ends, so the runs are compared with the f64 run's
+    drift, not with zero)."""
+    import ctypes
+    import numpy as np
+    L = lbm.load_library()
+    dev = torch.device("cuda")
+    fl = torch.from_numpy(mask == 0).to(dev)
+    fl[:, 0] = False  # the inlet column is set, not computed
+    tmp = torch.empty((NY, NX), dtype=torch.float32, device=dev)
+    runs = {}
+    for name, st in (("f64", lbm.F64), ("f32", lbm.F32), ("f16", lbm.F16), ("bf16", lbm.BF16)):
+        stream = torch.cuda.Stream()
+        acc = torch.zeros((2, NY, NX), dtype=torch.float64, device=dev)
+        fin = torch.empty((2, NY, NX), dtype=torch.float64, device=dev)
+        early = torch.empty((2, NY, NX), dtype=torch.float64, device=dev)
+        n_avg = 0
+        with lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, st) as lat:
+            lat.set_stream(stream.cuda_stream)
+            lat.set_inlet_velocity(UX)
+            lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+            lat.draw_mask(mask)
+            lat.iterate(1)
+            c0 = lat.conservation()
+            done = 1
+            with torch.cuda.stream(stream):
+                while done < steps:
+                    k = min(every - done % every, steps - done, short - done if done < short else steps)
+                    lat.iterate(k)
+                    done += k
+                    last = done >= steps
+                    if done > steps // 2 or last or done == short:
+                        for i, f in enumerate((3, 4)):  # ux, uy
+                            lbm._check(L.lbm_read_field_device(lat.handle, f, ctypes.c_void_p(tmp.data_ptr())))
+                            if done > steps // 2 and done % every == 0:
+                                acc[i] += tmp
+                            if last:
+                                fin[i] = tmp
+                            if done == short:
+                                early[i] = tmp
+                        n_avg += done > steps // 2 and done % every == 0
+            torch.cuda.synchronize()
+            try:
+                lat.synchronize()
+                finite = True
+            except lbm.LBMError:
+                finite = False
+            c1 = lat.conservation()
+        runs[name] = {"avg": acc / max(n_avg, 1), "fin": fin, "early": early, "finite": finite,
+                      "mass_drift": float((c1[0] - c0[0]) / c0[0]),
+                      "momentum_x_drift": float((c1[1] - c0[1]) / c0[1])}
+    ref = runs["f64"]
+
+    def rel(a, b):
+        d = (a - b)[:, fl]
+        return float(torch.linalg.vector_norm(d) / torch.linalg.vector_norm(b[:, fl]))
+
+    out = {"workload": "4096x2048 bench workload, %d steps; velocity averaged over the second half" % steps,
+           "reference": "f64 storage on the GPU", "short_steps": short}
+    for name, r in runs.items():
+        e = {"finite": r["finite"], "mass_drift": r["mass_drift"], "momentum_x_drift": r["momentum_x_drift"]}
+        if name != "f64":
+            e["rel_err_velocity_short"] = _finite_or_str(rel(r["early"], ref["early"]), 7)
+            e["rel_err_time_avg_velocity"] = _finite_or_str(rel(r["avg"], ref["avg"]), 7)
+            e["rel_err_final_velocity"] = _finite_or_str(rel(r["fin"], ref["fin"]), 7)
+        out[name] = e
+    return out
+
+
 def _finite_or_str(x, ndigits=4):
     """A float for the JSON line; "non-finite" where the run diverged (strict
     JSON has no Infinity or NaN)."""
@@ -339,6 +416,11 @@ def run_ours(args):
             variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
                               "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
 
+    # --- storage precision against an FP64 run of the same workload ----------------
+    precision = None
+    if not args.no_precision:
+        precision = precision_check(lbm, torch, mask, args.precision_steps)
+
     # --- learned closure: coarse run with the trained network vs the fine run -------
     closure_res = None
     if not args.no_closure:
@@ -378,6 +460,7 @@ def run_ours(args):
         "variants": variants,
         "batched": batched,
         "closure": closure_res,
+        "precision": precision,
         "gpu_launches": int(launches),
         "clocks": clocks.summary(),
         "wall_s_timed": round(wall, 4),
@@ -526,6 +609,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-closure", action="store_true")
+    ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--precision-steps", type=int, default=20000)
     ap.add_argument("--batched-steps", type=int, default=5000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
