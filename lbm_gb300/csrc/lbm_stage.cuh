@@ -3,11 +3,12 @@
 // A CTA owns a strip of kStageW = 256 columns and a contiguous band of rows.
 // One producer warp moves row segments of every population plane into a ring
 // of NS shared-memory stages with the bulk-copy engine (cp.async.bulk, bytes
-// counted on a "full" mbarrier per stage); 8 consumer warps (one cell per
-// thread) collide from shared memory and store straight to global memory,
-// then release the stage on an "empty" mbarrier (one arrival per warp).  No
-// CTA-wide barrier sits in the row loop, so warps run decoupled, limited only
-// by data arrival; the bytes in flight cost shared memory, not registers.
+// counted on a "full" mbarrier per stage); 256 / CPT consumer threads (CPT =
+// 1, 2 or 4 adjacent cells each) collide from shared memory and store
+// straight to global memory, then release the stage on an "empty" mbarrier
+// (one arrival per warp).  No CTA-wide barrier sits in the row loop, so warps
+// run decoupled, limited only by data arrival; the bytes in flight cost
+// shared memory, not registers.
 //
 // Stage r holds row r of the 8 moving planes of src (with a 16-byte halo on
 // each side for the x-1 / x+1 pulls), row r of the rest plane and row r of
@@ -19,8 +20,9 @@
 // solid cells collide their own previous values from dst (global memory) and
 // edge cells take the per-cell path (step_cell).
 //
-// Every mbarrier wait is bounded (~2^31 SM cycles).  A warp whose wait runs
-// out sets bit 1 of the error flag and leaves its loop; the other warps then
+// Every mbarrier wait is bounded (~2^31 SM cycles); a waiting thread sleeps
+// in try_wait rather than spinning.  A warp whose wait runs out sets bit 1 of
+// the error flag and leaves its loop; the other warps then
 // run out too, since nothing further completes; the producer finally waits,
 // again bounded, for the copies it issued, so no copy is in flight at exit.
 #pragma once
@@ -78,6 +80,13 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
   asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
                ::"r"(dst), "l"(src), "r"(bytes), "r"(bar)
                : "memory");
+}
+
+// One lane of a converged warp (elect.sync).
+__device__ __forceinline__ bool elect_one() {
+  uint32_t pred;
+  asm volatile("{\n .reg .pred p;\n elect.sync _|p, 0xffffffff;\n selp.u32 %0, 1, 0, p;\n}\n" : "=r"(pred));
+  return pred != 0;
 }
 
 constexpr int kStageW = 256;  // columns per CTA
@@ -182,35 +191,40 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   __syncthreads();
 
   if (producer) {
-    if ((tid & 31) == 0) {
-      // a strip narrower than kStageW (the grid's last) copies only its own
-      // columns and halo, rounded up to 16 bytes; stage offsets stay fixed
-      const int w = min(kStageW, L.nx - xb);
-      const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
-      const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
-      const uint32_t stage_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes;
-      int r = r_first, s = 0;
-      uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
-      bool ok = true;
-      for (; r <= r_last; r++) {
-        if (r - r_first >= NS && !mbar_wait(smem_addr(&empty[s]), empty_parity)) {
-          ok = false;
-          break;
-        }
-        int rr = r;
-        if (EDGE == EDGE_CHANNEL) rr = rr < 0 ? rr + L.ny : (rr >= L.ny ? rr - L.ny : rr);
-        else rr = min(max(rr, 0), L.ny - 1);
-        unsigned char* st = smem + (size_t)s * G::kBytes;
-        const uint32_t bar = smem_addr(&full[s]);
+    // the whole warp runs the loop on warp-uniform values; one elected lane
+    // arms the barrier and issues the stage's copies
+    // a strip narrower than kStageW (the grid's last) copies only its own
+    // columns and halo, rounded up to 16 bytes; stage offsets stay fixed
+    const int w = min(kStageW, L.nx - xb);
+    const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
+    const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
+    const uint32_t stage_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes;
+    int r = r_first, s = 0;
+    uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
+    bool ok = true;
+    for (; r <= r_last; r++) {
+      if (r - r_first >= NS && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&empty[s]), empty_parity))) {
+        ok = false;
+        break;
+      }
+      int rr = r;
+      if (EDGE == EDGE_CHANNEL) rr = rr < 0 ? rr + L.ny : (rr >= L.ny ? rr - L.ny : rr);
+      else rr = min(max(rr, 0), L.ny - 1);
+      unsigned char* st = smem + (size_t)s * G::kBytes;
+      const uint32_t bar = smem_addr(&full[s]);
+      const long long row = (long long)rr * L.pitch + xb;
+      if (elect_one()) {
         mbar_arrive_expect_tx(bar, stage_bytes);
-        const long long row = (long long)rr * L.pitch + xb;
 #pragma unroll
         for (int p = 0; p < 8; p++)
           bulk_g2s(smem_addr(st + p * G::kSegBytes), a.srcp[p] + row - G::kHalo, seg_bytes, bar);
         bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + row, rest_bytes, bar);
         bulk_g2s(smem_addr(st + G::kMaskOff), a.mask + (long long)rr * L.mw + (xb >> 5) - 4, G::kMaskBytes, bar);
-        if (++s == NS) { s = 0; empty_parity ^= 1u; }
       }
+      __syncwarp();
+      if (++s == NS) { s = 0; empty_parity ^= 1u; }
+    }
+    if ((tid & 31) == 0) {
       if (!ok) atomicOr(a.flag, 2);
       // no copy may be in flight when the CTA exits: wait (bounded) for the
       // last NS stages issued
