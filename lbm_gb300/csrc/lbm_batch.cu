@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 6)
           for (int j = 0; j < CPT; j++)
             if (x0 + j < sa.L.nx) step_cell<St, EDGE_CHANNEL>(sa, x0 + j, y);
     } else {
-      ws_tile<St, EDGE_CHANNEL, NS, CPT, false>(sa, T.y, T.z, T.w, smem, full, empty);
+      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, kStageW>(sa, T.y, T.z, T.w, smem, full, empty);
       __syncthreads();  // every arrival and copy of this tile is complete
       if (threadIdx.x == 0)
         for (int i = 0; i < NS; i++) {  // the next tile initialises them again

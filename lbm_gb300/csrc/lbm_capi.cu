@@ -231,12 +231,12 @@ void release(lbm_sim* s) {
 
 // Staged step launch: one strip of kStageW columns per grid column, row bands
 // sized so that all CTAs are resident at once (one wave, equal work).
-template <class St, int EDGE, int NS, int CPT, bool CL>
+template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
 int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
-  constexpr int W = kStageW, TPB = stage_threads<CPT>();
-  using G = StageGeom<typename St::S>;
+  constexpr int TPB = stage_threads<CPT, W>();
+  using G = StageGeom<typename St::S, W>;
   const size_t smem = (size_t)NS * G::kBytes;
-  auto kern = k_step_ws<St, EDGE, NS, CPT, CL>;
+  auto kern = k_step_ws<St, EDGE, NS, CPT, CL, W>;
   const int variant = 2 * s->kernel + (CL ? 1 : 0);
   if (s->staged_variant != variant) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -262,9 +262,10 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   return LBM_OK;
 }
 
-// Staged variants: ring depth and cells per consumer thread (two cells per
-// thread exist for channel mode only, four for channel mode with 16-bit
-// storage; elsewhere those variants run the widest that exists).  With the
+// Staged variants: ring depth, cells per consumer thread and strip width
+// (two cells per thread exist for channel mode only; four cells, and 512-
+// column strips, for channel mode with 16-bit storage; elsewhere those
+// variants run the widest that exists).  With the
 // closure on, one ring depth per cells-per-thread count runs (4 stages for one
 // or four cells, 6 for two).
 template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
@@ -273,7 +274,7 @@ template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename
   if constexpr (EDGE == EDGE_CHANNEL && sizeof(typename St::S) <= 4) {  // the closure's modes
     if (a.closure) {
       if (s->kernel >= 2 && s->kernel <= 5) return launch_staged<St, EDGE, 4, 1, true>(s, a);
-      if (s->kernel >= 9) return launch_staged<St, EDGE, 4, C4, true>(s, a);
+      if (s->kernel == 9 || s->kernel == 10) return launch_staged<St, EDGE, 4, C4, true>(s, a);
       return launch_staged<St, EDGE, 6, C2, true>(s, a);
     }
   }
@@ -286,6 +287,13 @@ template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename
     case 7: return launch_staged<St, EDGE, 6, C2, false>(s, a);
     case 9: return launch_staged<St, EDGE, 4, C4, false>(s, a);
     case 10: return launch_staged<St, EDGE, 6, C4, false>(s, a);
+    case 11:
+    case 12:
+      if constexpr (EDGE == EDGE_CHANNEL && sizeof(typename St::S) == 2) {  // 512-column strips
+        return s->kernel == 11 ? launch_staged<St, EDGE, 6, 2, false, 2 * kStageW>(s, a)
+                               : launch_staged<St, EDGE, 4, 2, false, 2 * kStageW>(s, a);
+      }
+      return launch_staged<St, EDGE, 6, C2, false>(s, a);
     default: return launch_staged<St, EDGE, 4, C2, false>(s, a);
   }
 }
@@ -330,9 +338,11 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   s->edge = edge_mode;
   s->storage = storage;
   // fastest measured variant per storage width: 4-stage ring, one cell per
-  // thread for 4-byte words; 6-stage ring, two cells per thread for 2-byte
-  // words (reference mode runs one cell per thread); f64: the per-cell kernel
-  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : 7);
+  // thread for 4-byte words; 6-stage ring, two cells per thread and 512-column
+  // strips for 2-byte words (256-column strips below 1024 columns, where wide
+  // strips leave SMs idle; reference mode runs one cell per thread); f64: the
+  // per-cell kernel
+  s->kernel = storage == STORE_F32 ? 3 : (storage == STORE_F64 ? 0 : (nx >= 1024 ? 11 : 7));
   s->omega = omega;
   s->es = store_bytes(storage);
   s->cs = storage == STORE_F64 ? 8 : 4;
@@ -429,7 +439,7 @@ int lbm_get_stream(const lbm_sim* s, void** stream) {
 int lbm_set_tuning(lbm_sim* s, int rows_per_thread, int kernel) {
   CHECK_SIM(s);
   if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
-  if (kernel < 0 || kernel > 10) return fail(LBM_ERR_ARG, "kernel %d", kernel);
+  if (kernel < 0 || kernel > 12) return fail(LBM_ERR_ARG, "kernel %d", kernel);
   s->rows = rows_per_thread;
   s->kernel = kernel;
   s->staged_variant = -1;  // recompute the staged launch shape

@@ -91,13 +91,13 @@ __device__ __forceinline__ bool elect_one() {
 
 constexpr int kStageW = 256;  // columns per CTA
 
-// Shared-memory layout of one stage.
-template <class S> struct StageGeom {
+// Shared-memory layout of one stage of a W-column strip.
+template <class S, int W = kStageW> struct StageGeom {
   static constexpr int kHalo = 16 / (int)sizeof(S);  // elements in 16 bytes
-  static constexpr int kSeg = kStageW + 2 * kHalo;   // moving-plane segment
-  static constexpr int kMaskWords = kStageW / 32 + 8;  // 4 words before the strip, 4 after
+  static constexpr int kSeg = W + 2 * kHalo;         // moving-plane segment
+  static constexpr int kMaskWords = W / 32 + 8;      // 4 words before the strip, 4 after
   static constexpr uint32_t kSegBytes = kSeg * sizeof(S);
-  static constexpr uint32_t kRestBytes = kStageW * sizeof(S);
+  static constexpr uint32_t kRestBytes = W * sizeof(S);
   static constexpr uint32_t kMaskBytes = kMaskWords * 4;
   static constexpr uint32_t kMaskOff = 8 * kSegBytes + kRestBytes;
   static constexpr uint32_t kBytes = 8 * kSegBytes + kRestBytes + kMaskBytes;
@@ -153,17 +153,17 @@ __device__ __forceinline__ void load_pair(const __nv_bfloat16*, uint32_t w, floa
   hi = __uint_as_float(w & 0xFFFF0000u);
 }
 
-// Threads per CTA: kStageW / CPT consumers (CPT cells each) + one producer warp.
-template <int CPT> constexpr int stage_threads() { return kStageW / CPT + 32; }
+// Threads per CTA: W / CPT consumers (CPT cells each) + one producer warp.
+template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / CPT + 32; }
 
-// One tile of the staged step: columns [xb, xb + kStageW) of rows [y0, y1) of
+// One tile of the staged step: columns [xb, xb + W) of rows [y0, y1) of
 // the lattice described by `a` (kernel parameters, or a copy in shared memory
 // for the batched kernel).  Every thread of the CTA calls it.  It arms the
 // ring's barriers itself, so consecutive tiles of a persistent CTA reuse the
 // ring once the CTA has synchronised between them.  CL selects the per-cell
 // relaxation time of the learned closure (a.closure must then be set);
 // without it omega is uniform and its derived constants are computed once.
-template <class St, int EDGE, int NS, int CPT, bool CL, class A>
+template <class St, int EDGE, int NS, int CPT, bool CL, int W, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
                                         uint64_t* empty) {
   using S = typename St::S;
@@ -171,8 +171,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
                     (CPT == 4 && EDGE == EDGE_CHANNEL && sizeof(S) == 2),
                 "two cells per thread: channel mode only; four: channel mode, 16-bit storage");
   using C = typename St::C;
-  using G = StageGeom<S>;
-  constexpr int kConsumers = kStageW / CPT;
+  using G = StageGeom<S, W>;
+  constexpr int kConsumers = W / CPT;
   constexpr int kConsumerWarps = kConsumers / 32;
   const Layout& L = a.L;
   const int tid = threadIdx.x;
@@ -193,9 +193,9 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   if (producer) {
     // the whole warp runs the loop on warp-uniform values; one elected lane
     // arms the barrier and issues the stage's copies
-    // a strip narrower than kStageW (the grid's last) copies only its own
+    // a strip narrower than W (the grid's last) copies only its own
     // columns and halo, rounded up to 16 bytes; stage offsets stay fixed
-    const int w = min(kStageW, L.nx - xb);
+    const int w = min(W, L.nx - xb);
     const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t stage_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes;
@@ -490,25 +490,26 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 }
 
 // The staged step over one lattice: CTA (bx, by) takes strip bx and row band by.
-template <class St, int EDGE, int NS, int CPT, bool CL>
-__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : (CPT == 2 ? (sizeof(typename St::S) == 8 ? 5 : 6) : 8))
+template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
+__global__ void __launch_bounds__(stage_threads<CPT, W>(),
+                                  W != kStageW ? 3 : (CPT == 1 ? 4 : (CPT == 2 ? (sizeof(typename St::S) == 8 ? 5 : 6) : 8)))
     k_step_ws(StepArgs<typename St::S, typename St::C> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NS];
   __shared__ __align__(8) uint64_t empty[NS];
-  const int xb = blockIdx.x * kStageW;
+  const int xb = blockIdx.x * W;
   const int y0 = blockIdx.y * a.rows;
   const int y1 = min(y0 + a.rows, a.L.ny);
   if (y0 >= y1) return;  // uniform per CTA
   if (a.materialised) {  // uniform: collide in place, per cell, from global memory
     const int x0 = xb + CPT * threadIdx.x;
-    if ((int)threadIdx.x < kStageW / CPT)
+    if ((int)threadIdx.x < W / CPT)
       for (int y = y0; y < y1; y++)
         for (int j = 0; j < CPT; j++)
           if (x0 + j < a.L.nx) step_cell<St, EDGE>(a, x0 + j, y);
     return;
   }
-  ws_tile<St, EDGE, NS, CPT, CL>(a, xb, y0, y1, smem, full, empty);
+  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty);
 }
 
 }  // namespace lbm

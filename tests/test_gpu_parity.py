@@ -124,7 +124,7 @@ STORAGES = [(0, 0, False), (3, 3, True), (1, 1, False), (2, 2, False)]  # (lbm s
 @pytest.mark.parametrize("edge", [0, 1])
 @pytest.mark.parametrize("nx,ny,rows", [(8, 6, 1), (33, 17, 4), (70, 41, 8), (129, 64, 5), (131, 20, 3),
                                         (600, 37, 7), (1100, 700, 9)])
-@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5, 6, 8, 9, 10])
+@pytest.mark.parametrize("kernel", [0, 1, 2, 3, 5, 6, 8, 9, 10, 11, 12])
 def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, edge, nx, ny, rows, kernel):
     P = oracle_mod
     rng = np.random.default_rng(nx * 1000 + ny + 7 * storage + edge)

@@ -8,7 +8,7 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("storage,kernel,slabs", [(0, 3, 2), (0, 0, 3), (1, 8, 2), (2, 1, 4)])
+@pytest.mark.parametrize("storage,kernel,slabs", [(0, 3, 2), (0, 0, 3), (1, 8, 2), (2, 1, 4), (1, 11, 2), (2, 9, 3)])
 def test_gpu_slabs_match_one_lattice(lbm, cuda_ok, storage, kernel, slabs):
     from lbm_gb300 import geometry
     from lbm_gb300.slab import LocalExchanger, SlabLattice, run_local
