@@ -60,8 +60,10 @@ int lbm_batch_synchronize(lbm_batch* batch);
 int lbm_batch_read_field(lbm_batch* batch, uint32_t domain, int field, float* out);
 int lbm_batch_read_populations(lbm_batch* batch, uint32_t domain, float* out);
 
-/* Fix the schedule by hand: variant 0..3 = (ring stages, cells per thread)
- * (4,1) (6,1) (4,2) (8,2); dynamic 0 = tiles sorted longest first and dealt
+/* Fix the schedule by hand: variant 0..5 = (ring stages, cells per thread,
+ * strip columns) (4,1,256) (6,1,256) (4,2,256) (8,2,256) (6,2,512)
+ * (4,2,512), the 512-column strips for f16 / bf16 only (f32 runs variants 4
+ * and 5 with 256-column strips); dynamic 0 = tiles sorted longest first and dealt
  * round-robin to the persistent CTAs, 1 = CTAs take tiles from an atomic
  * counter; rows_per_bucket[3] = target band height for domains of height
  * <= 128, <= 256 and taller (NULL keeps the current ones). */

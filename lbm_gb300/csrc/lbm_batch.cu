@@ -61,9 +61,10 @@ struct DomainDev {
   float omega;
 };
 
-// One step over every tile.  Tile t = (domain, xb, y0, y1).
-template <class St, int NS, int CPT>
-__global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 6)
+// One step over every tile.  Tile t = (domain, xb, y0, y1); strips are W
+// columns wide.
+template <class St, int NS, int CPT, int W>
+__global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (CPT == 1 ? 4 : 6))
     k_batch_step(const DomainDev* __restrict__ doms, const int4* __restrict__ tiles, int ntiles, int src_i, int dst_i,
                  int materialised, int write_moments, int dynamic, int* counter, int* flag) {
   using S = typename St::S;
@@ -108,12 +109,12 @@ __global__ void __launch_bounds__(stage_threads<CPT>(), CPT == 1 ? 4 : 6)
     __syncthreads();
     if (materialised) {
       const int x0 = T.y + CPT * (int)threadIdx.x;
-      if ((int)threadIdx.x < kStageW / CPT)
+      if ((int)threadIdx.x < W / CPT)
         for (int y = T.z; y < T.w; y++)
           for (int j = 0; j < CPT; j++)
             if (x0 + j < sa.L.nx) step_cell<St, EDGE_CHANNEL>(sa, x0 + j, y);
     } else {
-      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, kStageW>(sa, T.y, T.z, T.w, smem, full, empty);
+      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W>(sa, T.y, T.z, T.w, smem, full, empty);
       __syncthreads();  // every arrival and copy of this tile is complete
       if (threadIdx.x == 0)
         for (int i = 0; i < NS; i++) {  // the next tile initialises them again
@@ -140,7 +141,11 @@ struct Config {
 };
 
 // (ring depth, cells per thread)
-constexpr int kVariants[4][2] = {{4, 1}, {6, 1}, {4, 2}, {8, 2}};
+// (ring stages, cells per thread, strip columns); the 512-column strips exist
+// for 16-bit storage only (f32 runs them as 256-column strips)
+constexpr int kVariants[6][3] = {{4, 1, 256}, {6, 1, 256}, {4, 2, 256}, {8, 2, 256}, {6, 2, 512}, {4, 2, 512}};
+constexpr int kNumVariants = 6;
+int strip_of(int variant, int storage) { return storage == STORE_F32 ? kStageW : kVariants[variant][2]; }
 
 }  // namespace
 
@@ -179,22 +184,23 @@ template <class F> int dispatch_st(int storage, F&& f) {
   return bfail(LBM_ERR_ARG, "batched lattices support f32, f16 and bf16 storage");
 }
 
-template <class St, int NS, int CPT> void* kernel_ptr() { return (void*)k_batch_step<St, NS, CPT>; }
+template <class St, int NS, int CPT, int W> void* kernel_ptr() { return (void*)k_batch_step<St, NS, CPT, W>; }
 
 template <class St> void* variant_kernel(int v) {
+  constexpr bool k16 = sizeof(typename St::S) == 2;
   switch (v) {
-    case 0: return kernel_ptr<St, 4, 1>();
-    case 1: return kernel_ptr<St, 6, 1>();
-    case 2: return kernel_ptr<St, 4, 2>();
-    default: return kernel_ptr<St, 8, 2>();
+    case 0: return kernel_ptr<St, 4, 1, kStageW>();
+    case 1: return kernel_ptr<St, 6, 1, kStageW>();
+    case 2: return kernel_ptr<St, 4, 2, kStageW>();
+    case 3: return kernel_ptr<St, 8, 2, kStageW>();
+    case 4: return k16 ? kernel_ptr<St, 6, 2, 2 * kStageW>() : kernel_ptr<St, 6, 2, kStageW>();
+    default: return k16 ? kernel_ptr<St, 4, 2, 2 * kStageW>() : kernel_ptr<St, 4, 2, kStageW>();
   }
 }
 
-size_t stage_bytes(int storage) {
-  switch (storage) {
-    case STORE_F32: return StageGeom<float>::kBytes;
-    default: return StageGeom<__half>::kBytes;
-  }
+size_t stage_bytes(int storage, int w) {
+  if (storage == STORE_F32) return StageGeom<float>::kBytes;
+  return w == kStageW ? StageGeom<__half>::kBytes : StageGeom<__half, 2 * kStageW>::kBytes;
 }
 
 void drop_graphs(lbm_batch* b) {
@@ -207,18 +213,19 @@ void drop_graphs(lbm_batch* b) {
 
 // Tile table for the current configuration, longest tiles first.
 int build_tiles(lbm_batch* b) {
+  const int W = strip_of(b->cfg.variant, b->storage);
   std::vector<int4> t;
   for (int d = 0; d < b->count; d++) {
     const DomainHost& h = b->doms[d];
     const int want = b->cfg.rows[bucket_of(h.ny)];
     const int bands = std::max(1, (h.ny + want - 1) / want);
     const int rows = (h.ny + bands - 1) / bands;
-    for (int xb = 0; xb < h.nx; xb += kStageW)
+    for (int xb = 0; xb < h.nx; xb += W)
       for (int y0 = 0; y0 < h.ny; y0 += rows) t.push_back(make_int4(d, xb, y0, std::min(y0 + rows, h.ny)));
   }
   std::stable_sort(t.begin(), t.end(), [&](const int4& a, const int4& c) {
-    const long long wa = (long long)(a.w - a.z) * std::min(kStageW, b->doms[a.x].nx - a.y);
-    const long long wc = (long long)(c.w - c.z) * std::min(kStageW, b->doms[c.x].nx - c.y);
+    const long long wa = (long long)(a.w - a.z) * std::min(W, b->doms[a.x].nx - a.y);
+    const long long wc = (long long)(c.w - c.z) * std::min(W, b->doms[c.x].nx - c.y);
     return wa > wc;
   });
   if ((int)t.size() > b->tiles_cap) {
@@ -237,13 +244,14 @@ int configure(lbm_batch* b) {
   int rc = build_tiles(b);
   if (rc) return rc;
   const int NS = kVariants[b->cfg.variant][0], CPT = kVariants[b->cfg.variant][1];
-  const size_t smem = (size_t)NS * stage_bytes(b->storage);
+  const int W = strip_of(b->cfg.variant, b->storage);
+  const size_t smem = (size_t)NS * stage_bytes(b->storage, W);
   auto setup = [&](auto tag) -> int {
     using St = decltype(tag);
     void* k = variant_kernel<St>(b->cfg.variant);
     BCK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0, sms = 0;
-    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, kStageW / CPT + 32, smem));
+    BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, W / CPT + 32, smem));
     BCK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
     if (occ < 1) return bfail(LBM_ERR_CUDA, "batched step kernel does not fit on a multiprocessor");
     b->grid = std::min(occ * sms, b->ntiles);
@@ -257,14 +265,15 @@ int configure(lbm_batch* b) {
 // One step; `counter` is the ticket counter this launch uses.
 int launch_step(lbm_batch* b, bool write_moments, int* counter) {
   const int NS = kVariants[b->cfg.variant][0], CPT = kVariants[b->cfg.variant][1];
-  const size_t smem = (size_t)NS * stage_bytes(b->storage);
+  const int W = strip_of(b->cfg.variant, b->storage);
+  const size_t smem = (size_t)NS * stage_bytes(b->storage, W);
   const int src = b->cur, dst = b->materialised ? b->cur : 1 - b->cur;
   int mat = b->materialised ? 1 : 0, wm = write_moments ? 1 : 0, dyn = b->cfg.dynamic;
   if (dyn) BCK(cudaMemsetAsync(counter, 0, sizeof(int), b->stream));
   void* args[] = {&b->d_doms, &b->d_tiles, &b->ntiles, (void*)&src, (void*)&dst, &mat, &wm, &dyn, &counter, &b->d_flag};
   auto go = [&](auto tag) -> int {
     using St = decltype(tag);
-    BCK(cudaLaunchKernel(variant_kernel<St>(b->cfg.variant), dim3(b->grid), dim3(kStageW / CPT + 32), args, smem,
+    BCK(cudaLaunchKernel(variant_kernel<St>(b->cfg.variant), dim3(b->grid), dim3(W / CPT + 32), args, smem,
                          b->stream));
     return LBM_OK;
   };
@@ -597,7 +606,8 @@ int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
 
 int lbm_batch_set_schedule(lbm_batch* b, int variant, int dynamic, const int* rows_per_bucket) {
   if (!b) return bfail(LBM_ERR_ARG, "null batch");
-  if (variant < 0 || variant > 3 || (dynamic != 0 && dynamic != 1)) return bfail(LBM_ERR_ARG, "bad schedule");
+  if (variant < 0 || variant >= kNumVariants || (dynamic != 0 && dynamic != 1))
+    return bfail(LBM_ERR_ARG, "bad schedule");
   b->cfg.variant = variant;
   b->cfg.dynamic = dynamic;
   if (rows_per_bucket)
@@ -655,7 +665,7 @@ int lbm_batch_autotune(lbm_batch* b, uint32_t steps_per_trial, char* report, siz
   Config best_cfg = b->cfg;
   float best = 3.4e38f;
   // stage 1: ring depth x cells per thread x schedule
-  const int variants = b->storage == STORE_F32 ? 2 : 4;
+  const int variants = b->storage == STORE_F32 ? 2 : kNumVariants;
   for (int v = 0; v < variants; v++)
     for (int dyn = 0; dyn < 2; dyn++) {
       b->cfg = best_cfg;
@@ -682,10 +692,11 @@ int lbm_batch_autotune(lbm_batch* b, uint32_t steps_per_trial, char* report, siz
   int rc = configure(b);
   if (rc) return rc;
   const int NS = kVariants[b->cfg.variant][0], CPT = kVariants[b->cfg.variant][1];
-  snprintf(buf, sizeof buf, "], \"chosen\": {\"ring_stages\": %d, \"cells_per_thread\": %d, \"schedule\": \"%s\", "
+  snprintf(buf, sizeof buf, "], \"chosen\": {\"ring_stages\": %d, \"cells_per_thread\": %d, \"strip_columns\": %d, "
+           "\"schedule\": \"%s\", "
            "\"rows_per_band\": {\"ny<=128\": %d, \"ny<=256\": %d, \"ny>256\": %d}, \"ms_per_step\": %.5f, "
            "\"persistent_ctas\": %d, \"tiles\": %d}}",
-           NS, CPT, b->cfg.dynamic ? "dynamic" : "static_longest_first", b->cfg.rows[0], b->cfg.rows[1], b->cfg.rows[2],
+           NS, CPT, strip_of(b->cfg.variant, b->storage), b->cfg.dynamic ? "dynamic" : "static_longest_first", b->cfg.rows[0], b->cfg.rows[1], b->cfg.rows[2],
            best / T, b->grid, b->ntiles);
   rep += buf;
   b->report = rep;

@@ -73,7 +73,7 @@ def test_gpu_batch_matches_oracle_per_domain(lbm, cuda_ok, oracle_mod, storage, 
         assert b.info()[2] == 50
 
 
-SCHEDULES = [(v, dyn, rows) for v in range(4) for dyn in (0, 1) for rows in ([32, 32, 32], [5, 64, 7])]
+SCHEDULES = [(v, dyn, rows) for v in range(6) for dyn in (0, 1) for rows in ([32, 32, 32], [5, 64, 7])]
 
 
 @pytest.mark.parametrize("storage", [0, 1])
@@ -121,6 +121,7 @@ def test_gpu_batch_autotune_then_parity(lbm, cuda_ok, oracle_mod):
         rep = b.autotune(24)
         ch = rep["chosen"]
         assert ch["ring_stages"] in (4, 6, 8) and ch["cells_per_thread"] in (1, 2)
+        assert ch["strip_columns"] in (256, 512)
         assert ch["schedule"] in ("dynamic", "static_longest_first")
         assert len(rep["trials"]) >= 8 and ch["ms_per_step"] > 0
         b.init_equilibrium(1e-3, 1)
