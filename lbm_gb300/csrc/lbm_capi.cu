@@ -290,8 +290,8 @@ template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename
     case 11:
     case 12:
       if constexpr (EDGE == EDGE_CHANNEL && sizeof(typename St::S) == 2) {  // 512-column strips
-        return s->kernel == 11 ? launch_staged<St, EDGE, 6, 2, false, 2 * kStageW>(s, a)
-                               : launch_staged<St, EDGE, 4, 2, false, 2 * kStageW>(s, a);
+        return s->kernel == 11 ? launch_staged<St, EDGE, 5, 2, false, 2 * kStageW>(s, a)
+                               : launch_staged<St, EDGE, 6, 2, false, 2 * kStageW>(s, a);
       }
       return launch_staged<St, EDGE, 6, C2, false>(s, a);
     default: return launch_staged<St, EDGE, 4, C2, false>(s, a);
@@ -338,7 +338,7 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   s->edge = edge_mode;
   s->storage = storage;
   // fastest measured variant per storage width: 4-stage ring, one cell per
-  // thread for 4-byte words; 6-stage ring, two cells per thread and 512-column
+  // thread for 4-byte words; 5-stage ring, two cells per thread and 512-column
   // strips for 2-byte words (256-column strips below 1024 columns, where wide
   // strips leave SMs idle; reference mode runs one cell per thread); f64: the
   // per-cell kernel
