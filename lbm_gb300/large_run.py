@@ -12,8 +12,9 @@ For each run it reports MLUPS, achieved HBM GB/s on the step kernel
 (algorithmic bytes: 72 B per active cell in f32, 36 B in f16, +4 B of
 closure records), the relative FP64 drift of the fluid mass and momentum
 sums from the first to the last step, and the time-averaged velocity over
-the second half.  The f16 runs' time-averaged velocities are compared with
-the f32 run's (relative L2 over fluid cells).  Velocity averages stay on the
+the second half, and the first sample by which a step kernel had seen a
+non-finite density.  The f16 runs' time-averaged velocities are compared
+with the f32 run's (relative L2 over fluid cells).  Velocity averages stay on the
 device (lbm_read_field_device); the timed region holds only steps and
 inferences.  Prints one JSON line.
 """
@@ -48,7 +49,7 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
             _check(lib.lbm_closure_enable(lat.handle, float(drift)))
         lat.iterate(1)
         c0 = lat.conservation()
-        done, n_avg, dev_ms = 1, 0, 0.0
+        done, n_avg, dev_ms, first_bad = 1, 0, 0.0, None
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         while done < steps:
             k = min(every, steps - done)
@@ -65,6 +66,11 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
             torch.cuda.synchronize()
             dev_ms += e0.elapsed_time(e1)
             done += k
+            if first_bad is None:  # the step kernels' non-finite flag, outside the timing
+                try:
+                    lat.synchronize()
+                except LBMError:
+                    first_bad = done
             if done > steps // 2:
                 for i, f in enumerate((3, 4)):  # ux, uy of the last step's moments
                     _check(lib.lbm_read_field_device(lat.handle, f, ctypes.c_void_p(tmp.data_ptr())))
@@ -77,6 +83,7 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
         except LBMError:
             out["finite"] = False
         c1 = lat.conservation()
+        out["first_nonfinite_by_step"] = first_bad
         if params is not None:
             fb = ctypes.c_uint64(0)
             _check(lib.lbm_closure_fallback_count(lat.handle, ctypes.byref(fb), 1))
@@ -99,6 +106,8 @@ def main(argv=None):
     ap.add_argument("--u", type=float, default=0.05)
     ap.add_argument("--closure", default=None, help="train_closure output (.npz)")
     ap.add_argument("--refresh", type=int, default=20)
+    ap.add_argument("--drift", type=float, default=1.0, help="closure drift bound (multiples of the predicted |u|)")
+    ap.add_argument("--closure-only", action="store_true", help="skip the plain f32 and f16 runs")
     ap.add_argument("--seed", type=int, default=1)
     a = ap.parse_args(argv)
     nx, ny = a.size
@@ -106,21 +115,28 @@ def main(argv=None):
     rep = {"workload": "D2Q9 channel %dx%d, circles r 8-64, %.1f%% solid, tau %.2f, ux %.2f" %
            (nx, ny, 100 * mask.mean(), a.tau, a.u)}
     t0 = time.time()
-    r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed)
-    r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed)
+    rep["runs"] = []
+    u32 = None
     fl = mask == 0
     fl[:, 0] = False
 
     def err(u):
+        if u32 is None:
+            return None
         d = (u - u32)[:, fl]
         return float(np.linalg.norm(d) / np.linalg.norm(u32[:, fl])) if np.isfinite(d).all() else float("inf")
 
-    r16["vel_err_vs_f32"] = err(u16)
-    rep["runs"] = [r32, r16]
+    if not a.closure_only:
+        r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed)
+        r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed)
+        r16["vel_err_vs_f32"] = err(u16)
+        rep["runs"] = [r32, r16]
     if a.closure:
         params = np.load(a.closure)["params"]
-        rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh, seed=a.seed)
+        rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh,
+                     drift=a.drift, seed=a.seed)
         rc["vel_err_vs_f32"] = err(uc)
+        rc["refresh"], rc["drift"] = a.refresh, a.drift
         rep["runs"].append(rc)
     rep["wall_s"] = time.time() - t0
     print(json.dumps(rep))
