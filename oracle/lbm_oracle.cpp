@@ -141,8 +141,21 @@ struct StBF16 { using S = uint16_t; using C = float; static constexpr bool kDev 
   static C f_of(S s, int q) { return weight<float>(q) + bf16_to_float(s); }
   static S of_f(C v, int q) { return float_to_bf16_rn(v - weight<float>(q)); } };
 
+// Reciprocal by Newton's method, as the GPU kernels compute it: the seed
+// 0x7EF311C2 - bits(x) (a linear approximation of 1/x per binade), then three
+// steps r' = fma(r, fma(-x, r, 1), r).
+inline float recip_newton(float x) {
+  uint32_t b;
+  std::memcpy(&b, &x, 4);
+  b = 0x7EF311C2u - b;
+  float r;
+  std::memcpy(&r, &b, 4);
+  for (int i = 0; i < 3; i++) r = std::fma(r, std::fma(-x, r, 1.0f), r);
+  return r;
+}
+
 // Deviation-form BGK of the 16-bit storage modes, on g_q = f_q - w_q, with
-// rho = 1 + drho, one correctly rounded reciprocal and fused multiply-adds:
+// rho = 1 + drho, one reciprocal (recip_newton) and fused multiply-adds:
 // f_q^eq - w_q = w_q (c0 + rho (t + t^2/2)), t = 3 c_q.u, c0 = drho - 1.5 rho u^2,
 // written in j = rho u: rho (t + t^2/2) = T + (T / (2 rho)) T with T = 3 c_q.j,
 // c0 = drho - 1.5 |j|^2 / rho; relaxed as
@@ -162,7 +175,7 @@ inline float relax_dev(float g, float aw, float h, float t, float sign, float om
   return std::fma(aw, std::fma(h * t, t, sign * t), std::fma(omw, g, b));
 }
 inline void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
-  const float h = 0.5f * (1.0f / rho);
+  const float h = 0.5f * recip_newton(rho);
   const float c0 = std::fma(std::fma(jx, jx, jy * jy), -3.0f * h, drho);
   const float tx = 3.0f * jx, ty = 3.0f * jy;
   const float tp = tx + ty, tm = tx - ty;
