@@ -147,11 +147,14 @@ int lbm_single_cell(lbm_sim* sim, int direction);
  * collision (the reference's density_bg after iterate). Asynchronous. */
 int lbm_step(lbm_sim* sim, uint32_t n);
 
-/* Runs of 16 steps inside one lbm_step call are replayed from a CUDA graph
- * captured on first use (per buffer parity, recaptured when omega, the step
- * kernel, the stream or the closure change), on by default; results are the
- * same either way.  Not on the legacy default stream, which cannot be
- * captured.  enable = 0 turns it off and frees the graphs. */
+/* lbm_step replays CUDA graphs captured on first use: a call of 2 to 64
+ * steps is captured whole and replayed by later calls of the same length;
+ * longer calls replay runs of 16 steps (per buffer parity, recaptured when
+ * omega, the step kernel, the launch shape, the stream or the closure
+ * change).  On by default; results are the same either way.  Not on the
+ * legacy default stream, which cannot be captured, nor while the caller is
+ * capturing the lattice's stream.  enable = 0 turns it off and frees the
+ * graphs. */
 int lbm_set_graphs(lbm_sim* sim, int enable);
 
 /* Wait for queued work; returns LBM_ERR_STATE if a step saw a non-finite density. */

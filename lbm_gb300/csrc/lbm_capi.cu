@@ -65,7 +65,8 @@ namespace lbm_internal {
 void set_last_error(const char* msg) { g_err = msg; }
 }  // namespace lbm_internal
 
-constexpr int kStepGraph = 16;  // steps per captured graph (even)
+constexpr int kStepGraph = 16;   // steps per captured graph (even)
+constexpr int kRunGraphMax = 64; // longest call captured whole
 
 struct StepGraphKey {
   float omega = 0.0f, drift = 0.0f;
@@ -120,6 +121,11 @@ struct lbm_sim {
   bool use_graphs = true;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   StepGraphKey graph_key[2];
+  // a whole call of n <= kRunGraphMax steps (the last one writing moments),
+  // per starting buffer parity: repeated calls of the same length replay it
+  cudaGraphExec_t run_graph[2] = {nullptr, nullptr};
+  StepGraphKey run_key[2];
+  uint32_t run_n[2] = {0, 0};
 };
 
 namespace {
@@ -222,6 +228,8 @@ int check_sim(const lbm_sim* s) {
 
 void release(lbm_sim* s) {
   for (auto& g : s->graph)
+    if (g) cudaGraphExecDestroy(g);
+  for (auto& g : s->run_graph)
     if (g) cudaGraphExecDestroy(g);
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
@@ -622,16 +630,17 @@ static StepGraphKey graph_key(const lbm_sim* s) {
 }
 
 static void drop_step_graphs(lbm_sim* s) {
-  for (auto& g : s->graph)
-    if (g) {
-      cudaGraphExecDestroy(g);
-      g = nullptr;
-    }
+  for (auto* gs : {s->graph, s->run_graph})
+    for (int i = 0; i < 2; i++)
+      if (gs[i]) {
+        cudaGraphExecDestroy(gs[i]);
+        gs[i] = nullptr;
+      }
 }
 
-// Capture kStepGraph steps (no moments) from the current buffer parity.
-static int capture_steps(lbm_sim* s) {
-  cudaGraphExec_t& out = s->graph[s->cur];
+// Capture n steps from the current buffer parity into `out`; with
+// `moments` the last one writes the moments.
+static int capture_steps(lbm_sim* s, cudaGraphExec_t& out, uint32_t n, bool moments) {
   if (out) {
     cudaGraphExecDestroy(out);
     out = nullptr;
@@ -641,7 +650,7 @@ static int capture_steps(lbm_sim* s) {
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   int rc = LBM_OK;
-  for (int k = 0; k < kStepGraph && !rc; k++) rc = launch_step(s, false);
+  for (uint32_t k = 0; k < n && !rc; k++) rc = launch_step(s, moments && k + 1 == n);
   const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->cur = cur0;  // the capture recorded the launches without running them
   s->steps = steps0;
@@ -652,23 +661,45 @@ static int capture_steps(lbm_sim* s) {
   const cudaError_t ei = cudaGraphInstantiate(&out, g, 0);
   cudaGraphDestroy(g);
   if (ei != cudaSuccess) return fail(LBM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ei));
-  s->graph_key[s->cur] = graph_key(s);
   return LBM_OK;
 }
 
 int lbm_step(lbm_sim* s, uint32_t n) {
   CHECK_SIM(s);
   if (n == 0) return LBM_OK;
+  // Launch overhead dominates small grids, so steps replay captured graphs
+  // once the launch shape is known (the legacy default stream cannot be
+  // captured): a short call repeated with the same length replays one graph
+  // of the whole call; longer calls replay runs of kStepGraph steps.
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;  // a caller's own capture: plain launches
+  if (s->stream != nullptr) CK(cudaStreamIsCapturing(s->stream, &capturing));
+  auto steady = [&]() {
+    return s->use_graphs && s->stream != nullptr && capturing == cudaStreamCaptureStatusNone && !s->materialised &&
+           (s->storage == STORE_F64 || s->kernel < 2 ||
+            s->staged_variant == 2 * s->kernel + (s->closure_on ? 1 : 0));
+  };
+  if (n >= 2 && n <= (uint32_t)kRunGraphMax && steady()) {
+    const int c = s->cur;
+    if (!s->run_graph[c] || s->run_n[c] != n || !(s->run_key[c] == graph_key(s))) {
+      int rc = capture_steps(s, s->run_graph[c], n, true);
+      if (rc) return rc;
+      s->run_key[c] = graph_key(s);
+      s->run_n[c] = n;
+    }
+    CK(cudaGraphLaunch(s->run_graph[c], s->stream));
+    s->steps += n;
+    s->launches += n;
+    s->cur = c ^ (int)(n & 1u);
+    s->moments_valid = true;
+    return LBM_OK;
+  }
   for (uint32_t k = 0; k < n;) {
     const uint32_t left = n - k;
-    // runs of kStepGraph steps replay a captured graph: launch overhead
-    // dominates small grids (the legacy default stream cannot be captured)
-    const bool steady = !s->materialised && (s->storage == STORE_F64 || s->kernel < 2 ||
-                                             s->staged_variant == 2 * s->kernel + (s->closure_on ? 1 : 0));
-    if (s->use_graphs && steady && s->stream != nullptr && left > (uint32_t)kStepGraph) {
+    if (left > (uint32_t)kStepGraph && steady()) {
       if (!s->graph[s->cur] || !(s->graph_key[s->cur] == graph_key(s))) {
-        int rc = capture_steps(s);
+        int rc = capture_steps(s, s->graph[s->cur], kStepGraph, false);
         if (rc) return rc;
+        s->graph_key[s->cur] = graph_key(s);
       }
       CK(cudaGraphLaunch(s->graph[s->cur], s->stream));
       s->steps += kStepGraph;  // even: the buffer parity is unchanged

@@ -272,3 +272,33 @@ def test_gpu_graph_replay_is_transparent(lbm, cuda_ok, oracle_mod, kernel):
         states.append(lat.populations())
         lat.close()
     np.testing.assert_array_equal(states[0], states[1])
+
+
+@pytest.mark.parametrize("storage,prec,kernel", [(0, 0, 3), (1, 1, 11), (0, 0, 0)])
+def test_gpu_repeated_short_calls_replay_whole_call_graphs(lbm, cuda_ok, oracle_mod, storage, prec, kernel):
+    """Short lbm_step calls repeated with the same length replay one captured
+    graph per starting buffer parity (odd lengths alternate the two); a new
+    length, an omega change and a state edit recapture or fall back to plain
+    launches.  The state must match the oracle and a run without graphs."""
+    P = oracle_mod
+    nx, ny = 300, 70
+    rng = np.random.default_rng(5)
+    mask = (rng.random((ny, nx)) < 0.05).astype(np.uint8)
+    L = lbm.load_library()
+    plan = [7, 7, 7, 7, 2, 2, 64, 65, 7, 7]
+    states = []
+    for graphs in (1, 0):
+        lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, storage, prec, 0, mask, kernel=kernel)
+        lbm._check(L.lbm_set_graphs(lat.handle, graphs))
+        for i, n in enumerate(plan):
+            if i == 8:
+                w = float(np.float32(1.0 / 0.7))
+                lat.update_omega_buffer(w)
+                o.set_omega(w)
+            lat.iterate(n)
+            o.step(n)
+        assert_same_state(lat, o)
+        assert lat.get_compute_num() == sum(plan)
+        states.append(lat.populations())
+        lat.close()
+    np.testing.assert_array_equal(states[0], states[1])
