@@ -497,7 +497,7 @@ def cpu_baseline(mask, budget_s=12.0, threads=None):
         step, kind = o.step, "port"
     step(1)  # warm-up
     done, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < budget_s and done < 200:
+    while time.perf_counter() - t0 < budget_s and done < 2000:
         step(1)
         done += 1
     dt = time.perf_counter() - t0
