@@ -1,10 +1,11 @@
 // Staged, warp-specialised fused step (the default step kernel).
 //
-// A CTA owns a strip of kStageW = 256 columns and a contiguous band of rows.
-// One producer warp moves row segments of every population plane into a ring
-// of NS shared-memory stages with the bulk-copy engine (cp.async.bulk, bytes
-// counted on a "full" mbarrier per stage); 256 / CPT consumer threads (CPT =
-// 1, 2 or 4 adjacent cells each) collide from shared memory and store
+// A CTA owns a strip of W columns (kStageW = 256, or 512 for 16-bit storage)
+// and a contiguous band of rows.  One producer warp moves row segments of
+// every population plane into a ring of NS shared-memory stages with the
+// bulk-copy engine (cp.async.bulk, bytes counted on a "full" mbarrier per
+// stage); W / CPT consumer threads (CPT = 1, 2 or 4 adjacent cells each)
+// collide from shared memory and store
 // straight to global memory, then release the stage on an "empty" mbarrier
 // (one arrival per warp).  No CTA-wide barrier sits in the row loop, so warps
 // run decoupled, limited only by data arrival; the bytes in flight cost
@@ -191,10 +192,10 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   __syncthreads();
 
   if (producer) {
-    // the whole warp runs the loop on warp-uniform values; one elected lane
-    // arms the barrier and issues the stage's copies
-    // a strip narrower than W (the grid's last) copies only its own
-    // columns and halo, rounded up to 16 bytes; stage offsets stay fixed
+    // The whole warp runs the loop on warp-uniform values; one elected lane
+    // arms the barrier and issues the stage's copies.  A strip narrower than
+    // W (the grid's last) copies only its own columns and halo, rounded up
+    // to 16 bytes; stage offsets stay fixed.
     const int w = min(W, L.nx - xb);
     const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
