@@ -242,8 +242,7 @@ void release(lbm_sim* s) {
 template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
 int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int TPB = stage_threads<CPT, W>();
-  using G = StageGeom<typename St::S, W>;
-  const size_t smem = (size_t)NS * G::kBytes;
+  const size_t smem = (size_t)NS * stage_bytes<typename St::S, W, CL>();
   auto kern = k_step_ws<St, EDGE, NS, CPT, CL, W>;
   const int variant = 2 * s->kernel + (CL ? 1 : 0);
   if (s->staged_variant != variant) {

@@ -41,13 +41,11 @@ template <class S, class C> struct StepArgs {
   unsigned long long* __restrict__ fallback;  // cells that fell back to plain BGK, or null
 };
 
-// Relaxation rate of one cell: the uniform omega, or the closure's.
-// `counted`: the cell is a real fluid cell (lanes computing a discarded
-// result pass false and are not counted as fallbacks).
+// Relaxation rate of a cell under the closure record `rec`: 1 / (tau0 +
+// delta_tau) while the cell's speed stays within the drift bound of the
+// speed at prediction, the plain omega otherwise (`fell_back` set).
 template <class S, class C>
-__device__ __forceinline__ C cell_omega_rec(const StepArgs<S, C>& a, __half2 rec, C rho, C jx, C jy,
-                                            bool counted = true) {
-  if (!a.closure) return a.omega;
+__device__ __forceinline__ C closure_omega(const StepArgs<S, C>& a, __half2 rec, C rho, C jx, C jy, bool& fell_back) {
   const float2 r = __half22float2(rec);
   const float fr = (float)rho, fx = (float)jx, fy = (float)jy;
   // |u| within [lo, hi] compared as |j|^2 against rho^2 [lo^2, hi^2]: no root, no division
@@ -55,13 +53,29 @@ __device__ __forceinline__ C cell_omega_rec(const StepArgs<S, C>& a, __half2 rec
   const float lo = fmaxf(r.y - d, 0.0f), hi = r.y + d;
   const float j2 = fx * fx + fy * fy, r2 = fr * fr;
   const bool keep = j2 >= r2 * (lo * lo) && j2 <= r2 * (hi * hi) && r.x >= 0.0f && r.x <= 1.0f;
+  fell_back = !keep;
+  // __frcp_rn is the correctly rounded reciprocal: the same value as 1.0f / x
+  return keep ? (C)__frcp_rn(a.tau0 + r.x) : a.omega;
+}
+
+// Relaxation rate of one cell: the uniform omega, or the closure's, with the
+// fallback counted at once (the per-cell kernels; the staged kernel sums its
+// fallbacks per warp and adds them once per tile).  `counted`: the cell is a
+// real fluid cell (lanes computing a discarded result pass false and are not
+// counted as fallbacks).
+template <class S, class C>
+__device__ __forceinline__ C cell_omega_rec(const StepArgs<S, C>& a, __half2 rec, C rho, C jx, C jy,
+                                            bool counted = true) {
+  if (!a.closure) return a.omega;
+  bool fell_back;
+  const C w = closure_omega(a, rec, rho, jx, jy, fell_back);
+  const bool keep = !fell_back;
   if (a.fallback) {
     const unsigned am = __activemask();
     const unsigned fb = __ballot_sync(am, !keep && counted);
     if (fb && (threadIdx.x & 31) == __ffs(am) - 1) atomicAdd(a.fallback, (unsigned long long)__popc(fb));
   }
-  // __frcp_rn is the correctly rounded reciprocal: the same value as 1.0f / x
-  return keep ? (C)__frcp_rn(a.tau0 + r.x) : a.omega;
+  return w;
 }
 
 template <class S, class C>

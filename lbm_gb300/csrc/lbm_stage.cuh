@@ -12,8 +12,8 @@
 // shared memory, not registers.
 //
 // Stage r holds row r of the 8 moving planes of src (with a 16-byte halo on
-// each side for the x-1 / x+1 pulls), row r of the rest plane and row r of
-// the mask.  Output row y reads stages y-1, y, y+1: pulled populations, the
+// each side for the x-1 / x+1 pulls), row r of the rest plane, row r of the
+// mask and, with the learned closure, row r of the closure records.  Output row y reads stages y-1, y, y+1: pulled populations, the
 // bounce-back partner (the cell's own opposite population, stage y) and the
 // solid bits.  In channel mode the stage rows wrap (periodic top/bottom), the
 // outflow column pulls its own column, and the inlet column and solid cells
@@ -154,6 +154,12 @@ __device__ __forceinline__ void load_pair(const __nv_bfloat16*, uint32_t w, floa
   hi = __uint_as_float(w & 0xFFFF0000u);
 }
 
+// Bytes of one ring stage: the planes, rest and mask of StageGeom, then, with
+// the closure (CL), the row's closure records (one binary16 pair per cell).
+template <class S, int W, bool CL> constexpr uint32_t stage_bytes() {
+  return StageGeom<S, W>::kBytes + (CL ? (uint32_t)W * 4u : 0u);
+}
+
 // Threads per CTA: W / CPT consumers (CPT cells each) + one producer warp.
 template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / CPT + 32; }
 
@@ -173,6 +179,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
                 "two cells per thread: channel mode only; four: channel mode, 16-bit storage");
   using C = typename St::C;
   using G = StageGeom<S, W>;
+  constexpr uint32_t kStage = stage_bytes<S, W, CL>();
   constexpr int kConsumers = W / CPT;
   constexpr int kConsumerWarps = kConsumers / 32;
   const Layout& L = a.L;
@@ -199,7 +206,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     const int w = min(W, L.nx - xb);
     const uint32_t seg_bytes = ((uint32_t)((w + 2 * G::kHalo) * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
-    const uint32_t stage_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes;
+    const uint32_t rec_bytes = CL ? ((uint32_t)(w * 4) + 15u) & ~15u : 0u;
+    const uint32_t copy_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes + rec_bytes;
     int r = r_first, s = 0;
     uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
     bool ok = true;
@@ -211,16 +219,17 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       int rr = r;
       if (EDGE == EDGE_CHANNEL) rr = rr < 0 ? rr + L.ny : (rr >= L.ny ? rr - L.ny : rr);
       else rr = min(max(rr, 0), L.ny - 1);
-      unsigned char* st = smem + (size_t)s * G::kBytes;
+      unsigned char* st = smem + (size_t)s * kStage;
       const uint32_t bar = smem_addr(&full[s]);
       const long long row = (long long)rr * L.pitch + xb;
       if (elect_one()) {
-        mbar_arrive_expect_tx(bar, stage_bytes);
+        mbar_arrive_expect_tx(bar, copy_bytes);
 #pragma unroll
         for (int p = 0; p < 8; p++)
           bulk_g2s(smem_addr(st + p * G::kSegBytes), a.srcp[p] + row - G::kHalo, seg_bytes, bar);
         bulk_g2s(smem_addr(st + 8 * G::kSegBytes), a.rest + row, rest_bytes, bar);
         bulk_g2s(smem_addr(st + G::kMaskOff), a.mask + (long long)rr * L.mw + (xb >> 5) - 4, G::kMaskBytes, bar);
+        if constexpr (CL) bulk_g2s(smem_addr(st + G::kBytes), a.closure + row, rec_bytes, bar);
       }
       __syncwarp();
       if (++s == NS) { s = 0; empty_parity ^= 1u; }
@@ -249,7 +258,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   uint32_t wm = 0, w0 = 0;
   if (ok) {
     wm = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + G::kMaskOff), k, b);
-    w0 = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_0 * G::kBytes + G::kMaskOff), k, b);
+    w0 = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_0 * kStage + G::kMaskOff), k, b);
   }
   // column classes; the channel inlet (x = 0) is inert, the channel outflow
   // (x = nx-1) pulls its x+1 populations from its own column
@@ -268,27 +277,20 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   // finite exactly when they all were (inf - inf and NaN stay NaN), so one
   // add per cell replaces a per-cell test
   C rho_sum = C(0);
+  uint32_t fallbacks = 0;  // closure cells of this thread that took the plain omega
   uint32_t own = (uint32_t)y0 * (uint32_t)L.pitch + (uint32_t)x0;
-  // closure records (global memory) are loaded one row ahead, so their
-  // latency overlaps the stage wait and the previous row's arithmetic
-  __half2 rec[CPT], rec_next[CPT];
-  if constexpr (CL) {
-#pragma unroll
-    for (int j = 0; j < CPT; j++) rec_next[j] = a.closure[own + j];
-  }
   const typename St::Om om = St::omega_consts(a.omega);
   for (int y = y0; y < y1 && ok; y++, own += (uint32_t)L.pitch) {
+    if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
+    const unsigned char* sm = smem + (size_t)slot_m * kStage;
+    const unsigned char* s0 = smem + (size_t)slot_0 * kStage;
+    const unsigned char* sp = smem + (size_t)slot_p * kStage;
+    // closure records of row y, staged with the populations
+    __half2 rec[CPT];
     if constexpr (CL) {
 #pragma unroll
-      for (int j = 0; j < CPT; j++) {
-        rec[j] = rec_next[j];
-        if (y + 1 < y1) rec_next[j] = a.closure[own + L.pitch + j];
-      }
+      for (int j = 0; j < CPT; j++) rec[j] = reinterpret_cast<const __half2*>(s0 + G::kBytes)[CPT * tid + j];
     }
-    if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
-    const unsigned char* sm = smem + (size_t)slot_m * G::kBytes;
-    const unsigned char* s0 = smem + (size_t)slot_0 * G::kBytes;
-    const unsigned char* sp = smem + (size_t)slot_p * G::kBytes;
     const uint32_t wp = winN<CPT>(reinterpret_cast<const uint32_t*>(sp + G::kMaskOff), k, b);
     const bool yin = EDGE == EDGE_CHANNEL || (y >= 1 && y <= L.ny - 2);
     // a warp with no solid bit near any of its cells skips the bounce-back
@@ -404,8 +406,14 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         m_rho[j] = rho;
         m_jx[j] = jx;
         m_jy[j] = jy;
-        if constexpr (CL) St::collide(g, rho, aux, jx, jy, cell_omega_rec(a, rec[j], rho, jx, jy, act[j]));
-        else St::collide(g, rho, aux, jx, jy, om);
+        if constexpr (CL) {
+          bool fell_back;
+          const C w = closure_omega(a, rec[j], rho, jx, jy, fell_back);
+          fallbacks += (fell_back && act[j]) ? 1u : 0u;
+          St::collide(g, rho, aux, jx, jy, w);
+        } else {
+          St::collide(g, rho, aux, jx, jy, om);
+        }
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
       }
@@ -488,6 +496,10 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   }
   if (!(rho_sum - rho_sum == C(0))) atomicOr(a.flag, 1);
   if (!ok) atomicOr(a.flag, 2);
+  if constexpr (CL) {  // one counter update per warp and tile: the counter is a single word
+    const uint32_t warp_fallbacks = __reduce_add_sync(0xffffffffu, fallbacks);
+    if (a.fallback && lane == 0 && warp_fallbacks) atomicAdd(a.fallback, (unsigned long long)warp_fallbacks);
+  }
 }
 
 // The staged step over one lattice: CTA (bx, by) takes strip bx and row band by.
