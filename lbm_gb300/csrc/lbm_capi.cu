@@ -274,7 +274,7 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
 // column strips, for channel mode with 16-bit storage; elsewhere those
 // variants run the widest that exists).  With the
 // closure on, one ring depth per cells-per-thread count runs (4 stages for one
-// or four cells, 6 for two).
+// or four cells, 6 for two; 5 for two with 512-column strips).
 template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int C2 = EDGE == EDGE_CHANNEL ? 2 : 1;
   constexpr int C4 = EDGE == EDGE_CHANNEL && sizeof(typename St::S) == 2 ? 4 : C2;
@@ -282,6 +282,9 @@ template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename
     if (a.closure) {
       if (s->kernel >= 2 && s->kernel <= 5) return launch_staged<St, EDGE, 4, 1, true>(s, a);
       if (s->kernel == 9 || s->kernel == 10) return launch_staged<St, EDGE, 4, C4, true>(s, a);
+      if constexpr (sizeof(typename St::S) == 2) {
+        if (s->kernel == 11 || s->kernel == 12) return launch_staged<St, EDGE, 5, 2, true, 2 * kStageW>(s, a);
+      }
       return launch_staged<St, EDGE, 6, C2, true>(s, a);
     }
   }

@@ -167,7 +167,7 @@ def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda, kernel):
 
 
 @pytest.mark.parametrize("storage", [0, 1, 2])
-@pytest.mark.parametrize("kernel", [0, 1, 3, 8, 9])
+@pytest.mark.parametrize("kernel", [0, 1, 3, 8, 9, 11])
 def test_gpu_closure_step_equals_plain_step_at_the_same_omega(lbm, torch_cuda, storage, kernel):
     """All-zero weights give z = bias = 0, delta_tau = DT_MAX / 2 = 0.125
     exactly, so every fluid cell relaxes with 1 / (1 / omega + 0.125): that
