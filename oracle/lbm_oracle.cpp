@@ -627,5 +627,9 @@ uint16_t orc_float_to_half(float f) { return float_to_half_rn(f); }
 float orc_half_to_float(uint16_t h) { return half_to_float(h); }
 uint16_t orc_float_to_bf16(float f) { return float_to_bf16_rn(f); }
 double orc_noise_u01(uint64_t seed, uint64_t cell, int comp) { return noise_u01(seed, cell, comp); }
+// The 16-bit collision's reciprocal, for n values (tests of its accuracy).
+void orc_recip_newton(const float* x, float* out, int n) {
+  for (int i = 0; i < n; i++) out[i] = recip_newton(x[i]);
+}
 
 }  // extern "C"

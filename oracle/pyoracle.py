@@ -75,6 +75,7 @@ def lib():
         L.orc_half_to_float.argtypes = [ctypes.c_uint16]
         L.orc_float_to_bf16.restype = ctypes.c_uint16
         L.orc_float_to_bf16.argtypes = [ctypes.c_float]
+        L.orc_recip_newton.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]
         L.orc_noise_u01.restype = ctypes.c_double
         L.orc_noise_u01.argtypes = [ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int]
         _lib = L
