@@ -55,7 +55,7 @@ __device__ __forceinline__ void moments_dev(const float g[9], float& rho, float&
 // this constant, found by a search over [1, 2)), then three Newton steps
 // r' = r + r (1 - x r), each squaring the relative error, with fused
 // multiply-adds: within one ulp of 1 / x, and equal to the correctly rounded
-// value for 99.99 % of x.  Every step is an IEEE operation or an integer
+// value for about 99.98 % of x.  Every step is an IEEE operation or an integer
 // subtraction, so a CPU restatement reproduces it bit for bit.  Non-finite
 // x gives a non-finite result.
 __device__ __forceinline__ float recip_newton(float x) {
