@@ -1,16 +1,15 @@
 // Learned closure inference on the 5th-generation tensor cores: the whole
-// network per 16 x 16 tile in shared memory, the four layers as implicit
-// GEMMs issued with tcgen05.mma (BF16 operands from shared memory, f32
-// accumulators in tensor memory); the 1-channel output layer has its weights
-// padded to 16 outputs.
+// network per 16 x 16 tile in shared memory, the three 32-channel layers as
+// implicit GEMMs issued with tcgen05.mma (BF16 operands from shared memory,
+// f32 accumulators in tensor memory) and the 1-channel output layer on the
+// CUDA cores (one output per thread).
 //
 // GEMM shapes per tile (M = window pixels, N = 32 output channels):
 //   layer 1  M = 22 rows x 24 (the feature window's pitch), 5 blocks of 128,
 //            K = 3 kernel rows x 16;
 //   layer 2  M = 20 rows x 22 (the input window's pitch), K = 9 x 32;
-//   layer 3  M = 18 rows x 20, K = 9 x 32;
-//   layer 4  M = 16 rows x 18, K = 9 x 32, N = 16 (one real output).
-// For layers 2 to 4 the A operand of tap (ky, kx) is the input activation
+//   layer 3  M = 18 rows x 20, K = 9 x 32.
+// For layers 2 and 3 the A operand of tap (ky, kx) is the input activation
 // buffer itself viewed from row offset ky * pitch + kx: output pixel q =
 // oy * pitch + ox reads input pixel q + ky * pitch + kx, so each tap is one
 // shared-memory descriptor with a shifted start address (the columns per
@@ -67,7 +66,8 @@ constexpr uint32_t kOffX1 = kOffP, kOffX3 = kOffP, kOffF = kOffQ, kOffX2 = kOffQ
 constexpr uint32_t kOffW1 = kOffQ + 4u * kRX2 * 16u;            // [6][32][8] bf16
 constexpr uint32_t kOffW2 = kOffW1 + 6u * 32u * 16u;            // [36][32][8] bf16
 constexpr uint32_t kOffW3 = kOffW2 + 36u * 32u * 16u;           // [36][32][8] bf16
-constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // [36][16][8] bf16: layer 4 padded to 16 outputs
+constexpr uint32_t kOffW4 = kOffW3 + 36u * 32u * 16u;           // [36][16][8] bf16: layer 4, output 0 of 16 (the
+                                                                // operand layout of an N = 16 GEMM; read on the CUDA cores)
 constexpr uint32_t kOffBias = kOffW4 + 36u * 16u * 16u;         // f32 b1 b2 b3 (32 each), b4
 constexpr uint32_t kPackedBytes = kOffBias + 400u - kOffW1;     // 97 floats, padded to 16 B
 constexpr uint32_t kOffBar = kOffW1 + kPackedBytes;             // mbarrier (8 B), tensor-memory address (4 B)
@@ -403,20 +403,34 @@ __global__ void __launch_bounds__(256, 2)
     }
     sync_async();
 
-    // ---- layer 4 (32 -> 1, padded to N = 16) -> record ----------------------------------------
-    if (tid == 0) {
-      issue_layer<kB4, 9, 2, kRX3, kW3, 16>(tmem, base + kOffX3, base + kOffW4);
-      commit(bar);
-    }
-    wait_layer();
-    for (int mb = warp >> 2; mb < kB4; mb += 2) {
-      float v[32];
-      tmem_ld32(tmem + lane_base + (uint32_t)(mb * 32), v);
-      const int q = mb * 128 + 32 * (warp & 3) + lane;
-      const int oy = q / kW3, ox = q % kW3, gx = tx0 + ox, gy = ty0 + oy;
-      if (q < kM4 && ox < kT && gx < L.nx && gy < L.ny) {
+    // ---- layer 4 (32 -> 1) on the CUDA cores -> record -------------------------------------------
+    // One output per thread: 9 taps x 32 channels of X3 (pitch 18), four
+    // 16-byte rows per tap, against the layer's weights (output 0 of the
+    // packed [36][16][8] block, read by every thread at once: a broadcast).
+    // An N = 16 MMA for this one channel would stream 16 x more A operand
+    // from shared memory than the useful work needs.
+    {
+      const int oy = tid / kT, ox = tid % kT, gx = tx0 + ox, gy = ty0 + oy;
+      const unsigned char* x3 = sm + kOffX3;
+      const unsigned char* w4 = sm + kOffW4;
+      float z = bias[96];
+#pragma unroll
+      for (int t = 0; t < 9; t++) {
+        const int row = (oy + t / 3) * kW3 + ox + t % 3;
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+          const uint4 xv = *reinterpret_cast<const uint4*>(x3 + ((size_t)c * kRX3 + row) * 16);
+          const uint4 wv = *reinterpret_cast<const uint4*>(w4 + (size_t)((t * 4 + c) * 16) * 16);
+          const uint32_t xs[4] = {xv.x, xv.y, xv.z, xv.w}, ws[4] = {wv.x, wv.y, wv.z, wv.w};
+#pragma unroll
+          for (int i = 0; i < 4; i++) {  // bf16 -> f32 is exact: the high 16 bits
+            z = __fmaf_rn(__uint_as_float(xs[i] << 16), __uint_as_float(ws[i] << 16), z);
+            z = __fmaf_rn(__uint_as_float(xs[i] & 0xFFFF0000u), __uint_as_float(ws[i] & 0xFFFF0000u), z);
+          }
+        }
+      }
+      if (gx < L.nx && gy < L.ny) {
         const long long o = (long long)gy * L.pitch + gx;
-        const float z = v[0] + bias[96];
         const float dt = dt_max / (1.0f + expf(-z));
         // |u| of the cell (solid cells: 0), from its moments
         const bool solid = (mask[(long long)gy * L.mw + (gx >> 5)] >> (gx & 31)) & 1u;
