@@ -397,11 +397,7 @@ __global__ void __launch_bounds__(256, 2)
         store_row(sm + kOffX3, kRX3, oy * kW3 + ox, v);
       }
     }
-    for (int i = tid; i < 4 * (kRX3 - kW3 * kW3); i += blockDim.x) {
-      const int c = i / (kRX3 - kW3 * kW3), r = kW3 * kW3 + i % (kRX3 - kW3 * kW3);
-      *reinterpret_cast<uint4*>(sm + kOffX3 + ((size_t)c * kRX3 + r) * 16) = make_uint4(0u, 0u, 0u, 0u);
-    }
-    sync_async();
+    sync_async();  // (the output layer reads only the 18 x 18 window: no tail rows to clear)
 
     // ---- layer 4 (32 -> 1) on the CUDA cores -> record -------------------------------------------
     // One output per thread: 9 taps x 32 channels of X3 (pitch 18), four
