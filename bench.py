@@ -277,7 +277,7 @@ def time_closure(lbm, refresh=20, seed=1):
     for the closure and for plain coarse BGK."""
     import numpy as np
     from lbm_gb300 import closure as cl
-    path = os.path.join(HERE, "lbm_gb300", "models", "closure_2048x1024_f4.npz")
+    path = os.path.join(HERE, "lbm_gb300", "closure_weights", "closure_2048x1024_f4.npz")
     params = np.load(path)["params"]
     nx, ny, F, tau, u, steps = 2048, 1024, 4, 0.52, 0.06, 8000
     tau_c = cl.coarse_tau(tau, F)
