@@ -1,0 +1,16 @@
+"""bench.py's command line (CPU only): the flags the driver passes and the
+ones the profile summaries use all parse; nothing is run."""
+import subprocess
+import sys
+
+from conftest import ROOT
+
+
+def test_bench_flags():
+    out = subprocess.run([sys.executable, "bench.py", "--help"], cwd=ROOT, capture_output=True, text=True,
+                         timeout=300)
+    assert out.returncode == 0, out.stderr
+    for flag in ("--gpus", "--steps", "--warmup", "--impl", "--no-batched", "--no-closure", "--no-precision",
+                 "--no-variants", "--no-cpu-baseline", "--kernel-only", "--case", "--precision-steps",
+                 "--batched-steps", "--cpu-seconds"):
+        assert flag in out.stdout, flag
