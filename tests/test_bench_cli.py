@@ -1,5 +1,6 @@
-"""bench.py's command line (CPU only): the flags the driver passes and the
-ones the profile summaries use all parse; nothing is run."""
+"""bench.py's command line (CPU only): the run-length and implementation
+flags, the section switches and the small profiling cases all parse; nothing
+is run."""
 import subprocess
 import sys
 
