@@ -1,7 +1,7 @@
 // CPU oracle for the D2Q9 collide + stream step.  TEST INFRASTRUCTURE ONLY:
 // tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
-// arm load this library as the checker.  The product library never links,
-// loads or calls it.
+// arm load this library, to check results against it or to time the CPU
+// baseline.  The product library never links, loads or calls it.
 //
 // Parity status: the reference (PPLUSCHT/LBM, crate lbm-wgpu) ships no tests,
 // golden vectors or fixtures for this path.  This restatement is pinned
