@@ -1,4 +1,4 @@
-"""ctypes wrappers around the CPU checkers.  TEST INFRASTRUCTURE ONLY.
+"""ctypes wrappers around the CPU oracles.  TEST INFRASTRUCTURE ONLY.
 
 `Oracle` wraps liboracle.so (the C++ restatement, lbm_oracle.cpp) and `RefShaders`
 wraps _ref/libref.so (the reference's WGSL translated by wgsl2cpp.py and driven

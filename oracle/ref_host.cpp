@@ -1,6 +1,6 @@
 // Host driver for the reference's own WGSL shaders, translated to C++ by
 // oracle/wgsl2cpp.py into oracle/_ref/ref_shaders.inc.  TEST INFRASTRUCTURE
-// ONLY (checker and CPU baseline); the product library never loads it.
+// ONLY (result checks and the CPU baseline); the product library never loads it.
 //
 // It restates the engine side of lbm-wgpu/src/lbm.rs that binds buffers and
 // dispatches the shaders; the per-cell arithmetic is the reference's WGSL:
