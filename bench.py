@@ -8,12 +8,16 @@ inlet.  Synthetic geometry from a fixed seed; no dataset is involved.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A step is one fused launch over the whole grid.  `value` times K steps with the
-state resident in HBM (CUDA events on the engine's stream).  `e2e` runs the
-same K steps through the public API with host buffers: populations and mask
-uploaded from pinned host memory, K steps, rho / ux / uy read back, all inside
-the timed region.  The grid (570 MB in f32) is larger than L2, so no flush is
-needed between steps.  With --gpus N > 1 (torchrun) every rank advances its own
-replica of the grid: weak scaling, no collective on the data path.
+state resident in HBM (CUDA events on the engine's stream): the K-step call is
+first made untimed (so the CUDA graph it replays is captured and instantiated
+outside the timing), then repeated, each call bracketed by synchronisation and
+its own events, until at least --min-seconds have passed; the median call is
+reported.  `e2e` runs the same K steps through the public API with host
+buffers: populations and mask uploaded from pinned host memory, K steps, rho /
+ux / uy read back, all inside the timed region, repeated and reported the same
+way.  The grid (570 MB in f32) is larger than L2, so no flush is needed between
+steps.  With --gpus N > 1 (torchrun) every rank advances its own replica of the
+grid: weak scaling, no collective on the data path.
 
 --impl reference times the reference's own step arithmetic on the host cores:
 its WGSL shaders translated to C++ (oracle/_ref) when built, else the oracle
@@ -70,7 +74,7 @@ class ClockSampler:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -107,6 +111,44 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def repeat_timed(call, stream, min_seconds, world, dist, max_calls=5000):
+    """Median device time (ms) of one `call()`: each call is bracketed by a
+    barrier (N > 1) and a device synchronisation on both sides and timed with
+    CUDA events on `stream`; calls repeat until `min_seconds` of wall time have
+    passed (at least 3).  The number of calls is agreed over ranks and each
+    call's time is the maximum over ranks.  Returns (median_ms, calls, wall_s)."""
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def once():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        call()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    t0 = time.perf_counter()
+    first = once()
+    per = max(time.perf_counter() - t0, 1e-6)
+    calls = int(min(max_calls, max(3, -(-min_seconds // per))))
+    if world > 1:
+        t = torch.tensor([calls], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        calls = int(t.item())
+    t0 = time.perf_counter()
+    ms = [once() for _ in range(calls)]
+    wall = time.perf_counter() - t0
+    del first
+    if world > 1:
+        t = torch.tensor(ms, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = t.tolist()
+    return statistics.median(ms), calls, wall
 
 
 def dist_env():
@@ -337,6 +379,9 @@ def run_ours(args):
                           "frac": round(gbs / hbm_peak, 4), "launches": launches}))
         return
 
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
     # --- value: K steps with the state resident, f32 ---------------------------
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
     stream = torch.cuda.Stream()  # the engine's kernels and the timing events share this stream
@@ -345,29 +390,21 @@ def run_ours(args):
     lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
     lat.draw_mask(mask)
     lat.iterate(args.warmup)
+    # the timed call itself, untimed, at both buffer parities: lbm_step captures
+    # and instantiates the CUDA graph it replays for a call of this length here
+    lat.iterate(args.steps)
+    lat.iterate(args.steps)
     lat.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     l0 = lat.launch_count()
-    if world > 1:
-        dist.barrier()
-    torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        t0 = time.perf_counter()
-        e0.record(stream)
-        lat.iterate(args.steps)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
+        dev_ms, calls, wall = repeat_timed(lambda: lat.iterate(args.steps), stream, args.min_seconds, world, dist)
     lat.synchronize()
-    launches = lat.launch_count() - l0
-    dev_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([dev_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        dev_ms = float(t.item())
+    launches = (lat.launch_count() - l0) // (calls + 1)
     ms_step = dev_ms / args.steps
     mlups = world * n * args.steps / (dev_ms * 1e-3) / 1e6
-    kernel_ms = ms_step  # one launch per step
+    # one launch per step, replayed from a graph: the per-step device time is
+    # the launch's duration plus the graph's gap between launches
+    kernel_ms = ms_step
     achieved = BYTES_PER_CELL["f32"] * active / (kernel_ms * 1e-3) / 1e9
     lat.close()
 
@@ -384,28 +421,46 @@ def run_ours(args):
     lat.set_inlet_velocity(UX)
     L = lbm.load_library()
     import ctypes
+    lstream = torch.cuda.ExternalStream(lat.get_stream())
+    marks = [torch.cuda.Event(enable_timing=True) for _ in range(5)]
 
     def e2e_once(k):
+        marks[0].record(lstream)
         lbm._check(L.lbm_write_populations(lat.handle, ctypes.c_void_p(pops_h.data_ptr())))
+        marks[1].record(lstream)
         lbm._check(L.lbm_set_mask(lat.handle, ctypes.c_void_p(mask_h.data_ptr())))
+        marks[2].record(lstream)
         lbm._check(L.lbm_step(lat.handle, k))
+        marks[3].record(lstream)
         for o, f in zip(outs, (0, 3, 4)):  # rho, ux, uy
             lbm._check(L.lbm_read_field(lat.handle, f, ctypes.c_void_p(o.data_ptr())))
+        marks[4].record(lstream)
 
+    # the timed call, untimed first (captures the graph its K steps replay)
     e2e_once(max(args.warmup, 1))
-    if world > 1:
-        dist.barrier()
-    t0 = time.perf_counter()
     e2e_once(args.steps)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_once(args.steps)
+    lat.synchronize()
+    phases = []
+
+    def e2e_timed():
+        e2e_once(args.steps)
+        torch.cuda.synchronize()
+        phases.append([marks[i].elapsed_time(marks[i + 1]) for i in range(4)])
+
+    e2e_ms, e2e_calls, _ = repeat_timed(e2e_timed, lstream, args.min_seconds, world, dist, max_calls=400)
     lat.close()
-    e2e_mlups = world * n * args.steps / e2e_s / 1e6
-    h2d = (9 * n * 4 + n) / args.steps
-    d2h = 3 * n * 4 / args.steps
+    e2e_mlups = world * n * args.steps / (e2e_ms * 1e-3) / 1e6
+    pops_bytes, mask_bytes, out_bytes = 9 * n * 4, n, 3 * n * 4
+    h2d = (pops_bytes + mask_bytes) / args.steps
+    d2h = out_bytes / args.steps
+    ph = [statistics.median(p[i] for p in phases) for i in range(4)]
+    link = host_link(torch, pops_bytes)
+    e2e_phases = {"write_populations_ms": round(ph[0], 4), "set_mask_ms": round(ph[1], 4),
+                  "steps_ms": round(ph[2], 4), "read_fields_ms": round(ph[3], 4),
+                  "h2d_gbs": round((pops_bytes + mask_bytes) / ((ph[0] + ph[1]) * 1e-3) / 1e9, 1),
+                  "d2h_gbs": round(out_bytes / (ph[3] * 1e-3) / 1e9, 1),
+                  "host_link_h2d_gbs": link[0], "host_link_d2h_gbs": link[1], "calls": e2e_calls}
 
     # --- storage variants (same workload) -----------------------------------------
     variants = {}
@@ -448,8 +503,9 @@ def run_ours(args):
                    "storage": "f32", "l2": "state 570 MB > 129 MB L2: no flush",
                    "parallelism": "replicas x%d" % world},
         "e2e": {"value": round(e2e_mlups, 1), "unit": "MLUPS", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h),
-                "what": "write_populations + set_mask from pinned host, K steps, read rho/ux/uy to pinned host"},
+                "d2h_bytes_per_step": int(d2h), "ms_per_call": round(e2e_ms, 4), "phases": e2e_phases,
+                "what": "write_populations + set_mask from pinned host, K steps, read rho/ux/uy to pinned host; "
+                        "median of repeated calls"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                      "frac": round(achieved / hbm_peak, 4), "traffic": ncu_traffic("k_step_ws_f32_channel"),
                      "peak_source": peak_kind, "bytes_per_cell": BYTES_PER_CELL["f32"],
@@ -462,6 +518,8 @@ def run_ours(args):
         "closure": closure_res,
         "precision": precision,
         "gpu_launches": int(launches),
+        "timing": {"calls": calls, "per_call": "median", "min_seconds": args.min_seconds,
+                   "graph": "the K-step call replays a captured graph, instantiated before timing"},
         "clocks": clocks.summary(),
         "wall_s_timed": round(wall, 4),
     }
@@ -471,6 +529,27 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
         dist.destroy_process_group()
+
+
+def host_link(torch, nbytes):
+    """Pinned host <-> device copy bandwidth (GB/s) of one `nbytes` buffer,
+    the median of 5 copies each way timed with CUDA events: the link the e2e
+    copies run over."""
+    h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    out = []
+    for src, dst in ((h, d), (d, h)):
+        ms = []
+        for _ in range(6):
+            torch.cuda.synchronize()
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out.append(round(nbytes / (statistics.median(ms[1:]) * 1e-3) / 1e9, 1))
+    return out
 
 
 def cpu_baseline(mask, budget_s=12.0, threads=None):
@@ -613,6 +692,8 @@ def main():
     ap.add_argument("--precision-steps", type=int, default=20000)
     ap.add_argument("--batched-steps", type=int, default=5000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--min-seconds", type=float, default=1.0,
+                    help="repeat the timed K-step call until this much wall time has passed (median reported)")
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
                     help="time only the step kernel of one storage format (profiling runs)")
     ap.add_argument("--case", choices=["batched64", "closure2048"], default=None,

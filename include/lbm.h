@@ -113,8 +113,11 @@ int lbm_set_barrier(lbm_sim* sim, const uint32_t* idx_val_pairs, size_t npairs);
  * fluid in LBM_EDGE_CHANNEL. */
 int lbm_reset_barrier(lbm_sim* sim);
 
-/* Whole-mask upload / download: one byte per cell, nonzero = solid (the
- * reference uploads whole barrier buffers in reset_barrier, lbm.rs:1364). */
+/* Whole-mask upload / download: one byte per cell, nonzero = solid, dense
+ * nx-wide rows (the reference uploads whole barrier buffers in reset_barrier,
+ * lbm.rs:1364).  lbm_set_mask copies the bytes to the device and bit-packs
+ * them there; it returns once `mask` has been read, with the packing queued on
+ * the handle's stream. */
 int lbm_set_mask(lbm_sim* sim, const uint8_t* mask);
 int lbm_get_mask(lbm_sim* sim, uint8_t* mask);
 
@@ -180,7 +183,8 @@ int lbm_read_populations_device(lbm_sim* sim, float* device_out);
 
 /* Upload populations (9 planes, reference order) to both buffer sets, as
  * custom_speed / single_cell upload states (lbm.rs:1092-1095); the step
- * count restarts at 0. */
+ * count restarts at 0.  Returns once `in` has been read (the caller may reuse
+ * it); the conversion into the buffer sets is queued on the handle's stream. */
 int lbm_write_populations(lbm_sim* sim, const float* in);
 int lbm_write_populations_f64(lbm_sim* sim, const double* in);
 
@@ -206,7 +210,9 @@ int lbm_conservation(lbm_sim* sim, double out[3]);
  * real-time loop that cannot afford cudaMalloc's implicit synchronisation):
  * no handle, no allocation.  No counterpart in the reference.
  *   rho, jx, jy: device arrays of f32 moments, row pitch `pitch` elements;
- *   solid: device array, one byte per cell (nonzero = excluded), or NULL;
+ *   solid: device array, one byte per cell (nonzero = excluded) with the
+ *          same row pitch `pitch` (cell (x, y) at solid[y * pitch + x]), or
+ *          NULL (every cell counts);
  *   out: device pointer to 3 doubles (sum rho, sum jx, sum jy);
  *   stream: cudaStream_t as void* (NULL = the legacy default stream).
  * Its scratch is a fixed 96 KiB array in the library's device image (present
@@ -214,7 +220,10 @@ int lbm_conservation(lbm_sim* sim, double out[3]);
  * 2^28 cells; larger inputs return LBM_ERR_ARG before any device work.  All
  * calls share that array, so calls that overlap on the GPU race: serialise
  * them.  The first call on a device resolves the array's address there; make
- * it before any stream capture.  Errors are reported by lbm_last_error(). */
+ * it before any stream capture.  The address is kept per CUDA context: after
+ * cudaDeviceReset (or any other end of the device's context) the next call
+ * resolves it again, and should again come before any capture.  Errors are
+ * reported by lbm_last_error(). */
 int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy, const uint8_t* solid, uint32_t nx,
                              uint32_t ny, uint32_t pitch, double* out, void* stream);
 

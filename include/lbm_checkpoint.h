@@ -9,10 +9,10 @@
  * mask and, when the learned closure is on, its per-cell records.
  *
  * Layout (little-endian): a 96-byte header
- *   char magic[8] = "LBMGB3CK"; u32 version = 1, nx, ny; i32 edge, storage;
+ *   char magic[8] = "LBMGB3CK"; u32 version = 2, nx, ny; i32 edge, storage;
  *   f32 omega, u_in, drift; u64 steps; u32 cur, materialised, closure,
- *   elem_bytes; u64 payload_bytes; u32 crc32 (of the payload, zlib's CRC-32);
- *   u32 reserved[5]
+ *   elem_bytes; u64 payload_bytes; u32 crc32 (zlib's CRC-32 of the header
+ *   with this field zero, continued over the payload); u32 reserved[5]
  * then the payload, every plane dense row-major (nx * ny, row 0 first):
  *   mask (u8 per cell); buffer 0 (8 planes, direction slots 0..3 = nw, n, ne,
  *   w and 4..7 = e, sw, s, se); buffer 1 (8 planes); rest plane; closure
@@ -32,7 +32,10 @@ extern "C" {
 int lbm_checkpoint_size(const lbm_sim* sim, size_t* bytes);
 /* Into a caller buffer of at least lbm_checkpoint_size bytes (synchronises). */
 int lbm_checkpoint_save(lbm_sim* sim, void* buf, size_t len);
-/* From a buffer; LBM_ERR_ARG on a size / mode mismatch or a CRC error. */
+/* From a buffer; LBM_ERR_ARG, before any device work, on a size / mode
+ * mismatch, a CRC error, or a header field out of range (cur, materialised
+ * and closure must be 0 or 1; omega in (0, 2); u_in finite; drift finite and
+ * > 0). */
 int lbm_checkpoint_load(lbm_sim* sim, const void* buf, size_t len);
 /* The same through a file. */
 int lbm_checkpoint_write(lbm_sim* sim, const char* path);

@@ -7,6 +7,7 @@
 #include <vector>
 #include <algorithm>
 #include <cstdarg>
+#include <cmath>
 
 #include "../../include/lbm.h"
 #include "lbm_kernels.cuh"
@@ -99,6 +100,8 @@ struct lbm_sim {
   size_t staging_bytes = 0;
   std::vector<uint8_t> mask_h;
   std::vector<uint32_t> words_h;
+  bool mask_h_valid = true;        // mask_h mirrors mask_d (lbm_set_mask packs on the device only)
+  cudaEvent_t copied = nullptr;    // marks the end of a copy from a caller's host buffer
   cudaStream_t own_stream = nullptr, stream = nullptr;
   int cur = 0;               // buffer holding the latest state
   bool materialised = true;  // cur holds a pre-collision state
@@ -158,6 +161,36 @@ int upload_words(lbm_sim* s, uint32_t y0, uint32_t y1) {
   const size_t off = (size_t)y0 * s->L.mw, cnt = (size_t)(y1 - y0) * s->L.mw;
   CK(cudaMemcpyAsync(s->mask_d + off, s->words_h.data() + off, cnt * 4, cudaMemcpyHostToDevice, s->stream));
   CK(cudaStreamSynchronize(s->stream));  // words_h is pageable and reused
+  return LBM_OK;
+}
+
+// Rebuild the host mirror of the mask from the device words when the last
+// lbm_set_mask packed it on the device only.
+int ensure_mask_host(lbm_sim* s) {
+  if (s->mask_h_valid) return LBM_OK;
+  const int nx = s->L.nx, mw = s->L.mw;
+  CK(cudaMemcpyAsync(s->words_h.data(), s->mask_d, s->words_h.size() * 4, cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  for (int y = 0; y < s->L.ny; y++) {
+    const uint32_t* row = s->words_h.data() + (size_t)y * mw;
+    uint8_t* m = s->mask_h.data() + (size_t)y * nx;
+    for (int x = 0; x < nx; x++) m[x] = (uint8_t)((row[x >> 5] >> (x & 31)) & 1u);
+  }
+  s->mask_h_valid = true;
+  return LBM_OK;
+}
+
+// A copy from a caller's host buffer: queued on the handle's stream and
+// marked by `copied`; the caller's buffer is free once that event has passed
+// (kernels queued after the copy may still be running).
+int copy_from_host(lbm_sim* s, void* dst, const void* src, size_t bytes) {
+  CK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s->stream));
+  CK(cudaEventRecord(s->copied, s->stream));
+  return LBM_OK;
+}
+
+int wait_host_copy(lbm_sim* s) {
+  CK(cudaEventSynchronize(s->copied));
   return LBM_OK;
 }
 
@@ -234,6 +267,7 @@ void release(lbm_sim* s) {
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
   cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
+  if (s->copied) cudaEventDestroy(s->copied);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -392,10 +426,11 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   if ((rc = alloc((void**)&s->partial_d, (size_t)kReduceBlocks * 3 * 8))) return rc;
   s->staging_bytes = (size_t)9 * nx * ny * 8;
   if ((rc = alloc((void**)&s->staging_d, s->staging_bytes))) return rc;
-  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+  if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->copied, cudaEventDisableTiming) != cudaSuccess) {
     release(s);
     delete s;
-    return fail(LBM_ERR_CUDA, "cudaStreamCreate failed");
+    return fail(LBM_ERR_CUDA, "cudaStreamCreate / cudaEventCreate failed");
   }
   s->stream = s->own_stream;
   cudaDeviceGetAttribute(&s->sms, cudaDevAttrMultiProcessorCount, s->device);
@@ -461,6 +496,7 @@ int lbm_set_barrier(lbm_sim* s, const uint32_t* pairs, size_t npairs) {
   if (npairs && !pairs) return fail(LBM_ERR_ARG, "pairs is null");
   if (npairs == 0) return LBM_OK;
   int rc = materialise(s);
+  if (!rc) rc = ensure_mask_host(s);
   if (rc) return rc;
   const size_t n = s->mask_h.size();
   uint32_t ymin = UINT32_MAX, ymax = 0;
@@ -481,22 +517,35 @@ int lbm_reset_barrier(lbm_sim* s) {
   int rc = materialise(s);
   if (rc) return rc;
   default_walls(s);
+  s->mask_h_valid = true;
   pack_words(s, 0, s->L.ny);
   return upload_words(s, 0, s->L.ny);
 }
 
+// The whole mask is uploaded as bytes and bit-packed on the device; the host
+// mirror is rebuilt from the device words only when a later call needs it
+// (lbm_set_barrier, lbm_get_mask, lbm_checkpoint_save).
 int lbm_set_mask(lbm_sim* s, const uint8_t* mask) {
   CHECK_SIM(s);
   if (!mask) return fail(LBM_ERR_ARG, "mask is null");
   int rc = materialise(s);
   if (rc) return rc;
-  for (size_t i = 0; i < s->mask_h.size(); i++) s->mask_h[i] = mask[i] ? 1 : 0;
-  pack_words(s, 0, s->L.ny);
-  return upload_words(s, 0, s->L.ny);
+  const size_t cells = (size_t)s->L.nx * s->L.ny;
+  uint8_t* bytes = (uint8_t*)s->staging_d;  // 72 B per cell: room for the byte mask
+  if ((rc = copy_from_host(s, bytes, mask, cells))) return rc;
+  dim3 grid((s->L.mw + kBlockX - 1) / kBlockX, s->L.ny);
+  k_pack_mask<<<grid, kBlockX, 0, s->stream>>>(s->L, bytes, s->mask_d);
+  CK_LAUNCH();
+  s->launches++;
+  s->mask_h_valid = false;
+  return wait_host_copy(s);  // the caller may reuse `mask` once this returns
 }
 
 int lbm_get_mask(lbm_sim* s, uint8_t* mask) {
-  if (!s || !mask) return fail(LBM_ERR_ARG, "null argument");
+  CHECK_SIM(s);
+  if (!mask) return fail(LBM_ERR_ARG, "null argument");
+  int rc = ensure_mask_host(s);
+  if (rc) return rc;
   std::memcpy(mask, s->mask_h.data(), s->mask_h.size());
   return LBM_OK;
 }
@@ -803,8 +852,8 @@ int lbm_read_populations_device(lbm_sim* s, float* device_out) { return read_pop
 static int write_pops(lbm_sim* s, const void* in, bool f64) {
   CHECK_SIM(s);
   if (!in) return fail(LBM_ERR_ARG, "in is null");
-  CK(cudaMemcpyAsync(s->staging_d, in, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyHostToDevice,
-                     s->stream));
+  int rc = copy_from_host(s, s->staging_d, in, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4));
+  if (rc) return rc;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
@@ -818,10 +867,11 @@ static int write_pops(lbm_sim* s, const void* in, bool f64) {
     CK_LAUNCH();
     return LBM_OK;
   };
-  int rc = dispatch_storage(s->storage, launch);
+  rc = dispatch_storage(s->storage, launch);
   if (rc) return rc;
   s->launches++;
-  CK(cudaStreamSynchronize(s->stream));
+  rc = wait_host_copy(s);  // `in` has been read; k_write_pops runs on in stream order
+  if (rc) return rc;
   s->cur = 0;
   s->materialised = true;
   s->moments_valid = false;
@@ -1099,7 +1149,7 @@ int lbm_render(lbm_sim* s, int stat, int cmap, uint32_t width, uint32_t height, 
 namespace {
 
 constexpr char kCkMagic[8] = {'L', 'B', 'M', 'G', 'B', '3', 'C', 'K'};
-constexpr uint32_t kCkVersion = 1;
+constexpr uint32_t kCkVersion = 2;  // 2: the CRC covers the header too
 
 struct CkHeader {  // 96 bytes, little-endian, written as is
   char magic[8];
@@ -1109,7 +1159,7 @@ struct CkHeader {  // 96 bytes, little-endian, written as is
   uint64_t steps;
   uint32_t cur, materialised, closure, elem_bytes;
   uint64_t payload_bytes;
-  uint32_t crc32, reserved[5];
+  uint32_t crc32, reserved[5];  // crc32: over the header (with this field zero), then the payload
 };
 static_assert(sizeof(CkHeader) == 96, "checkpoint header layout");
 
@@ -1128,6 +1178,12 @@ uint32_t crc32_update(uint32_t crc, const uint8_t* p, size_t n) {
   crc = ~crc;
   for (size_t i = 0; i < n; i++) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
   return ~crc;
+}
+
+uint32_t ck_crc(const CkHeader& h, const uint8_t* payload) {
+  CkHeader z = h;
+  z.crc32 = 0u;
+  return crc32_update(crc32_update(0u, (const uint8_t*)&z, sizeof z), payload, h.payload_bytes);
 }
 
 size_t ck_payload_bytes(const lbm_sim* s, bool closure) {
@@ -1164,6 +1220,8 @@ int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
   const bool closure = s->closure_on && s->closure_d;
   const size_t need = sizeof(CkHeader) + ck_payload_bytes(s, closure);
   if (!buf || len < need) return fail(LBM_ERR_ARG, "checkpoint needs %zu bytes", need);
+  int rc = ensure_mask_host(s);
+  if (rc) return rc;
   const size_t cells = (size_t)s->L.nx * s->L.ny, e = s->es;
   CkHeader h{};
   std::memcpy(h.magic, kCkMagic, 8);
@@ -1184,13 +1242,13 @@ int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
   uint8_t* p = (uint8_t*)buf + sizeof(CkHeader);
   std::memcpy(p, s->mask_h.data(), cells);
   uint8_t* q = p + cells;
-  int rc = copy_planes(q, s->f[0], e, s->L, 8, true, s->stream);
+  rc = copy_planes(q, s->f[0], e, s->L, 8, true, s->stream);
   if (!rc) rc = copy_planes(q + 8 * cells * e, s->f[1], e, s->L, 8, true, s->stream);
   if (!rc) rc = copy_planes(q + 16 * cells * e, s->rest, e, s->L, 1, true, s->stream);
   if (!rc && closure) rc = copy_planes(q + 17 * cells * e, s->closure_d, sizeof(__half2), s->L, 1, true, s->stream);
   if (rc) return rc;
   CK(cudaStreamSynchronize(s->stream));
-  h.crc32 = crc32_update(0u, p, h.payload_bytes);
+  h.crc32 = ck_crc(h, p);
   std::memcpy(buf, &h, sizeof h);
   return LBM_OK;
 }
@@ -1205,18 +1263,27 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
   if ((int)h.nx != s->L.nx || (int)h.ny != s->L.ny || h.edge != s->edge || h.storage != s->storage)
     return fail(LBM_ERR_ARG, "checkpoint is %ux%u edge %d storage %d, the lattice %dx%d edge %d storage %d", h.nx, h.ny,
                 h.edge, h.storage, s->L.nx, s->L.ny, s->edge, s->storage);
+  // Every header field that steers device work is checked before any of it:
+  // `cur` selects a buffer set, so anything but 0 or 1 would index past them.
+  if (h.cur > 1u || h.materialised > 1u || h.closure > 1u)
+    return fail(LBM_ERR_ARG, "checkpoint header: cur %u, materialised %u, closure %u (each must be 0 or 1)", h.cur,
+                h.materialised, h.closure);
+  if (!(h.omega > 0.0f && h.omega < 2.0f) || !std::isfinite(h.u_in) || !(h.drift > 0.0f) || !std::isfinite(h.drift))
+    return fail(LBM_ERR_ARG, "checkpoint header: omega %g, inlet %g, drift %g out of range", (double)h.omega,
+                (double)h.u_in, (double)h.drift);
   const bool closure = h.closure != 0;
   if (h.elem_bytes != s->es || h.payload_bytes != ck_payload_bytes(s, closure) ||
       len < sizeof(CkHeader) + h.payload_bytes)
     return fail(LBM_ERR_ARG, "checkpoint size mismatch");
   const uint8_t* p = (const uint8_t*)buf + sizeof(CkHeader);
-  if (crc32_update(0u, p, h.payload_bytes) != h.crc32) return fail(LBM_ERR_ARG, "checkpoint CRC mismatch");
+  if (ck_crc(h, p) != h.crc32) return fail(LBM_ERR_ARG, "checkpoint CRC mismatch");
   if (closure && !s->closure_base) {
     int rc = lbm_closure_enable(s, h.drift);
     if (rc) return rc;
   }
   const size_t cells = (size_t)s->L.nx * s->L.ny, e = s->es;
   for (size_t i = 0; i < cells; i++) s->mask_h[i] = p[i] ? 1 : 0;
+  s->mask_h_valid = true;
   pack_words(s, 0, s->L.ny);
   int rc = upload_words(s, 0, s->L.ny);
   const uint8_t* q = p + cells;
@@ -1273,8 +1340,9 @@ static int rows_io(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, v
                    bool read) {
   CHECK_SIM(s);
   if (!host) return fail(LBM_ERR_ARG, "null buffer");
-  if (nrows == 0 || y + nrows > (uint32_t)s->L.ny || slot_mask == 0 || slot_mask > 0xFFu)
-    return fail(LBM_ERR_ARG, "rows %u..%u, slot mask 0x%x", y, y + nrows, slot_mask);
+  // y >= ny || nrows > ny - y: no sum that could wrap in 32 bits
+  if (nrows == 0 || y >= (uint32_t)s->L.ny || nrows > (uint32_t)s->L.ny - y || slot_mask == 0 || slot_mask > 0xFFu)
+    return fail(LBM_ERR_ARG, "rows %u (+%u) of %d, slot mask 0x%x", y, nrows, s->L.ny, slot_mask);
   const size_t e = s->es, row = (size_t)s->L.nx * e;
   const cudaMemcpyKind kind = read ? (on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost)
                                    : (on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice);

@@ -468,6 +468,19 @@ __global__ void k_read_pops(Layout L, const typename St::S* f, const typename St
   }
 }
 
+// Bit-packs a dense nx-wide byte mask (nonzero = solid) into the pitched mask
+// words: one thread per word, bits past column nx-1 cleared.
+static __global__ void k_pack_mask(Layout L, const uint8_t* __restrict__ bytes, uint32_t* __restrict__ words) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (w >= L.mw) return;
+  const uint8_t* row = bytes + (long long)y * L.nx;
+  const int x0 = w * 32, x1 = min(x0 + 32, L.nx);
+  uint32_t v = 0u;
+  for (int x = x0; x < x1; x++) v |= (row[x] != 0 ? 1u : 0u) << (x - x0);
+  words[(long long)y * L.mw + w] = v;
+}
+
 // Compact plane-major populations into both sets and the rest plane.
 template <class St, class I>
 __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,

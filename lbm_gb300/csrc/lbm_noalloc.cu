@@ -12,9 +12,8 @@
 // a fixed array that is part of the library's device image.
 //
 // Limits and rules, as stated in include/lbm.h:
-//   * at most kNoAllocMaxCells = 2^28 cells (kNoAllocMaxBlocks blocks of
-//     kNoAllocCellsPerBlock cells); larger inputs are rejected before any
-//     device work;
+//   * at most kNoAllocMaxCells = 2^28 cells (ny * pitch); larger inputs are
+//     rejected before any device work;
 //   * the scratch array (kNoAllocMaxBlocks * 3 doubles = 96 KiB) exists on
 //     every GPU that loads the library, until the process exits;
 //   * every call shares that array: calls that overlap on the GPU (on
@@ -22,6 +21,10 @@
 //     sums; serialise them;
 //   * the first call on a device resolves the array's device address there
 //     (cudaGetSymbolAddress); make that first call before any stream capture.
+//     The address is kept per CUDA context: after cudaDeviceReset, or any
+//     other end of the device's primary context, the next call resolves it
+//     again in the new context (and should again come before any capture).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -33,33 +36,43 @@
 namespace {
 
 constexpr int kNoAllocThreads = 256;
-constexpr long long kNoAllocCellsPerBlock = 1ll << 16;
 constexpr int kNoAllocMaxBlocks = 4096;
-constexpr long long kNoAllocMaxCells = kNoAllocCellsPerBlock * kNoAllocMaxBlocks;  // 2^28
+constexpr long long kNoAllocMaxCells = 1ll << 28;
+constexpr int kBlocksPerSM = 4;
 constexpr int kMaxDevices = 64;
 
 // Partial sums (rho, jx, jy) of each block.  Every block writes its own slot
 // before the final pass reads it, so no slot has to start at zero.
 static __device__ __align__(256) double g_noalloc_partial[kNoAllocMaxBlocks * 3];
 
-// Block b sums cells [b * kNoAllocCellsPerBlock, (b+1) * kNoAllocCellsPerBlock)
-// that are fluid (solid == null or solid[cell] == 0), in a fixed order.
+// Block b sums the fluid cells (solid == null or solid[cell] == 0) among
+// row-major cells [b * per_block, (b+1) * per_block), in a fixed order.  A
+// thread walks its cells by rows: one division at the start, then a carry.
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_noalloc_partial(const float* __restrict__ rho, const float* __restrict__ jx, const float* __restrict__ jy,
                       const uint8_t* __restrict__ solid, uint32_t nx, uint32_t ny, uint32_t pitch,
-                      double* __restrict__ partial) {
+                      long long per_block, double* __restrict__ partial) {
   __shared__ double sh[3][kNoAllocThreads];
   const long long n = (long long)nx * ny;
-  const long long c0 = (long long)blockIdx.x * kNoAllocCellsPerBlock;
-  const long long c1 = c0 + kNoAllocCellsPerBlock < n ? c0 + kNoAllocCellsPerBlock : n;
+  const long long c0 = (long long)blockIdx.x * per_block;
+  const long long c1 = c0 + per_block < n ? c0 + per_block : n;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-  for (long long c = c0 + threadIdx.x; c < c1; c += kNoAllocThreads) {
-    const long long y = c / nx, x = c - y * nx;
+  long long c = c0 + threadIdx.x;
+  long long y = c / nx, x = c - y * nx;
+  const long long dy = kNoAllocThreads / nx, dx = kNoAllocThreads % nx;
+  for (; c < c1; c += kNoAllocThreads) {
     const long long i = y * pitch + x;
-    if (solid && solid[i]) continue;
-    s0 += (double)rho[i];
-    s1 += (double)jx[i];
-    s2 += (double)jy[i];
+    if (!(solid && solid[i])) {
+      s0 += (double)rho[i];
+      s1 += (double)jx[i];
+      s2 += (double)jy[i];
+    }
+    x += dx;
+    y += dy;
+    if (x >= nx) {
+      x -= nx;
+      y++;
+    }
   }
   sh[0][threadIdx.x] = s0;
   sh[1][threadIdx.x] = s1;
@@ -92,6 +105,35 @@ __global__ void __launch_bounds__(kNoAllocThreads)
 
 std::mutex g_setup_mutex;
 double* g_partial_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxDevices] = {};  // context the address was resolved in (0: none yet)
+int g_sms[kMaxDevices] = {};
+
+// The current context's unique ID, through driver entry points the runtime
+// hands out (no link against the driver library); 0 when unavailable.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)f;
+    looked_up = true;
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != CUDA_SUCCESS || !ctx || get_id(ctx, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
 
 }  // namespace
 
@@ -119,32 +161,51 @@ int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy,
   if (nx == 0 || ny == 0 || pitch < nx) return noalloc_fail(LBM_ERR_ARG, "bad shape %ux%u (pitch %u)", nx, ny, pitch);
   if ((long long)ny * pitch > kNoAllocMaxCells)
     return noalloc_fail(LBM_ERR_ARG,
-                        "%ux%u cells (pitch %u) exceed this entry point's limit of %lld cells; its fixed scratch "
-                        "holds %d partial sums of %lld cells each",
-                        nx, ny, pitch, kNoAllocMaxCells, kNoAllocMaxBlocks, kNoAllocCellsPerBlock);
+                        "%ux%u cells (pitch %u) exceed this entry point's limit of %lld cells (ny * pitch); its "
+                        "fixed scratch holds %d partial sums",
+                        nx, ny, pitch, kNoAllocMaxCells, kNoAllocMaxBlocks);
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(LBM_ERR_ARG, "device %d beyond %d", dev, kMaxDevices);
   double* partial = nullptr;
+  int sms = 1;
   {
-    // set-up, once per device, with that device current
+    // set-up, once per device and context, with that device current
     std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_partial_addr[dev]) {
+    const unsigned long long ctx = current_context_id();
+    if (!g_partial_addr[dev] || ctx != g_ctx_id[dev]) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_partial);
       if (e != cudaSuccess)
         return noalloc_fail(LBM_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+      int m = 0;
+      e = cudaDeviceGetAttribute(&m, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess)
+        return noalloc_fail(LBM_ERR_CUDA, "cudaDeviceGetAttribute: %s", cudaGetErrorString(e));
       g_partial_addr[dev] = (double*)p;
+      g_ctx_id[dev] = ctx;
+      g_sms[dev] = m > 0 ? m : 1;
     }
     partial = g_partial_addr[dev];
+    sms = g_sms[dev];
   }
+  // a few blocks per multiprocessor (at most the scratch's partial sums),
+  // each over a whole number of 256-cell passes
   const long long n = (long long)nx * ny;
-  const int nblocks = (int)((n + kNoAllocCellsPerBlock - 1) / kNoAllocCellsPerBlock);
+  const long long want = kBlocksPerSM * (long long)sms < kNoAllocMaxBlocks ? kBlocksPerSM * (long long)sms
+                                                                           : kNoAllocMaxBlocks;
+  long long per_block = (n + want - 1) / want;
+  per_block = (per_block + kNoAllocThreads - 1) / kNoAllocThreads * kNoAllocThreads;
+  const int nblocks = (int)((n + per_block - 1) / per_block);
   cudaStream_t st = (cudaStream_t)stream;
-  k_noalloc_partial<<<nblocks, kNoAllocThreads, 0, st>>>(rho, jx, jy, solid, nx, ny, pitch, partial);
-  k_noalloc_final<<<1, kNoAllocThreads, 0, st>>>(partial, nblocks, out);
+  (void)cudaGetLastError();  // an earlier call's launch error is not this call's
+  k_noalloc_partial<<<nblocks, kNoAllocThreads, 0, st>>>(rho, jx, jy, solid, nx, ny, pitch, per_block, partial);
   e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_noalloc_final<<<1, kNoAllocThreads, 0, st>>>(partial, nblocks, out);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) return noalloc_fail(LBM_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
   return LBM_OK;
 }

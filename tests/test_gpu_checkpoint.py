@@ -82,11 +82,11 @@ def test_gpu_checkpoint_layout_and_refusals(lbm, cuda_ok):
     a.iterate(5)
     ck = a.checkpoint()
     magic, version, nx, ny, edge, storage = struct.unpack_from("<8sIIIii", ck, 0)
-    assert (magic, version, nx, ny, edge, storage) == (b"LBMGB3CK", 1, 50, 30, 1, 0)
+    assert (magic, version, nx, ny, edge, storage) == (b"LBMGB3CK", 2, 50, 30, 1, 0)
     steps, = struct.unpack_from("<Q", ck, 40)
     payload, crc = struct.unpack_from("<QI", ck, 64)
     assert steps == 5 and payload == len(ck) - 96 == 50 * 30 * (1 + 17 * 4)
-    assert crc == zlib.crc32(ck[96:]) & 0xFFFFFFFF
+    assert crc == _crc(ck)
     mask = np.frombuffer(ck[96:96 + 1500], np.uint8).reshape(30, 50)
     np.testing.assert_array_equal(mask, a.mask())
     bad = bytearray(ck)
@@ -100,5 +100,61 @@ def test_gpu_checkpoint_layout_and_refusals(lbm, cuda_ok):
         lbm.Lattice(50, 30, 1.0, 1, lbm.F16).restore(ck)
     with pytest.raises(lbm.LBMError):
         a.restore(ck[:50])
+    bad = bytearray(ck)
+    bad[84] ^= 1  # a reserved header word: the header is under the CRC too
+    with pytest.raises(lbm.LBMError):
+        a.restore(bytes(bad))
     other.close()
+    a.close()
+
+
+def _crc(ck):
+    """The header's CRC-32: over the 96-byte header with its crc32 field
+    (offset 72) zero, continued over the payload."""
+    z = bytearray(ck[:96])
+    z[72:76] = b"\0\0\0\0"
+    return zlib.crc32(bytes(ck[96:]), zlib.crc32(bytes(z))) & 0xFFFFFFFF
+
+
+def _forge(ck, fmt, offset, *values):
+    """A copy of `ck` with header fields overwritten and the CRC redone, so
+    that only the range checks can refuse it."""
+    b = bytearray(ck)
+    struct.pack_into(fmt, b, offset, *values)
+    struct.pack_into("<I", b, 72, _crc(b))
+    return bytes(b)
+
+
+@pytest.mark.parametrize("field,fmt,offset,value", [
+    ("cur", "<I", 48, 2), ("materialised", "<I", 52, 7), ("closure", "<I", 56, 2),
+    ("omega", "<f", 28, float("nan")), ("omega", "<f", 28, 2.5), ("u_in", "<f", 32, float("inf")),
+    ("drift", "<f", 36, float("nan")), ("drift", "<f", 36, -1.0)])
+def test_gpu_checkpoint_header_fields_are_range_checked(lbm, cuda_ok, field, fmt, offset, value):
+    """A header whose fields steer device work (the buffer index `cur`, the
+    flags, omega, the inlet and the drift bound) is refused with LBM_ERR_ARG
+    before anything is copied, even with a matching CRC."""
+    a = make(lbm, 40, 20, 1, lbm.F32, 3)
+    a.iterate(4)
+    ck = a.checkpoint()
+    want = a.populations()
+    with pytest.raises(lbm.LBMError) as e:
+        a.restore(_forge(ck, fmt, offset, value))
+    assert e.value.code == 1 and "checkpoint header" in str(e.value)
+    np.testing.assert_array_equal(a.populations(), want)  # the lattice is untouched
+    a.restore(_forge(ck, "<I", 80, 5))  # a reserved word: accepted once the CRC matches
+    a.close()
+
+
+def test_gpu_rows_io_refuses_ranges_that_wrap(lbm, cuda_ok):
+    """Row ranges are checked without a 32-bit sum that could wrap: y =
+    0xFFFFFFF0 with 0x20 rows is refused, not copied."""
+    import ctypes
+    L = lbm.load_library()
+    a = make(lbm, 40, 20, 1, lbm.F32, 3)
+    buf = np.zeros(3 * 40 * 0x20, np.float32)
+    p = buf.ctypes.data_as(ctypes.c_void_p)
+    for y, n in ((0xFFFFFFF0, 0x20), (20, 1), (19, 2), (0, 0), (0, 0xFFFFFFFF)):
+        assert L.lbm_rows_read(a.handle, y, n, 0x7, p, 0) == 1
+        assert L.lbm_rows_write(a.handle, y, n, 0x7, p, 0) == 1
+    assert L.lbm_rows_read(a.handle, 19, 1, 0x7, p, 0) == 0
     a.close()
