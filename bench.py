@@ -163,8 +163,10 @@ def workload_mask():
     return geometry.random_circles(NX, NY, NCIRC, 4, 32, seed=SEED, inlet_clearance=64)
 
 
-def time_storage(lbm, torch, storage, mask, steps, warmup):
-    """Device-resident MLUPS of one storage format; returns (ms_per_step, launches)."""
+def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0):
+    """Device-resident MLUPS of one storage format, timed like `value` (the
+    K-step call made untimed first, then repeated for `min_seconds`, median
+    call); returns (ms_per_step, launches per call)."""
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, storage)
     stream = torch.cuda.Stream()
     lat.set_stream(stream.cuda_stream)
@@ -172,19 +174,15 @@ def time_storage(lbm, torch, storage, mask, steps, warmup):
     lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
     lat.draw_mask(mask)
     lat.iterate(warmup)
+    lat.iterate(steps)
+    lat.iterate(steps)
     lat.synchronize()
     l0 = lat.launch_count()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    lat.iterate(steps)
-    e1.record(stream)
-    torch.cuda.synchronize()
+    ms, calls, _ = repeat_timed(lambda: lat.iterate(steps), stream, min_seconds, 1, None)
     lat.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    launches = lat.launch_count() - l0
+    launches = (lat.launch_count() - l0) // (calls + 1)
     lat.close()
-    return ms, launches
+    return ms / steps, launches
 
 
 def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
@@ -372,7 +370,7 @@ def run_ours(args):
     hbm_peak, peak_kind = peaks()
     if args.kernel_only:
         st = {"f32": lbm.F32, "f16": lbm.F16, "bf16": lbm.BF16, "f64": lbm.F64}[args.kernel_only]
-        ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup)
+        ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds)
         gbs = BYTES_PER_CELL[args.kernel_only] * active / (ms * 1e-3) / 1e9
         print(json.dumps({"kernel_only": args.kernel_only, "ms_per_step": round(ms, 5),
                           "mlups": round(n / (ms * 1e-3) / 1e6, 1), "achieved_gbs": round(gbs, 1),
@@ -466,7 +464,7 @@ def run_ours(args):
     variants = {}
     if not args.no_variants:
         for name, st in (("f16", lbm.F16), ("bf16", lbm.BF16)):
-            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup)
+            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds)
             gbs = BYTES_PER_CELL[name] * active / (vms * 1e-3) / 1e9
             variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
                               "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}

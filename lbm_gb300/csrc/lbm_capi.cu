@@ -194,6 +194,19 @@ int wait_host_copy(lbm_sim* s) {
   return LBM_OK;
 }
 
+// Device address of a caller's page-locked host buffer (cudaHostAlloc,
+// cudaHostRegister, torch's pinned memory), or null for any other memory.
+// Kernels read or write such a buffer directly over the host link, so the
+// transfer needs no staging copy in device memory and no separate pass.
+void* mapped_host(const void* p) {
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    (void)cudaGetLastError();  // not a pointer CUDA knows: ordinary host memory
+    return nullptr;
+  }
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+}
+
 void default_walls(lbm_sim* s) {
   std::fill(s->mask_h.begin(), s->mask_h.end(), 0);
   if (s->edge == EDGE_REF) {
@@ -795,7 +808,8 @@ static int read_field(lbm_sim* s, int field, float* out, bool device_out) {
     if (rc) return rc;
   }
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
-  float* tmp = device_out ? out : s->staging_d;
+  float* mapped = device_out ? nullptr : (float*)mapped_host(out);
+  float* tmp = device_out ? out : (mapped ? mapped : s->staging_d);
   if (s->storage == STORE_F64)
     k_field<double><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const double*)mom_plane(s, 0),
                                                     (const double*)mom_plane(s, 1), (const double*)mom_plane(s, 2), tmp);
@@ -805,7 +819,8 @@ static int read_field(lbm_sim* s, int field, float* out, bool device_out) {
   CK_LAUNCH();
   s->launches++;
   if (device_out) return LBM_OK;
-  CK(cudaMemcpyAsync(out, tmp, (size_t)s->L.nx * s->L.ny * 4, cudaMemcpyDeviceToHost, s->stream));
+  if (!mapped)
+    CK(cudaMemcpyAsync(out, tmp, (size_t)s->L.nx * s->L.ny * 4, cudaMemcpyDeviceToHost, s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }
@@ -822,7 +837,8 @@ static int read_pops(lbm_sim* s, void* out, bool f64, bool device_out = false) {
   int rc = materialise(s);
   if (rc) return rc;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
-  void* dst = device_out ? out : (void*)s->staging_d;
+  void* mapped = device_out ? nullptr : mapped_host(out);
+  void* dst = device_out ? out : (mapped ? mapped : (void*)s->staging_d);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
@@ -839,8 +855,9 @@ static int read_pops(lbm_sim* s, void* out, bool f64, bool device_out = false) {
   if (rc) return rc;
   s->launches++;
   if (device_out) return LBM_OK;
-  CK(cudaMemcpyAsync(out, s->staging_d, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyDeviceToHost,
-                     s->stream));
+  if (!mapped)
+    CK(cudaMemcpyAsync(out, s->staging_d, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4), cudaMemcpyDeviceToHost,
+                       s->stream));
   CK(cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }
@@ -852,25 +869,32 @@ int lbm_read_populations_device(lbm_sim* s, float* device_out) { return read_pop
 static int write_pops(lbm_sim* s, const void* in, bool f64) {
   CHECK_SIM(s);
   if (!in) return fail(LBM_ERR_ARG, "in is null");
-  int rc = copy_from_host(s, s->staging_d, in, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4));
-  if (rc) return rc;
+  // a page-locked `in` is read by the kernel itself; other memory is staged
+  const void* src = mapped_host(in);
+  int rc = LBM_OK;
+  if (!src) {
+    rc = copy_from_host(s, s->staging_d, in, (size_t)9 * s->L.nx * s->L.ny * (f64 ? 8 : 4));
+    if (rc) return rc;
+    src = s->staging_d;
+  }
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
     if (f64)
       k_write_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
-                                                                 (const double*)s->staging_d);
+                                                                 (const double*)src);
     else
       k_write_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
-                                                                (const float*)s->staging_d);
+                                                                (const float*)src);
     CK_LAUNCH();
     return LBM_OK;
   };
   rc = dispatch_storage(s->storage, launch);
   if (rc) return rc;
   s->launches++;
-  rc = wait_host_copy(s);  // `in` has been read; k_write_pops runs on in stream order
+  if (src != s->staging_d) CK(cudaEventRecord(s->copied, s->stream));  // read by the kernel itself
+  rc = wait_host_copy(s);  // `in` has been read (what follows the copy runs in stream order)
   if (rc) return rc;
   s->cur = 0;
   s->materialised = true;

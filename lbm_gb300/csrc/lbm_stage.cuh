@@ -170,9 +170,15 @@ template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / C
 // ring once the CTA has synchronised between them.  CL selects the per-cell
 // relaxation time of the learned closure (a.closure must then be set);
 // without it omega is uniform and its derived constants are computed once.
+//
+// `down` walks the rows from y1-1 to y0 instead of upwards.  Bands that
+// alternate direction meet in time: two neighbouring bands start, or end,
+// together at their shared edge, so the halo rows one of them copies are read
+// by the other at about the same moment and come from L2 rather than HBM.
+// The order of rows does not change any cell's result.
 template <class St, int EDGE, int NS, int CPT, bool CL, int W, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
-                                        uint64_t* empty) {
+                                        uint64_t* empty, bool down = false) {
   using S = typename St::S;
   static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL) ||
                     (CPT == 4 && EDGE == EDGE_CHANNEL && sizeof(S) == 2),
@@ -186,8 +192,10 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   const int tid = threadIdx.x;
   const bool producer = tid >= kConsumers;
   const int x0 = xb + CPT * tid;
-  // stage r (r_first .. r_last) lives in ring slot (r - r_first) % NS
-  const int r_first = y0 - 1, r_last = y1;
+  // the i-th staged row (i = 0 .. y1 - y0 + 1) lives in ring slot i % NS: row
+  // y0 - 1 + i upwards, y1 - i downwards
+  const int n_stage = y1 - y0 + 2;
+  const int r_first = down ? y1 : y0 - 1, r_step = down ? -1 : 1;
   if (tid == 0) {
     for (int i = 0; i < NS; i++) {
       mbar_init(smem_addr(&full[i]), 1);
@@ -208,15 +216,15 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t rec_bytes = CL ? ((uint32_t)(w * 4) + 15u) & ~15u : 0u;
     const uint32_t copy_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes + rec_bytes;
-    int r = r_first, s = 0;
+    int i = 0, s = 0;
     uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
     bool ok = true;
-    for (; r <= r_last; r++) {
-      if (r - r_first >= NS && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&empty[s]), empty_parity))) {
+    for (; i < n_stage; i++) {
+      if (i >= NS && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&empty[s]), empty_parity))) {
         ok = false;
         break;
       }
-      int rr = r;
+      int rr = r_first + r_step * i;
       if (EDGE == EDGE_CHANNEL) rr = rr < 0 ? rr + L.ny : (rr >= L.ny ? rr - L.ny : rr);
       else rr = min(max(rr, 0), L.ny - 1);
       unsigned char* st = smem + (size_t)s * kStage;
@@ -238,10 +246,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       if (!ok) atomicOr(a.flag, 2);
       // no copy may be in flight when the CTA exits: wait (bounded) for the
       // last NS stages issued
-      for (int q = max(r_first, r - NS); q < r; q++) {
-        const int i = q - r_first;
-        mbar_wait(smem_addr(&full[i % NS]), (uint32_t)((i / NS) & 1));
-      }
+      for (int q = max(0, i - NS); q < i; q++) mbar_wait(smem_addr(&full[q % NS]), (uint32_t)((q / NS) & 1));
     }
     return;
   }
@@ -251,13 +256,15 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   const int e = G::kHalo + CPT * tid;  // element index of x0 in a moving segment
   const int k = (x0 >> 5) - (xb >> 5) + 4, b = x0 & 31;
   constexpr uint32_t kWin = (1u << (CPT + 2)) - 1u;
-  // ring slots of stages y-1, y, y+1 and the phase parity of stage y+1
+  // ring slots of the three staged rows around y, in arrival order (the
+  // oldest is y-1 walking upwards, y+1 walking downwards), and the phase
+  // parity of the newest
   int slot_m = 0, slot_0 = 1 % NS, slot_p = 2 % NS;
   uint32_t parity_p = 2 / NS;
   bool ok = mbar_wait(smem_addr(&full[0]), 0) && mbar_wait(smem_addr(&full[1 % NS]), 1 / NS);
-  uint32_t wm = 0, w0 = 0;
+  uint32_t wa = 0, w0 = 0;  // mask windows of the oldest row and of row y
   if (ok) {
-    wm = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + G::kMaskOff), k, b);
+    wa = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + G::kMaskOff), k, b);
     w0 = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_0 * kStage + G::kMaskOff), k, b);
   }
   // column classes; the channel inlet (x = 0) is inert, the channel outflow
@@ -278,20 +285,26 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   // add per cell replaces a per-cell test
   C rho_sum = C(0);
   uint32_t fallbacks = 0;  // closure cells of this thread that took the plain omega
-  uint32_t own = (uint32_t)y0 * (uint32_t)L.pitch + (uint32_t)x0;
+  const int y_start = down ? y1 - 1 : y0, y_step = down ? -1 : 1;
+  uint32_t own = (uint32_t)y_start * (uint32_t)L.pitch + (uint32_t)x0;
+  const uint32_t own_step = down ? 0u - (uint32_t)L.pitch : (uint32_t)L.pitch;
   const typename St::Om om = St::omega_consts(a.omega);
-  for (int y = y0; y < y1 && ok; y++, own += (uint32_t)L.pitch) {
+  for (int y = y_start, it = y0; it < y1 && ok; it++, y += y_step, own += own_step) {
     if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
-    const unsigned char* sm = smem + (size_t)slot_m * kStage;
+    // rows y-1 (sm) and y+1 (sp) by the walking direction
+    const unsigned char* s_old = smem + (size_t)slot_m * kStage;
     const unsigned char* s0 = smem + (size_t)slot_0 * kStage;
-    const unsigned char* sp = smem + (size_t)slot_p * kStage;
+    const unsigned char* s_new = smem + (size_t)slot_p * kStage;
+    const unsigned char* sm = down ? s_new : s_old;
+    const unsigned char* sp = down ? s_old : s_new;
     // closure records of row y, staged with the populations
     __half2 rec[CPT];
     if constexpr (CL) {
 #pragma unroll
       for (int j = 0; j < CPT; j++) rec[j] = reinterpret_cast<const __half2*>(s0 + G::kBytes)[CPT * tid + j];
     }
-    const uint32_t wp = winN<CPT>(reinterpret_cast<const uint32_t*>(sp + G::kMaskOff), k, b);
+    const uint32_t wn = winN<CPT>(reinterpret_cast<const uint32_t*>(s_new + G::kMaskOff), k, b);
+    const uint32_t wm = down ? wn : wa, wp = down ? wa : wn;
     const bool yin = EDGE == EDGE_CHANNEL || (y >= 1 && y <= L.ny - 2);
     // a warp with no solid bit near any of its cells skips the bounce-back
     // pass (all 32 lanes vote, before any lane branches)
@@ -485,11 +498,11 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         step_cell<St, EDGE>(a, x0 + j, y);
       }
     }
-    // stage y-1 is no longer needed by this warp
+    // the oldest staged row is no longer needed by this warp
     __syncwarp();
     if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
-    wm = w0;
-    w0 = wp;
+    wa = w0;
+    w0 = wn;
     slot_m = slot_0;
     slot_0 = slot_p;
     if (++slot_p == NS) { slot_p = 0; parity_p ^= 1u; }
@@ -522,7 +535,9 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
           if (x0 + j < a.L.nx) step_cell<St, EDGE>(a, x0 + j, y);
     return;
   }
-  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty);
+  // odd bands walk downwards: each band edge is then crossed by its two bands
+  // at the same time (both at the start, or both at the end of the launch)
+  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty, (blockIdx.y & 1u) != 0u);
 }
 
 }  // namespace lbm
