@@ -298,6 +298,53 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     return out
 
 
+STEADY = {"nx": 1024, "ny": 512, "cx": 256, "cy": 256, "r": 24, "ux": 0.05, "tau": 0.8}
+
+
+def steady_precision(lbm, steps=20000, every=1000):
+    """Storage precision where rounding is not amplified by chaos: flow past
+    one cylinder at Reynolds number u D / nu = 0.05 * 48 / 0.1 = 24, below the
+    onset of vortex shedding (about 47), so the wake is steady and a rounding
+    difference decays instead of growing.  1024 x 512 channel, circle r = 24 at
+    (256, 256), tau 0.8, inlet ux 0.05, started from rest at the inlet
+    velocity.  Every storage runs `steps` steps; returns, per storage, the
+    relative L2 error over fluid cells against the f64 run of the final
+    velocity and of the velocity averaged over the second half (samples every
+    `every` steps)."""
+    import numpy as np
+    from lbm_gb300 import geometry
+    c = STEADY
+    mask = geometry.single_circle(c["nx"], c["ny"], c["cx"], c["cy"], c["r"])
+    fl = mask == 0
+    fl[:, 0] = False
+    res = {}
+    for name, st in (("f64", lbm.F64), ("f32", lbm.F32), ("f16", lbm.F16), ("bf16", lbm.BF16)):
+        acc, n = 0.0, 0
+        with lbm.Lattice(c["nx"], c["ny"], 1.0 / c["tau"], lbm.EDGE_CHANNEL, st) as lat:
+            lat.set_inlet_velocity(c["ux"])
+            lat.init_equilibrium(1.0, c["ux"], 0.0, 0.0, 0)
+            lat.draw_mask(mask)
+            done = 0
+            while done < steps:
+                lat.iterate(every)
+                done += every
+                u = np.stack([lat.field("ux"), lat.field("uy")]).astype(np.float64)
+                if done > steps // 2:
+                    acc = acc + u
+                    n += 1
+            res[name] = (u, acc / max(n, 1))
+
+    def rel(a, b):
+        return float(np.linalg.norm((a - b)[:, fl]) / np.linalg.norm(b[:, fl]))
+
+    out = {"workload": "steady cylinder wake (Re 24): 1024x512 channel, r 24, tau 0.8, ux 0.05, %d steps" % steps,
+           "reference": "f64 storage on the GPU"}
+    for name in ("f32", "f16", "bf16"):
+        out[name] = {"rel_err_final_velocity": _finite_or_str(rel(res[name][0], res["f64"][0]), 7),
+                     "rel_err_time_avg_velocity": _finite_or_str(rel(res[name][1], res["f64"][1]), 7)}
+    return out
+
+
 def _finite_or_str(x, ndigits=4):
     """A float for the JSON line; "non-finite" where the run diverged (strict
     JSON has no Infinity or NaN)."""
@@ -473,6 +520,7 @@ def run_ours(args):
     precision = None
     if not args.no_precision:
         precision = precision_check(lbm, torch, mask, args.precision_steps)
+        precision["steady"] = steady_precision(lbm)
 
     # --- learned closure: coarse run with the trained network vs the fine run -------
     closure_res = None

@@ -94,9 +94,9 @@ int lbm_get_stream(const lbm_sim* sim, void** cuda_stream);
  * band height); 6, 7, 8: the same with rings of 8, 6, 4 stages and two cells
  * per consumer thread (channel mode; reference mode runs one); 9, 10: rings
  * of 4, 6 stages and four cells per consumer thread, 2 consumer warps per
- * strip (channel mode with f16 / bf16 storage; otherwise as 8); 11, 12:
- * rings of 5, 6 stages, two cells per thread and 512-column strips (channel
- * mode with f16 / bf16 storage; otherwise as 7).  Defaults: 3
+ * strip (channel mode with f16 / bf16 storage; otherwise as 8); 11, 12, 13:
+ * rings of 5, 6, 7 stages, two cells per thread and 512-column strips
+ * (channel mode with f16 / bf16 storage; otherwise as 7).  Defaults: 3
  * for f32, 11 for f16 / bf16 (7 below 1024 columns), with rows_per_thread 8 for kernels 0 / 1 and a
  * band floor of 2 rows for the staged kernels; f64 storage always uses
  * kernel 0.  No counterpart in the reference, whose dispatch is fixed at

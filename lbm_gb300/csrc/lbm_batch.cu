@@ -61,8 +61,12 @@ struct DomainDev {
   float omega;
 };
 
-// One step over every tile.  Tile t = (domain, xb, y0, y1); strips are W
-// columns wide.
+// One step over every tile.  Tile t = (domain, xb | down << 30, y0, y1);
+// strips are W columns wide.  `down` (odd bands) walks the band's rows
+// downwards: the bands of a strip sit next to each other in the tile table,
+// so neighbouring bands run at the same time and, walking in opposite
+// directions, cross their shared halo rows together (one of the two reads
+// then hits L2).
 template <class St, int NS, int CPT, int W>
 __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (CPT == 1 ? 4 : 6))
     k_batch_step(const DomainDev* __restrict__ doms, const int4* __restrict__ tiles, int ntiles, int src_i, int dst_i,
@@ -83,6 +87,8 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
     const int t = ticket;
     if (t >= ntiles || stop) break;
     const int4 T = tiles[t];
+    const int xb = T.y & 0x3FFFFFFF;
+    const bool down = (T.y >> 30) != 0;
     if (threadIdx.x == 0) {
       const DomainDev& d = doms[T.x];
       sa.L = d.L;
@@ -108,13 +114,13 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
     }
     __syncthreads();
     if (materialised) {
-      const int x0 = T.y + CPT * (int)threadIdx.x;
+      const int x0 = xb + CPT * (int)threadIdx.x;
       if ((int)threadIdx.x < W / CPT)
         for (int y = T.z; y < T.w; y++)
           for (int j = 0; j < CPT; j++)
             if (x0 + j < sa.L.nx) step_cell<St, EDGE_CHANNEL>(sa, x0 + j, y);
     } else {
-      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W>(sa, T.y, T.z, T.w, smem, full, empty);
+      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W>(sa, xb, T.z, T.w, smem, full, empty, down);
       __syncthreads();  // every arrival and copy of this tile is complete
       if (threadIdx.x == 0)
         for (int i = 0; i < NS; i++) {  // the next tile initialises them again
@@ -221,13 +227,13 @@ int build_tiles(lbm_batch* b) {
     const int bands = std::max(1, (h.ny + want - 1) / want);
     const int rows = (h.ny + bands - 1) / bands;
     for (int xb = 0; xb < h.nx; xb += W)
-      for (int y0 = 0; y0 < h.ny; y0 += rows) t.push_back(make_int4(d, xb, y0, std::min(y0 + rows, h.ny)));
+      for (int y0 = 0, band = 0; y0 < h.ny; y0 += rows, band++)
+        t.push_back(make_int4(d, xb | ((band & 1) << 30), y0, std::min(y0 + rows, h.ny)));
   }
-  std::stable_sort(t.begin(), t.end(), [&](const int4& a, const int4& c) {
-    const long long wa = (long long)(a.w - a.z) * std::min(W, b->doms[a.x].nx - a.y);
-    const long long wc = (long long)(c.w - c.z) * std::min(W, b->doms[c.x].nx - c.y);
-    return wa > wc;
-  });
+  auto cells = [&](const int4& a) {
+    return (long long)(a.w - a.z) * std::min(W, b->doms[a.x].nx - (a.y & 0x3FFFFFFF));
+  };
+  std::stable_sort(t.begin(), t.end(), [&](const int4& a, const int4& c) { return cells(a) > cells(c); });
   if ((int)t.size() > b->tiles_cap) {
     cudaFree(b->d_tiles);
     b->d_tiles = nullptr;

@@ -346,9 +346,11 @@ template <class St, int EDGE> int launch_staged_ns(lbm_sim* s, StepArgs<typename
     case 10: return launch_staged<St, EDGE, 6, C4, false>(s, a);
     case 11:
     case 12:
+    case 13:
       if constexpr (EDGE == EDGE_CHANNEL && sizeof(typename St::S) == 2) {  // 512-column strips
-        return s->kernel == 11 ? launch_staged<St, EDGE, 5, 2, false, 2 * kStageW>(s, a)
-                               : launch_staged<St, EDGE, 6, 2, false, 2 * kStageW>(s, a);
+        if (s->kernel == 11) return launch_staged<St, EDGE, 5, 2, false, 2 * kStageW>(s, a);
+        if (s->kernel == 12) return launch_staged<St, EDGE, 6, 2, false, 2 * kStageW>(s, a);
+        return launch_staged<St, EDGE, 7, 2, false, 2 * kStageW>(s, a);
       }
       return launch_staged<St, EDGE, 6, C2, false>(s, a);
     default: return launch_staged<St, EDGE, 4, C2, false>(s, a);
@@ -497,7 +499,7 @@ int lbm_get_stream(const lbm_sim* s, void** stream) {
 int lbm_set_tuning(lbm_sim* s, int rows_per_thread, int kernel) {
   CHECK_SIM(s);
   if (rows_per_thread < 1 || rows_per_thread > 1024) return fail(LBM_ERR_ARG, "rows_per_thread %d", rows_per_thread);
-  if (kernel < 0 || kernel > 12) return fail(LBM_ERR_ARG, "kernel %d", kernel);
+  if (kernel < 0 || kernel > 13) return fail(LBM_ERR_ARG, "kernel %d", kernel);
   s->rows = rows_per_thread;
   s->kernel = kernel;
   s->staged_variant = -1;  // recompute the staged launch shape

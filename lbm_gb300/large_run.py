@@ -17,6 +17,13 @@ non-finite density.  The f16 runs' time-averaged velocities are compared
 with the f32 run's (relative L2 over fluid cells).  Velocity averages stay on the
 device (lbm_read_field_device); the timed region holds only steps and
 inferences.  Prints one JSON line.
+
+With --diagnose, a run that goes non-finite is repeated (the engine is
+deterministic) up to the sample before, then stepped one step at a time to
+the first step whose density is non-finite; the report gives that step, where
+the non-finite cells are (position, distance to the inlet, the outflow and the
+nearest solid cell) and the state one step earlier: the largest speed and the
+lowest density over the lattice, with their positions.
 """
 import argparse
 import ctypes
@@ -97,6 +104,81 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
     return out, (acc / max(n_avg, 1)).cpu().numpy()
 
 
+def _field(lat, lib, code, tmp):
+    _check(lib.lbm_read_field_device(lat.handle, code, ctypes.c_void_p(tmp.data_ptr())))
+    return tmp
+
+
+def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refresh=20, drift=1.0, seed=1):
+    """Where and how a run first goes non-finite (see the module docstring).
+    `first_bad` is the sample at which the step kernels' flag was first seen
+    set; the run is repeated to `first_bad - every` and then stepped singly.
+    The repeat follows run()'s schedule exactly (one step, then the closure
+    inferred before steps 1, 1 + refresh, ...), so it retraces the same
+    states bit for bit."""
+    import torch
+    from scipy import ndimage
+    lib = load_library()
+    stream = torch.cuda.Stream()
+    tmp = torch.empty((ny, nx), dtype=torch.float32, device="cuda")
+    rep = {}
+    with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
+        lat.set_stream(stream.cuda_stream)
+        lat.set_inlet_velocity(u)
+        lat.init_equilibrium(1.0, u, 0.0, 1e-4, seed)
+        lat.draw_mask(mask)
+        if params is not None:
+            p = np.ascontiguousarray(params, np.float32)
+            _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
+            _check(lib.lbm_closure_enable(lat.handle, float(drift)))
+        lat.iterate(1)  # run() takes its first step before any inference
+        done = 1
+        start = max(first_bad - every, 1)
+        fl = torch.from_numpy(mask == 0).cuda()
+
+        def advance(k):
+            nonlocal done
+            while k > 0:
+                c = min(k, refresh - (done - 1) % refresh) if params is not None else k
+                if params is not None and (done - 1) % refresh == 0:
+                    _check(lib.lbm_closure_infer(lat.handle))
+                lat.iterate(c)
+                done += c
+                k -= c
+
+        advance(start - 1)
+        prev = None
+        while done < first_bad + 1:
+            rho = _field(lat, lib, 0, tmp).clone()
+            ux = _field(lat, lib, 3, tmp).clone()
+            uy = _field(lat, lib, 4, tmp).clone()
+            bad = ~torch.isfinite(rho)
+            if bool(bad.any()):
+                break
+            sp = torch.sqrt(ux * ux + uy * uy)
+            sp = torch.where(fl & torch.isfinite(sp), sp, torch.zeros_like(sp))
+            rr = torch.where(fl, rho, torch.full_like(rho, float("inf")))
+            i_sp, i_rho = int(torch.argmax(sp)), int(torch.argmin(rr))
+            prev = {"step": done, "max_speed": float(sp.view(-1)[i_sp]), "max_speed_at": [i_sp % nx, i_sp // nx],
+                    "min_rho": float(rr.view(-1)[i_rho]), "min_rho_at": [i_rho % nx, i_rho // nx]}
+            advance(1)
+        if not bool(bad.any()):
+            return {"first_nonfinite_step": None}
+        ys, xs = np.nonzero(bad.cpu().numpy())
+        # distance to the nearest solid cell, within a window around them
+        m = 256
+        x0, x1 = max(int(xs.min()) - m, 0), min(int(xs.max()) + m + 1, nx)
+        y0, y1 = max(int(ys.min()) - m, 0), min(int(ys.max()) + m + 1, ny)
+        dist = ndimage.distance_transform_edt(mask[y0:y1, x0:x1] == 0)
+        d = dist[ys - y0, xs - x0]
+        rep = {"first_nonfinite_step": done, "cells": int(len(xs)),
+               "x_range": [int(xs.min()), int(xs.max())], "y_range": [int(ys.min()), int(ys.max())],
+               "distance_to_inlet": int(xs.min()), "distance_to_outflow": int(nx - 1 - xs.max()),
+               "distance_to_nearest_solid": [float(d.min()), float(np.median(d)), float(d.max())],
+               "state_one_step_earlier": prev}
+    return rep
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
     ap.add_argument("--size", type=int, nargs=2, default=[16384, 8192])
@@ -109,6 +191,8 @@ def main(argv=None):
     ap.add_argument("--drift", type=float, default=1.0, help="closure drift bound (multiples of the predicted |u|)")
     ap.add_argument("--closure-only", action="store_true", help="skip the plain f32 and f16 runs")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--diagnose", action="store_true",
+                    help="for each run that goes non-finite, locate the first non-finite step and cells")
     a = ap.parse_args(argv)
     nx, ny = a.size
     mask = random_circles(nx, ny, 10 ** 7, 8, 64, a.seed, inlet_clearance=64, target_fraction=0.08)
@@ -126,15 +210,23 @@ def main(argv=None):
         d = (u - u32)[:, fl]
         return float(np.linalg.norm(d) / np.linalg.norm(u32[:, fl])) if np.isfinite(d).all() else float("inf")
 
+    def diag(r, storage, params=None):
+        if a.diagnose and r["first_nonfinite_by_step"] is not None:
+            r["diagnosis"] = diagnose(nx, ny, a.tau, a.u, mask, storage, r["first_nonfinite_by_step"], a.every,
+                                      params=params, refresh=a.refresh, drift=a.drift, seed=a.seed)
+
     if not a.closure_only:
         r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed)
+        diag(r32, F32)
         r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed)
+        diag(r16, F16)
         r16["vel_err_vs_f32"] = err(u16)
         rep["runs"] = [r32, r16]
     if a.closure:
         params = np.load(a.closure)["params"]
         rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh,
                      drift=a.drift, seed=a.seed)
+        diag(rc, F16, params)
         rc["vel_err_vs_f32"] = err(uc)
         rc["refresh"], rc["drift"] = a.refresh, a.drift
         rep["runs"].append(rc)
