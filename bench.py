@@ -221,6 +221,43 @@ def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
             "nonfinite_domains": bad}
 
 
+SLAB = {"nx": 16384, "ny": 8192, "tau": 0.51, "ux": 0.05}
+
+
+def time_slab(lbm, torch, steps, warmup, min_seconds, rank=0, world=1, dist=None):
+    """The large-grid workload (16384 x 8192, circles r 8-64 at 8 % solid, tau
+    0.51, inlet ux 0.05, f32) split into `world` y-slabs, one per rank, each
+    step overlapped with its halo exchange: edge rows, exchange on a side
+    stream (NCCL between ranks; a device copy onto itself when alone),
+    interior rows, ghost rows.  Strong scaling: the whole grid is fixed.
+    Returns the whole-job MLUPS and ms per step (median call of `steps`
+    steps, max over ranks)."""
+    from lbm_gb300.geometry import random_circles
+    from lbm_gb300.slab import DistExchanger, SlabLattice
+    c = SLAB
+    mask = random_circles(c["nx"], c["ny"], 10 ** 7, 8, 64, 1, inlet_clearance=64, target_fraction=0.08)
+    s = SlabLattice(c["nx"], c["ny"], 1.0 / c["tau"], rank, world, storage=lbm.F32, u_in=c["ux"])
+    stream = torch.cuda.Stream()
+    s.lat.set_stream(stream.cuda_stream)
+    s.lat.init_equilibrium(1.0, c["ux"], 0.0, 1e-4, SEED + rank)
+    s.set_mask(mask)
+    s.attach(DistExchanger(s, device=True))
+    s.step(max(warmup, 3))
+    ms, calls, _ = repeat_timed(lambda: s.step(steps), stream, min_seconds, world, dist)
+    try:
+        s.lat.synchronize()
+        finite = True
+    except lbm.LBMError:
+        finite = False  # plain BGK at tau 0.51 diverges on this grid; the timing does not depend on it
+    s.lat.close()
+    n = c["nx"] * c["ny"]
+    return {"workload": "%dx%d channel, circles r 8-64 at 8%% solid, tau %.2f, ux %.2f, f32, %d y-slab(s), "
+                        "halo exchange overlapped with the interior rows" % (c["nx"], c["ny"], c["tau"], c["ux"],
+                                                                            world),
+            "mlups": round(n * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 5),
+            "launches_per_step": 3, "calls": calls, "scaling": "strong", "finite": finite}
+
+
 def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     """Storage precision on the 4096 x 2048 workload: the same seeded run in
     f64 (the GPU's FP64 run is the reference), f32, f16 (f - w) and bf16
@@ -400,6 +437,7 @@ def run_ours(args):
     from lbm_gb300 import build as B
 
     rank, world, local = dist_env()
+    dist = None
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -415,6 +453,19 @@ def run_ours(args):
     # inert (never read or written by the step), so they carry no algorithmic bytes
     active = int((mask[:, 1:] == 0).sum())
     hbm_peak, peak_kind = peaks()
+    if args.slab:
+        r = time_slab(lbm, torch, args.steps, args.warmup, args.min_seconds, rank, world, dist)
+        if rank == 0:
+            print(json.dumps({
+                "metric": METRIC, "value": r["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded circles)",
+                "config": {"workload": r["workload"], "parallelism": "y-slabs x%d" % world},
+                "gpu_launches": 3 * args.steps, "slab": r}), flush=True)
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
     if args.kernel_only:
         st = {"f32": lbm.F32, "f16": lbm.F16, "bf16": lbm.BF16, "f64": lbm.F64}[args.kernel_only]
         ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds)
@@ -424,9 +475,6 @@ def run_ours(args):
                           "frac": round(gbs / hbm_peak, 4), "launches": launches}))
         return
 
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
     # --- value: K steps with the state resident, f32 ---------------------------
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, lbm.F32)
     stream = torch.cuda.Stream()  # the engine's kernels and the timing events share this stream
@@ -507,6 +555,11 @@ def run_ours(args):
                   "d2h_gbs": round(out_bytes / (ph[3] * 1e-3) / 1e9, 1),
                   "host_link_h2d_gbs": link[0], "host_link_d2h_gbs": link[1], "calls": e2e_calls}
 
+    # --- the large grid split into y-slabs (one here), exchange overlapped ------------
+    slab = None
+    if not args.no_slab:
+        slab = time_slab(lbm, torch, args.steps, args.warmup, min(args.min_seconds, 0.5))
+
     # --- storage variants (same workload) -----------------------------------------
     variants = {}
     if not args.no_variants:
@@ -563,6 +616,7 @@ def run_ours(args):
         "batched": batched,
         "closure": closure_res,
         "precision": precision,
+        "slab": slab,
         "gpu_launches": int(launches),
         "timing": {"calls": calls, "per_call": "median", "min_seconds": args.min_seconds,
                    "graph": "the K-step call replays a captured graph, instantiated before timing"},
@@ -735,6 +789,9 @@ def main():
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-closure", action="store_true")
     ap.add_argument("--no-precision", action="store_true")
+    ap.add_argument("--no-slab", action="store_true")
+    ap.add_argument("--slab", action="store_true",
+                    help="time only the y-slab decomposition of the 16384x8192 grid across the ranks (strong scaling)")
     ap.add_argument("--precision-steps", type=int, default=20000)
     ap.add_argument("--batched-steps", type=int, default=5000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)

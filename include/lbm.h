@@ -150,6 +150,22 @@ int lbm_single_cell(lbm_sim* sim, int direction);
  * collision (the reference's density_bg after iterate). Asynchronous. */
 int lbm_step(lbm_sim* sim, uint32_t n);
 
+/* One step taken in row ranges, for a lattice split into y-slabs: a call
+ * computes rows [y0, y1) of the next step (same results as lbm_step), and
+ * the call with LBM_ROWS_COMPLETE in `flags` completes it (the step count and
+ * buffer parity advance then).  A slab computes its edge rows first, starts
+ * sending them, and overlaps that with its interior rows.  Until the step is
+ * complete, lbm_rows_read / lbm_rows_write address the rows being written,
+ * and only they, further lbm_step_rows calls, lbm_set_stream and
+ * lbm_synchronize are accepted (others return LBM_ERR_STATE).  Rows that no
+ * call of the step covers keep stale values.  LBM_ROWS_MOMENTS: these rows
+ * also write their moments; read_field then reflects the step only if every
+ * call of it asked for them.  Plain launches, no graphs.  No counterpart in
+ * the reference (one lattice per adapter, driver.rs:14-40). */
+#define LBM_ROWS_COMPLETE 1
+#define LBM_ROWS_MOMENTS 2
+int lbm_step_rows(lbm_sim* sim, uint32_t y0, uint32_t y1, int flags);
+
 /* lbm_step replays CUDA graphs captured on first use: a call of 2 to 64
  * steps is captured whole and replayed by later calls of the same length;
  * longer calls replay runs of 16 steps (per buffer parity, recaptured when

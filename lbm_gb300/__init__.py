@@ -77,6 +77,7 @@ _SIGS = [
                                             ctypes.c_uint64]),
     ("lbm_single_cell", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_step", ctypes.c_int, [_P, ctypes.c_uint32]),
+    ("lbm_step_rows", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]),
     ("lbm_set_graphs", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_synchronize", ctypes.c_int, [_P]),
     ("lbm_read_field", ctypes.c_int, [_P, ctypes.c_int, _P]),
@@ -271,6 +272,10 @@ class Lattice:
     def iterate(self, n):
         _check(_lib.lbm_step(self._h, int(n)))
 
+    def step_rows(self, y0, y1, complete=False, moments=False):
+        """Rows [y0, y1) of the next step (lbm_step_rows); `complete` ends the step."""
+        _check(_lib.lbm_step_rows(self._h, int(y0), int(y1), (1 if complete else 0) | (2 if moments else 0)))
+
     def synchronize(self):
         _check(_lib.lbm_synchronize(self._h))
 
@@ -356,6 +361,15 @@ class Lattice:
         out = np.zeros((len(slots), nrows, self.x), self.storage_dtype)
         _check(_lib.lbm_rows_read(self._h, int(y), int(nrows), mask, _ptr(out), 0))
         return out
+
+    def read_rows_device(self, y, nrows, slots, ptr):
+        """The same rows into device memory at `ptr` (an integer address),
+        queued on the lattice's stream."""
+        _check(_lib.lbm_rows_read(self._h, int(y), int(nrows), sum(1 << s for s in slots), ctypes.c_void_p(ptr), 1))
+
+    def write_rows_device(self, y, nrows, slots, ptr):
+        """Rows from device memory at `ptr`, queued on the lattice's stream."""
+        _check(_lib.lbm_rows_write(self._h, int(y), int(nrows), sum(1 << s for s in slots), ctypes.c_void_p(ptr), 1))
 
     def write_rows(self, y, slots, words):
         mask = sum(1 << s for s in slots)

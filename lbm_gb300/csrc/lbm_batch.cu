@@ -103,6 +103,8 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
       sa.omega = (C)d.omega;
       sa.materialised = materialised;
       sa.rows = T.w - T.z;
+      sa.row0 = 0;
+      sa.row_end = d.L.ny;
       C* mom = (C*)d.mom;
       sa.rho_out = write_moments ? mom : nullptr;
       sa.jx_out = write_moments ? mom + d.L.ps : nullptr;

@@ -110,7 +110,11 @@ struct lbm_sim {
   int rows = 0;    // rows per thread / band floor; 0: 8 for the per-cell kernels, 2 for the staged ones
   int kernel = 2;  // step kernel variant (lbm_set_tuning)
   int sms = 0;     // multiprocessors of the device
-  int staged_variant = -1, staged_bands = 0, staged_rows = 0;  // cached launch shape
+  int staged_variant = -1, staged_bands = 0, staged_rows = 0, staged_occ = 1;  // cached launch shape
+  // a step taken in row ranges (lbm_step_rows): the buffer it writes until
+  // the call that completes it, and whether every call wrote moments
+  int pending = -1;
+  bool pending_moments = true;
   // learned closure (include/lbm_cnn.h)
   void* closure_base = nullptr;          // padded allocation of the per-cell records
   __half2* closure_d = nullptr;          // (delta_tau, |u| at prediction) per cell, pitch layout
@@ -260,14 +264,25 @@ int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64
   return LBM_OK;
 }
 
-int check_sim(const lbm_sim* s) {
+int check_sim(const lbm_sim* s, bool pending_ok) {
   if (!s) return fail(LBM_ERR_ARG, "null handle");
+  if (!pending_ok && s->pending >= 0)
+    return fail(LBM_ERR_STATE, "a step taken in row ranges is not complete (lbm_step_rows)");
   return LBM_OK;
 }
 
+// Entry points that touch the state: refused while a step taken in row
+// ranges is incomplete.  CHECK_SIM_ANY: the calls allowed in between
+// (further row ranges, halo rows, stream and synchronisation).
 #define CHECK_SIM(s)                      \
   do {                                    \
-    int rc_ = check_sim(s);               \
+    int rc_ = check_sim(s, false);        \
+    if (rc_) return rc_;                  \
+    CK(cudaSetDevice((s)->device));       \
+  } while (0)
+#define CHECK_SIM_ANY(s)                  \
+  do {                                    \
+    int rc_ = check_sim(s, true);         \
     if (rc_) return rc_;                  \
     CK(cudaSetDevice((s)->device));       \
   } while (0)
@@ -284,8 +299,20 @@ void release(lbm_sim* s) {
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
-// Staged step launch: one strip of kStageW columns per grid column, row bands
-// sized so that all CTAs are resident at once (one wave, equal work).
+// Rows per band for `span` rows of W-column strips: as many bands as fit in
+// ONE wave (rounding up would leave a second, nearly empty wave, e.g. 64
+// strips x 10 bands = 640 CTAs for 608 slots, which cost 22 % at 16384
+// columns), and at least the tuning value's rows per band (short bands
+// re-read their two halo rows too often).
+int band_rows(const lbm_sim* s, int occ, int W, int span) {
+  const int strips = (s->L.nx + W - 1) / W;
+  const int bands = std::max(1, std::min((occ * s->sms) / strips, span));
+  return std::max((span + bands - 1) / bands, std::min(s->rows > 0 ? s->rows : 2, span));
+}
+
+// Staged step launch over rows [a.row0, a.row_end): one strip of W columns
+// per grid column, row bands sized so that all CTAs are resident at once
+// (one wave, equal work).  The whole lattice's shape is cached.
 template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
 int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int TPB = stage_threads<CPT, W>();
@@ -297,20 +324,19 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     int occ = 0;
     CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem));
     if (occ < 1) return fail(LBM_ERR_CUDA, "staged step kernel does not fit on a multiprocessor");
-    const int strips = (s->L.nx + W - 1) / W;
-    // as many bands as fit in ONE wave: rounding up would leave a second,
-    // nearly empty wave (e.g. 64 strips x 10 bands = 640 CTAs for 608
-    // slots), which cost 22 % at 16384 columns
-    int bands = (occ * s->sms) / strips;
-    bands = std::max(1, std::min(bands, s->L.ny));
-    // at least `rows` rows per band (the tuning value): short bands re-read
-    // their two halo rows too often
-    s->staged_rows = std::max((s->L.ny + bands - 1) / bands, std::min(s->rows > 0 ? s->rows : 2, s->L.ny));
+    s->staged_occ = occ;
+    s->staged_rows = band_rows(s, occ, W, s->L.ny);
     s->staged_bands = (s->L.ny + s->staged_rows - 1) / s->staged_rows;
     s->staged_variant = variant;
   }
-  a.rows = s->staged_rows;
-  dim3 grid((s->L.nx + W - 1) / W, s->staged_bands);
+  const int span = a.row_end - a.row0;
+  int rows = s->staged_rows, bands = s->staged_bands;
+  if (span != s->L.ny) {
+    rows = band_rows(s, s->staged_occ, W, span);
+    bands = (span + rows - 1) / rows;
+  }
+  a.rows = rows;
+  dim3 grid((s->L.nx + W - 1) / W, bands);
   kern<<<grid, TPB, smem, s->stream>>>(a);
   CK_LAUNCH();
   return LBM_OK;
@@ -485,7 +511,7 @@ int lbm_get_info(const lbm_sim* s, uint32_t* nx, uint32_t* ny, int* edge, int* s
 }
 
 int lbm_set_stream(lbm_sim* s, void* stream) {
-  CHECK_SIM(s);
+  CHECK_SIM_ANY(s);
   s->stream = (cudaStream_t)stream;  // NULL is CUDA's legacy default stream
   return LBM_OK;
 }
@@ -626,15 +652,16 @@ int lbm_single_cell(lbm_sim* s, int dir) {
   return launch_init(s, 1.0, 0.0, 0.0, 0.0, 0, dir, x + y * X);
 }
 
-// One step launch on the handle's stream; `last` writes the moments.
-static int launch_step(lbm_sim* s, bool last) {
+// One step launch over rows [row0, row_end) on the handle's stream, reading
+// buffer cur and writing buffer `dst`; `last` writes the moments.  The
+// caller updates the state.
+static int launch_rows(lbm_sim* s, bool last, int row0, int row_end, int dst) {
   const int rows = s->rows > 0 ? s->rows : 8;
   // f64 always runs the per-cell kernel: the pipelined and staged variants
   // would spill its doubled register footprint.
   const int variant = s->storage == STORE_F64 ? 0 : s->kernel;
-  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, (s->L.ny + rows - 1) / rows);
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, (row_end - row0 + rows - 1) / rows);
   const int src = s->cur;
-  const int dst = s->materialised ? s->cur : 1 - s->cur;
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
@@ -652,6 +679,8 @@ static int launch_step(lbm_sim* s, bool last) {
     a.omega = (C)s->omega;
     a.materialised = s->materialised ? 1 : 0;
     a.rows = rows;
+    a.row0 = row0;
+    a.row_end = row_end;
     a.rho_out = last ? (C*)mom_plane(s, 0) : nullptr;
     a.jx_out = last ? (C*)mom_plane(s, 1) : nullptr;
     a.jy_out = last ? (C*)mom_plane(s, 2) : nullptr;
@@ -675,6 +704,14 @@ static int launch_step(lbm_sim* s, bool last) {
   int rc = dispatch_storage(s->storage, launch);
   if (rc) return rc;
   s->launches++;
+  return LBM_OK;
+}
+
+// One whole step on the handle's stream; `last` writes the moments.
+static int launch_step(lbm_sim* s, bool last) {
+  const int dst = s->materialised ? s->cur : 1 - s->cur;
+  int rc = launch_rows(s, last, 0, s->L.ny, dst);
+  if (rc) return rc;
   s->cur = dst;
   s->materialised = false;
   s->steps++;
@@ -781,6 +818,28 @@ int lbm_step(lbm_sim* s, uint32_t n) {
   return LBM_OK;
 }
 
+int lbm_step_rows(lbm_sim* s, uint32_t y0, uint32_t y1, int flags) {
+  CHECK_SIM_ANY(s);
+  if (y0 >= y1 || y1 > (uint32_t)s->L.ny || (flags & ~(LBM_ROWS_COMPLETE | LBM_ROWS_MOMENTS)))
+    return fail(LBM_ERR_ARG, "rows %u..%u of %d, flags 0x%x", y0, y1, s->L.ny, flags);
+  if (s->pending < 0) {
+    s->pending = s->materialised ? s->cur : 1 - s->cur;
+    s->pending_moments = true;
+  }
+  const bool moments = (flags & LBM_ROWS_MOMENTS) != 0;
+  int rc = launch_rows(s, moments, (int)y0, (int)y1, s->pending);
+  if (rc) return rc;
+  s->pending_moments = s->pending_moments && moments;
+  if (flags & LBM_ROWS_COMPLETE) {
+    s->cur = s->pending;
+    s->pending = -1;
+    s->materialised = false;
+    s->steps++;
+    s->moments_valid = s->pending_moments;
+  }
+  return LBM_OK;
+}
+
 int lbm_set_graphs(lbm_sim* s, int enable) {
   CHECK_SIM(s);
   s->use_graphs = enable != 0;
@@ -789,7 +848,7 @@ int lbm_set_graphs(lbm_sim* s, int enable) {
 }
 
 int lbm_synchronize(lbm_sim* s) {
-  CHECK_SIM(s);
+  CHECK_SIM_ANY(s);
   CK(cudaStreamSynchronize(s->stream));
   int flag = 0;
   CK(cudaMemcpy(&flag, s->flag_d, 4, cudaMemcpyDeviceToHost));
@@ -1364,7 +1423,7 @@ int lbm_checkpoint_read(lbm_sim* s, const char* path) {
 
 static int rows_io(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, void* host, bool on_device,
                    bool read) {
-  CHECK_SIM(s);
+  CHECK_SIM_ANY(s);
   if (!host) return fail(LBM_ERR_ARG, "null buffer");
   // y >= ny || nrows > ny - y: no sum that could wrap in 32 bits
   if (nrows == 0 || y >= (uint32_t)s->L.ny || nrows > (uint32_t)s->L.ny - y || slot_mask == 0 || slot_mask > 0xFFu)
@@ -1375,7 +1434,9 @@ static int rows_io(lbm_sim* s, uint32_t y, uint32_t nrows, uint32_t slot_mask, v
   char* buf = (char*)host;
   for (int slot = 0; slot < 8; slot++) {
     if (!((slot_mask >> slot) & 1u)) continue;
-    char* dev = (char*)s->f[s->cur] + ((size_t)slot * s->L.ps + (size_t)y * s->L.pitch) * e;
+    // while a step taken in row ranges is incomplete: the buffer it writes
+    char* dev = (char*)s->f[s->pending >= 0 ? s->pending : s->cur] +
+                ((size_t)slot * s->L.ps + (size_t)y * s->L.pitch) * e;
     cudaError_t r = read ? cudaMemcpy2DAsync(buf, row, dev, (size_t)s->L.pitch * e, row, nrows, kind, s->stream)
                          : cudaMemcpy2DAsync(dev, (size_t)s->L.pitch * e, buf, row, row, nrows, kind, s->stream);
     if (r != cudaSuccess) return fail(LBM_ERR_CUDA, "row copy: %s", cudaGetErrorString(r));

@@ -27,7 +27,8 @@ template <class S, class C> struct StepArgs {
   const uint32_t* __restrict__ mask;
   C omega;
   int materialised;  // 1: dst holds S_k, collide in place without pulling
-  int rows;          // rows per thread
+  int rows;          // rows per thread (per CTA band for the staged kernels)
+  int row0, row_end; // the launch covers rows [row0, row_end): the whole lattice, or part of one step
   C* __restrict__ rho_out;    // moments of this step's collision, or null
   C* __restrict__ jx_out;
   C* __restrict__ jy_out;
@@ -203,8 +204,8 @@ template <class St, int EDGE>
 __global__ void __launch_bounds__(128) k_step(StepArgs<typename St::S, typename St::C> a) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= a.L.nx) return;
-  const int y0 = blockIdx.y * a.rows;
-  const int y1 = min(y0 + a.rows, a.L.ny);
+  const int y0 = a.row0 + blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, a.row_end);
   for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);
 }
 
@@ -296,8 +297,8 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
   const Layout& L = a.L;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   if (x >= L.nx) return;
-  const int y0 = blockIdx.y * a.rows;
-  const int y1 = min(y0 + a.rows, L.ny);
+  const int y0 = a.row0 + blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, a.row_end);
   if (y0 >= y1) return;
   if (a.materialised) {  // uniform: collide in place, per cell
     for (int y = y0; y < y1; y++) step_cell<St, EDGE>(a, x, y);

@@ -524,8 +524,8 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
   __shared__ __align__(8) uint64_t full[NS];
   __shared__ __align__(8) uint64_t empty[NS];
   const int xb = blockIdx.x * W;
-  const int y0 = blockIdx.y * a.rows;
-  const int y1 = min(y0 + a.rows, a.L.ny);
+  const int y0 = a.row0 + blockIdx.y * a.rows;
+  const int y1 = min(y0 + a.rows, a.row_end);
   if (y0 >= y1) return;  // uniform per CTA
   if (a.materialised) {  // uniform: collide in place, per cell, from global memory
     const int x0 = xb + CPT * threadIdx.x;

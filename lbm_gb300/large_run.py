@@ -79,9 +79,10 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
                 except LBMError:
                     first_bad = done
             if done > steps // 2:
-                for i, f in enumerate((3, 4)):  # ux, uy of the last step's moments
-                    _check(lib.lbm_read_field_device(lat.handle, f, ctypes.c_void_p(tmp.data_ptr())))
-                    acc[i] += tmp
+                with torch.cuda.stream(stream):  # ordered after the reads queued on the lattice's stream
+                    for i, f in enumerate((3, 4)):  # ux, uy of the last step's moments
+                        _check(lib.lbm_read_field_device(lat.handle, f, ctypes.c_void_p(tmp.data_ptr())))
+                        acc[i] += tmp
                 n_avg += 1
         torch.cuda.synchronize()
         try:
@@ -149,15 +150,16 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
         advance(start - 1)
         prev = None
         while done < first_bad + 1:
-            rho = _field(lat, lib, 0, tmp).clone()
-            ux = _field(lat, lib, 3, tmp).clone()
-            uy = _field(lat, lib, 4, tmp).clone()
-            bad = ~torch.isfinite(rho)
+            with torch.cuda.stream(stream):  # the reads are queued on the lattice's stream
+                rho = _field(lat, lib, 0, tmp).clone()
+                ux = _field(lat, lib, 3, tmp).clone()
+                uy = _field(lat, lib, 4, tmp).clone()
+                bad = ~torch.isfinite(rho)
+                sp = torch.sqrt(ux * ux + uy * uy)
+                sp = torch.where(fl & torch.isfinite(sp), sp, torch.zeros_like(sp))
+                rr = torch.where(fl, rho, torch.full_like(rho, float("inf")))
             if bool(bad.any()):
                 break
-            sp = torch.sqrt(ux * ux + uy * uy)
-            sp = torch.where(fl & torch.isfinite(sp), sp, torch.zeros_like(sp))
-            rr = torch.where(fl, rho, torch.full_like(rho, float("inf")))
             i_sp, i_rho = int(torch.argmax(sp)), int(torch.argmin(rr))
             prev = {"step": done, "max_speed": float(sp.view(-1)[i_sp]), "max_speed_at": [i_sp % nx, i_sp // nx],
                     "min_rho": float(rr.view(-1)[i_rho]), "min_rho_at": [i_rho % nx, i_rho // nx]}

@@ -37,16 +37,35 @@ class NumpyLattice:
         rho = self.P.sum(0)
         return {"rho": rho, "jx": np.tensordot(CX, self.P, 1)}[name]
 
+    def _rows_target(self):
+        return self.pending if getattr(self, "pending", None) is not None else self.P
+
     def read_rows(self, y, n, slots):
-        return np.stack([self.P[SLOTS[s], y:y + n] for s in slots])
+        return np.stack([self._rows_target()[SLOTS[s], y:y + n] for s in slots])
 
     def write_rows(self, y, slots, words):
         for k, s in enumerate(slots):
-            self.P[SLOTS[s], y:y + words.shape[1]] = words[k]
+            self._rows_target()[SLOTS[s], y:y + words.shape[1]] = words[k]
 
     def iterate(self, n):
         for _ in range(n):
             self._step()
+
+    def step_rows(self, y0, y1, complete=False, moments=False):
+        """Rows [y0, y1) of the next step into a pending state that reads and
+        writes of rows address until `complete` (the engine's lbm_step_rows);
+        rows no call covers keep the previous values."""
+        if getattr(self, "pending", None) is None:
+            self.pending = self.P.copy()
+            self.pending_mat = self.materialised
+        keep, mat = self.P, self.materialised
+        self.materialised = self.pending_mat
+        self._step()
+        self.pending[:, y0:y1] = self.P[:, y0:y1]
+        self.P, self.materialised = keep, mat
+        if complete:
+            self.P, self.pending = self.pending, None
+            self.materialised = False
 
     def _step(self):
         P, m = self.P, self.mask.astype(bool)

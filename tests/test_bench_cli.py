@@ -13,5 +13,5 @@ def test_bench_flags():
     assert out.returncode == 0, out.stderr
     for flag in ("--gpus", "--steps", "--warmup", "--impl", "--no-batched", "--no-closure", "--no-precision",
                  "--no-variants", "--no-cpu-baseline", "--kernel-only", "--case", "--precision-steps",
-                 "--batched-steps", "--cpu-seconds"):
+                 "--batched-steps", "--cpu-seconds", "--min-seconds", "--slab", "--no-slab"):
         assert flag in out.stdout, flag

@@ -36,7 +36,7 @@ def _worker(rank, world, port, nx, ny, steps, out_dir, mode):
     slab = SlabLattice(nx, ny, 1.0 / 0.6, rank, world, make_lattice=lambda x, y: NumpyLattice(x, y, 1.0 / 0.6))
     slab.set_mask(mask)
     slab.write_populations(pops)
-    slab.attach(DistExchanger(slab, timeout_s=2.0))
+    slab.attach(DistExchanger(slab, timeout_s=2.0, overlap=mode == "overlap"))
     if mode == "silent" and rank == 1:
         import time
         time.sleep(6.0)  # never exchanges
@@ -58,10 +58,12 @@ def _spawn(world, nx, ny, steps, out_dir, mode="run"):
                        join=True, start_method="spawn")
 
 
-@pytest.mark.parametrize("world", [2])
-def test_two_gloo_ranks_match_the_undivided_lattice(tmp_path, world):
-    nx, ny, steps = 24, 16, 9
-    _spawn(world, nx, ny, steps, tmp_path)
+@pytest.mark.parametrize("world,mode", [(2, "run"), (2, "overlap"), (3, "overlap")])
+def test_gloo_ranks_match_the_undivided_lattice(tmp_path, world, mode):
+    """Whole-lattice steps then the exchange ("run"), and the overlapped
+    schedule: edge rows, exchange, interior rows, ghost rows ("overlap")."""
+    nx, ny, steps = 24, 18, 9
+    _spawn(world, nx, ny, steps, tmp_path, mode)
     pops, mask = state(nx, ny, 3)
     ref = NumpyLattice(nx, ny, 1.0 / 0.6)
     ref.draw_mask(mask)
@@ -77,13 +79,14 @@ def test_a_silent_rank_times_out_the_exchange(tmp_path):
     assert err, "rank 0 should report the failed exchange"
 
 
-def test_local_exchanger_three_slabs_match():
+@pytest.mark.parametrize("overlap", [False, True])
+def test_local_exchanger_three_slabs_match(overlap):
     from lbm_gb300.slab import LocalExchanger, SlabLattice, run_local
     nx, ny = 20, 12
     pops, mask = state(nx, ny, 5)
     slabs = [SlabLattice(nx, ny, 1.0 / 0.7, r, 3, make_lattice=lambda x, y: NumpyLattice(x, y, 1.0 / 0.7))
              for r in range(3)]
-    ex = LocalExchanger(slabs)
+    ex = LocalExchanger(slabs, overlap=overlap)
     for s in slabs:
         s.set_mask(mask)
         s.write_populations(pops)
