@@ -158,6 +158,7 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
                 sp = torch.sqrt(ux * ux + uy * uy)
                 sp = torch.where(fl & torch.isfinite(sp), sp, torch.zeros_like(sp))
                 rr = torch.where(fl, rho, torch.full_like(rho, float("inf")))
+            torch.cuda.synchronize()  # everything above ran on the lattice's stream
             if bool(bad.any()):
                 break
             i_sp, i_rho = int(torch.argmax(sp)), int(torch.argmin(rr))

@@ -24,11 +24,18 @@ _c_f32p = ctypes.POINTER(ctypes.c_float)
 _c_f64p = ctypes.POINTER(ctypes.c_double)
 
 
+# Where the reference tree is read from when its shaders are translated:
+# LBM_REFERENCE_ROOT, else the build container's copy.  Without either, an
+# earlier translation (_ref/ref_shaders.inc) is compiled as it is.
+REFERENCE_ROOT = os.environ.get("LBM_REFERENCE_ROOT") or "/root/reference"
+
+
 def build(ref=True):
     """Compile liboracle.so and, when possible, the translated reference."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
     if ref:
-        r = subprocess.run(["make", "-s", "-C", HERE, "ref"], capture_output=True, text=True)
+        root = REFERENCE_ROOT if os.path.isdir(REFERENCE_ROOT) else ""
+        r = subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_ROOT=" + root], capture_output=True, text=True)
         return r.returncode == 0
     return os.path.exists(REF_SO)
 
