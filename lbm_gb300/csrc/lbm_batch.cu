@@ -59,6 +59,7 @@ struct DomainDev {
   uint32_t* mask;
   void* mom;  // rho, jx, jy planes
   float omega;
+  StoreRef ref;  // reference state of 16-bit storage (the domain's inlet velocity and omega)
 };
 
 // One step over every tile.  Tile t = (domain, xb | down << 30, y0, y1);
@@ -101,6 +102,7 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
       sa.rest = (S*)d.rest;
       sa.mask = d.mask;
       sa.omega = (C)d.omega;
+      sa.ref = d.ref;
       sa.materialised = materialised;
       sa.rows = T.w - T.z;
       sa.row0 = 0;
@@ -332,12 +334,13 @@ int materialise_all(lbm_batch* b) {
   if (b->materialised) return LBM_OK;
   const int dst = 1 - b->cur;
   auto go = [&](auto tag) -> int {
-    using S = typename decltype(tag)::S;
+    using St = decltype(tag);
+    using S = typename St::S;
     for (const DomainHost& h : b->doms) {
       dim3 grid((h.nx + kBlock - 1) / kBlock, h.ny);
-      k_materialise<S, EDGE_CHANNEL><<<grid, kBlock, 0, b->stream>>>(
+      k_materialise<St, EDGE_CHANNEL><<<grid, kBlock, 0, b->stream>>>(
           h.L, (const S*)(b->arena + h.off_f[b->cur]), (S*)(b->arena + h.off_f[dst]),
-          (const uint32_t*)(b->arena + h.off_mask));
+          (const uint32_t*)(b->arena + h.off_mask), make_store_ref(h.u_in, h.omega));
     }
     BCK(cudaGetLastError());
     return LBM_OK;
@@ -455,6 +458,7 @@ int lbm_batch_create(uint32_t count, const uint32_t* nx, const uint32_t* ny, con
     dd[d].mask = (uint32_t*)(b->arena + h.off_mask);
     dd[d].mom = b->arena + h.off_mom;
     dd[d].omega = h.omega;
+    dd[d].ref = make_store_ref(h.u_in, h.omega);
   }
   cudaMemcpyAsync(b->d_doms, dd.data(), count * sizeof(DomainDev), cudaMemcpyHostToDevice, b->stream);
   if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cleanup(LBM_ERR_CUDA, "setup", e);
@@ -513,7 +517,8 @@ int lbm_batch_init_equilibrium(lbm_batch* b, float noise_amp, uint64_t seed) {
       dim3 grid((h.nx + kBlock - 1) / kBlock, h.ny);
       k_init<St><<<grid, kBlock, 0, b->stream>>>(h.L, (S*)(b->arena + h.off_f[0]), (S*)(b->arena + h.off_f[1]),
                                                   (S*)(b->arena + h.off_rest), 1.0f, h.u_in, 0.0f, noise_amp,
-                                                  seed + (uint64_t)d, 1, h.u_in, -1, -1);
+                                                  seed + (uint64_t)d, 1, h.u_in, -1, -1,
+                                                  make_store_ref(h.u_in, h.omega));
     }
     BCK(cudaGetLastError());
     return LBM_OK;
@@ -574,7 +579,7 @@ int lbm_batch_read_field(lbm_batch* b, uint32_t domain, int field, float* out) {
       using S = typename St::S;
       k_moments<St><<<grid, kBlock, 0, b->stream>>>(h.L, (const S*)(b->arena + h.off_f[b->cur]),
                                                    (const S*)(b->arena + h.off_rest), mom, mom + h.L.ps,
-                                                   mom + 2 * h.L.ps);
+                                                   mom + 2 * h.L.ps, make_store_ref(h.u_in, h.omega));
       BCK(cudaGetLastError());
       return LBM_OK;
     };
@@ -601,7 +606,8 @@ int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
     using St = decltype(tag);
     using S = typename St::S;
     k_read_pops<St, float><<<grid, kBlock, 0, b->stream>>>(h.L, (const S*)(b->arena + h.off_f[b->cur]),
-                                                           (const S*)(b->arena + h.off_rest), b->d_staging);
+                                                           (const S*)(b->arena + h.off_rest), b->d_staging,
+                                                           make_store_ref(h.u_in, h.omega));
     BCK(cudaGetLastError());
     return LBM_OK;
   };

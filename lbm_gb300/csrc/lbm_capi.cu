@@ -70,12 +70,13 @@ constexpr int kStepGraph = 16;   // steps per captured graph (even)
 constexpr int kRunGraphMax = 64; // longest call captured whole
 
 struct StepGraphKey {
-  float omega = 0.0f, drift = 0.0f;
+  float omega = 0.0f, drift = 0.0f, u_in = 0.0f;
   int kernel = -1, rows = 0, bands = 0, staged_rows = 0;
   const void* closure = nullptr;
   cudaStream_t stream = nullptr;
   bool operator==(const StepGraphKey& o) const {
-    return omega == o.omega && drift == o.drift && kernel == o.kernel && rows == o.rows && bands == o.bands &&
+    return omega == o.omega && drift == o.drift && u_in == o.u_in && kernel == o.kernel && rows == o.rows &&
+           bands == o.bands &&
            staged_rows == o.staged_rows && closure == o.closure && stream == o.stream;
   }
 };
@@ -138,6 +139,9 @@ struct lbm_sim {
 namespace {
 
 void* mom_plane(lbm_sim* s, int k) { return (char*)s->mom + (size_t)k * s->L.ps * s->cs; }
+
+// Reference state of 16-bit storage: the inlet velocity, and the lattice's omega.
+StoreRef store_ref(const lbm_sim* s) { return make_store_ref(s->u_in, s->omega); }
 
 template <class F> int dispatch_storage(int storage, F&& f) {
   switch (storage) {
@@ -224,12 +228,16 @@ int materialise(lbm_sim* s) {
   if (s->materialised) return LBM_OK;
   const int dst = 1 - s->cur;
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  const StoreRef ref = store_ref(s);
   auto launch = [&](auto tag) -> int {
-    using S = typename decltype(tag)::S;
+    using St = decltype(tag);
+    using S = typename St::S;
     if (s->edge == EDGE_REF)
-      k_materialise<S, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (S*)s->f[dst], s->mask_d);
+      k_materialise<St, EDGE_REF><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (S*)s->f[dst],
+                                                                    s->mask_d, ref);
     else
-      k_materialise<S, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (S*)s->f[dst], s->mask_d);
+      k_materialise<St, EDGE_CHANNEL><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur],
+                                                                        (S*)s->f[dst], s->mask_d, ref);
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -250,7 +258,7 @@ int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64
     using C = typename St::C;
     k_init<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)rho, (C)ux, (C)uy,
                                                   (C)amp, seed, s->edge == EDGE_CHANNEL, (C)s->u_in, single,
-                                                  single_cell);
+                                                  single_cell, store_ref(s));
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -390,7 +398,8 @@ int compute_moments(lbm_sim* s) {
     using S = typename St::S;
     using C = typename St::C;
     k_moments<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
-                                                     (C*)mom_plane(s, 0), (C*)mom_plane(s, 1), (C*)mom_plane(s, 2));
+                                                     (C*)mom_plane(s, 0), (C*)mom_plane(s, 1), (C*)mom_plane(s, 2),
+                                                     store_ref(s));
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -603,17 +612,34 @@ int lbm_set_viscosity(lbm_sim* s, float nu) {
   return lbm_set_omega(s, 1.0f / (3.0f * nu + 0.5f));  // lib.rs:183
 }
 
+// The inlet velocity is also the reference state of 16-bit storage: without a
+// field reset, the stored words are first re-expressed against the new one.
 int lbm_set_inlet_velocity(lbm_sim* s, float ux, int reset_field) {
   CHECK_SIM(s);
-  s->u_in = ux;
-  if (reset_field) return launch_init(s, 1.0, ux, 0.0, 0.0, 0, -1, -1);
+  if (reset_field) {
+    s->u_in = ux;
+    return launch_init(s, 1.0, ux, 0.0, 0.0, 0, -1, -1);
+  }
   int rc = materialise(s);
   if (rc) return rc;
+  const StoreRef from = store_ref(s);
+  const bool rebase = (s->storage == STORE_F16 || s->storage == STORE_BF16) && ux != s->u_in;
+  s->u_in = ux;
+  const StoreRef to = store_ref(s);
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
     using C = typename St::C;
-    k_inlet<St><<<(s->L.ny + 127) / 128, 128, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)ux);
+    if constexpr (St::kDev) {
+      if (rebase) {
+        k_rebase<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, from, to);
+        CK_LAUNCH();
+        s->launches++;
+      }
+    }
+    k_inlet<St><<<(s->L.ny + 127) / 128, 128, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)ux,
+                                                               to);
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -689,6 +715,7 @@ static int launch_rows(lbm_sim* s, bool last, int row0, int row_end, int dst) {
     a.tau0 = 1.0f / s->omega;
     a.drift = s->drift;
     a.fallback = s->closure_on ? s->fallback_d : nullptr;
+    a.ref = store_ref(s);
     if (variant >= 2) {
       return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
     } else if (variant == 1) {
@@ -722,6 +749,7 @@ static int launch_step(lbm_sim* s, bool last) {
 static StepGraphKey graph_key(const lbm_sim* s) {
   StepGraphKey k;
   k.omega = s->omega;
+  k.u_in = s->u_in;
   k.kernel = s->kernel;
   k.rows = s->rows;
   k.closure = s->closure_on ? (const void*)s->closure_d : nullptr;
@@ -905,10 +933,10 @@ static int read_pops(lbm_sim* s, void* out, bool f64, bool device_out = false) {
     using S = typename St::S;
     if (f64)
       k_read_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
-                                                                (double*)dst);
+                                                                (double*)dst, store_ref(s));
     else
       k_read_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (const S*)s->f[s->cur], (const S*)s->rest,
-                                                               (float*)dst);
+                                                               (float*)dst, store_ref(s));
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -944,10 +972,10 @@ static int write_pops(lbm_sim* s, const void* in, bool f64) {
     using S = typename St::S;
     if (f64)
       k_write_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
-                                                                 (const double*)src);
+                                                                 (const double*)src, store_ref(s));
     else
       k_write_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
-                                                                (const float*)src);
+                                                                (const float*)src, store_ref(s));
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -978,10 +1006,11 @@ int lbm_read_force(lbm_sim* s, double out[2]) {
     using St = decltype(tag);
     using S = typename St::S;
     if (s->edge == EDGE_REF)
-      k_force_partial<St, EDGE_REF><<<kReduceBlocks, 256, 0, s->stream>>>(s->L, (const S*)P, s->mask_d, s->partial_d);
+      k_force_partial<St, EDGE_REF><<<kReduceBlocks, 256, 0, s->stream>>>(s->L, (const S*)P, s->mask_d,
+                                                                          s->partial_d, store_ref(s));
     else
       k_force_partial<St, EDGE_CHANNEL><<<kReduceBlocks, 256, 0, s->stream>>>(s->L, (const S*)P, s->mask_d,
-                                                                              s->partial_d);
+                                                                              s->partial_d, store_ref(s));
     CK_LAUNCH();
     return LBM_OK;
   };

@@ -29,25 +29,47 @@ template <class C> __host__ __device__ inline C weight(int q) {
 template <class C> __device__ __forceinline__ void moments(const C f[9], C& rho, C& jx, C& jy);
 template <class C> __device__ __forceinline__ void bgk(C f[9], C rho, C jx, C jy, C w);
 
-// Deviation-form BGK on g_i = f_i - w_i, for 16-bit storage (f32 arithmetic,
-// explicit FMA, one reciprocal by Newton's method: recip_newton).  rho = 1 + drho keeps the density
-// deviation at full precision; f_i^eq - w_i = w_i * (c0 + rho * (t + t^2/2))
-// with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho u^2.  Both
-// are written in the momentum j = rho u, so u itself is never formed:
+// Reference state of the 16-bit storage: the stored word of direction q is
+// h_q = f_q - r_q, r_q = f_q^eq(rho = 1, u = (u_ref, 0)) with u_ref the
+// lattice's inlet velocity.  Flow near the inlet velocity then stores small
+// words, whose 16-bit rounding error is as much smaller than that of f_q - w_q.
+//   d_q  = r_q - w_q = w_q (3 c.u + 4.5 (c.u)^2 - 1.5 u^2), in double, rounded to f32
+//   r_q  = w_q + d_q (f32), for the readout f_q = r_q + h_q
+//   bb_q = d_{8-q} - d_q (f32): a population bounced back into q from the
+//          cell's own 8 - q is re-expressed as h_{8-q} + bb_q and rounded to
+//          the storage format (opposite directions have different references)
+//   nk_q = -(omega d_q) (f32) for the lattice's uniform omega (the collision
+//          computes the same product itself where omega varies per cell)
+// u_ref = 0 gives d = bb = nk = 0 and the plain f_q - w_q words.  f32 / f64
+// storage ignores it.
+struct StoreRef {
+  float d[9], r[9], bb[9], nk[9];
+  float ux, uy;
+};
+
+// Deviation-form BGK on the 16-bit storage words h_i = f_i - r_i (StoreRef),
+// in f32 arithmetic with explicit FMA and one reciprocal by Newton's method
+// (recip_newton).  rho = 1 + drho keeps the density deviation at full
+// precision, drho = sum h_i, and j = u_ref + sum c_i h_i (the reference
+// state's moments are 1 and u_ref).  f_i^eq - w_i = w_i * (c0 + rho * (t +
+// t^2/2)) with t = 3 c_i.u and the per-cell constant c0 = drho - 1.5 rho
+// u^2.  Both are written in the momentum j = rho u, so u itself is never
+// formed:
 //   rho (t + t^2/2) = T + (T / (2 rho)) T,  T = 3 c_i.j,
 //   c0 = drho - 1.5 |j|^2 / rho.
-// The relaxation g_i' = (1 - omega) g_i + omega (f_i^eq - w_i) is evaluated as
-// g_i' = (omega w_i) X_i + ((1 - omega) g_i + b_i), X_i = T + (T / (2 rho)) T,
-// b_i = (omega w_i) c0 (two weight classes): three fused operations per
-// moving direction.  The moments sum the three columns (c_x = -1, 0, +1)
-// first, so jx and drho share them.
-__device__ __forceinline__ void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
+// The relaxation h_i' = (1 - omega) h_i + omega (f_i^eq - r_i) is evaluated as
+// h_i' = (omega w_i) X_i + ((1 - omega) h_i + b_i), X_i = T + (T / (2 rho)) T,
+// b_i = (omega w_i) c0 - omega d_i: four fused operations per moving
+// direction.  The moments sum the three columns (c_x = -1, 0, +1) first, so
+// jx and drho share them.
+__device__ __forceinline__ void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy,
+                                            const StoreRef& R) {
   const float cw = (g[0] + g[3]) + g[6];  // c_x = -1
   const float ce = (g[2] + g[5]) + g[8];  // c_x = +1
   const float cm = (g[1] + g[7]) + g[4];  // c_x = 0
   drho = (cw + ce) + cm;
-  jx = ce - cw;
-  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  jx = (ce - cw) + R.ux;
+  jy = (((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8])) + R.uy;
   rho = 1.0f + drho;
 }
 // 1 / x for a positive normal x: a seed from the float's bits (a linear
@@ -71,25 +93,25 @@ struct DevOmega {
   __device__ __forceinline__ explicit DevOmega(float omega)
       : omw(1.0f - omega), aw1(omega * (1.0f / 9.0f)), aw2(omega * (1.0f / 36.0f)), aw0(omega * (4.0f / 9.0f)) {}
 };
-__device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, const DevOmega& o) {
+// NK(q) is -(omega d_q): the lattice's precomputed R.nk[q] where omega is
+// uniform, the same product formed per cell where it is not.
+template <class NK>
+__device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, const DevOmega& o,
+                                            NK nk) {
   const float h = 0.5f * recip_newton(rho);               // 1 / (2 rho)
   const float c0 = __fmaf_rn(__fmaf_rn(jx, jx, jy * jy), -3.0f * h, drho);
   const float tx = 3.0f * jx, ty = 3.0f * jy;              // T of the axis directions
   const float tp = tx + ty, tm = tx - ty;                  // and of the diagonals
   const float hx = h * tx, hy = h * ty, hp = h * tp, hm = h * tm;
-  const float b1 = o.aw1 * c0, b2 = o.aw2 * c0;
-  g[5] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, tx), __fmaf_rn(o.omw, g[5], b1));   // e  (+x)
-  g[3] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, -tx), __fmaf_rn(o.omw, g[3], b1));  // w  (-x)
-  g[1] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, ty), __fmaf_rn(o.omw, g[1], b1));   // n  (+y)
-  g[7] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, -ty), __fmaf_rn(o.omw, g[7], b1));  // s  (-y)
-  g[2] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, tp), __fmaf_rn(o.omw, g[2], b2));   // ne (+x+y)
-  g[6] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, -tp), __fmaf_rn(o.omw, g[6], b2));  // sw (-x-y)
-  g[8] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, tm), __fmaf_rn(o.omw, g[8], b2));   // se (+x-y)
-  g[0] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, -tm), __fmaf_rn(o.omw, g[0], b2));  // nw (-x+y)
-  g[4] = __fmaf_rn(o.omw, g[4], o.aw0 * c0);                                    // rest (T = 0)
-}
-__device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
-  collide_dev(g, rho, drho, jx, jy, DevOmega(omega));
+  g[5] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, tx), __fmaf_rn(o.omw, g[5], __fmaf_rn(o.aw1, c0, nk(5))));   // e
+  g[3] = __fmaf_rn(o.aw1, __fmaf_rn(hx, tx, -tx), __fmaf_rn(o.omw, g[3], __fmaf_rn(o.aw1, c0, nk(3))));  // w
+  g[1] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, ty), __fmaf_rn(o.omw, g[1], __fmaf_rn(o.aw1, c0, nk(1))));   // n
+  g[7] = __fmaf_rn(o.aw1, __fmaf_rn(hy, ty, -ty), __fmaf_rn(o.omw, g[7], __fmaf_rn(o.aw1, c0, nk(7))));  // s
+  g[2] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, tp), __fmaf_rn(o.omw, g[2], __fmaf_rn(o.aw2, c0, nk(2))));   // ne
+  g[6] = __fmaf_rn(o.aw2, __fmaf_rn(hp, tp, -tp), __fmaf_rn(o.omw, g[6], __fmaf_rn(o.aw2, c0, nk(6))));  // sw
+  g[8] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, tm), __fmaf_rn(o.omw, g[8], __fmaf_rn(o.aw2, c0, nk(8))));   // se
+  g[0] = __fmaf_rn(o.aw2, __fmaf_rn(hm, tm, -tm), __fmaf_rn(o.omw, g[0], __fmaf_rn(o.aw2, c0, nk(0))));  // nw
+  g[4] = __fmaf_rn(o.omw, g[4], __fmaf_rn(o.aw0, c0, nk(4)));                                            // rest
 }
 
 // Storage policies.  S is the stored word, C the arithmetic type, and a
@@ -103,46 +125,85 @@ __device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, f
 //                     once per lattice where omega is uniform
 struct StF32 {
   using S = float; using C = float; using Om = float;
+  static constexpr bool kDev = false;
   __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
-  __device__ static C f_of(S s, int) { return s; }
-  __device__ static S of_f(C f, int) { return f; }
-  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
-  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
+  __device__ static C f_of(S s, int, const StoreRef&) { return s; }
+  __device__ static S of_f(C f, int, const StoreRef&) { return f; }
+  __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef&) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
+  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
+  __device__ static void collide_u(C v[9], C rho, C, C jx, C jy, const Om& w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF64 {
   using S = double; using C = double; using Om = double;
+  static constexpr bool kDev = false;
   __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
-  __device__ static C f_of(S s, int) { return s; }
-  __device__ static S of_f(C f, int) { return f; }
-  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
-  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w) { bgk<C>(v, rho, jx, jy, w); }
+  __device__ static C f_of(S s, int, const StoreRef&) { return s; }
+  __device__ static S of_f(C f, int, const StoreRef&) { return f; }
+  __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef&) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
+  __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
+  __device__ static void collide_u(C v[9], C rho, C, C jx, C jy, const Om& w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
 };
-struct StF16 {  // binary16 deviation from the rest-state weight
-  using S = __half; using C = float; using Om = DevOmega;
+// 16-bit words relative to the reference state (StoreRef); `Word` supplies
+// the conversions of binary16 or bfloat16.
+template <class Word> struct StDev {
+  using S = typename Word::S; using C = float; using Om = DevOmega;
+  static constexpr bool kDev = true;
   __device__ static Om omega_consts(C w) { return DevOmega(w); }
-  __device__ static C load(S s, int) { return __half2float(s); }
-  __device__ static S store(C v, int) { return __float2half_rn(v); }
-  __device__ static C f_of(S s, int q) { return weight<float>(q) + __half2float(s); }
-  __device__ static S of_f(C f, int q) { return __float2half_rn(f - weight<float>(q)); }
-  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
-  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
-  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, const Om& o) { collide_dev(v, rho, aux, jx, jy, o); }
+  __device__ static C load(S s, int) { return Word::to_f(s); }
+  __device__ static S store(C v, int) { return Word::of(v); }
+  __device__ static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + Word::to_f(s); }
+  __device__ static S of_f(C f, int q, const StoreRef& R) { return Word::of((f - weight<float>(q)) - R.d[q]); }
+  // the own population 8 - q bounced back into direction q: re-expressed
+  // against q's reference and rounded to the storage format
+  __device__ static C bounce(S s, int q, const StoreRef& R) { return Word::to_f(Word::of(Word::to_f(s) + R.bb[q])); }
+  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef& R) {
+    moments_dev(v, rho, aux, jx, jy, R);
+  }
+  // per-cell omega: -(omega d_q) formed here
+  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w, const StoreRef& R) {
+    collide_dev(v, rho, aux, jx, jy, DevOmega(w), [&](int q) { return -(w * R.d[q]); });
+  }
+  // the lattice's uniform omega: its constants, and -(omega d_q) from R.nk
+  __device__ static void collide_u(C v[9], C rho, C aux, C jx, C jy, const Om& o, const StoreRef& R) {
+    collide_dev(v, rho, aux, jx, jy, o, [&](int q) { return R.nk[q]; });
+  }
 };
-struct StBF16 {  // bfloat16 deviation from the rest-state weight
-  using S = __nv_bfloat16; using C = float; using Om = DevOmega;
-  __device__ static Om omega_consts(C w) { return DevOmega(w); }
-  __device__ static C load(S s, int) { return __bfloat162float(s); }
-  __device__ static S store(C v, int) { return __float2bfloat16_rn(v); }
-  __device__ static C f_of(S s, int q) { return weight<float>(q) + __bfloat162float(s); }
-  __device__ static S of_f(C f, int q) { return __float2bfloat16_rn(f - weight<float>(q)); }
-  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy) { moments_dev(v, rho, aux, jx, jy); }
-  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w) { collide_dev(v, rho, aux, jx, jy, w); }
-  __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, const Om& o) { collide_dev(v, rho, aux, jx, jy, o); }
+struct WordF16 {
+  using S = __half;
+  __device__ static float to_f(S s) { return __half2float(s); }
+  __device__ static S of(float v) { return __float2half_rn(v); }
 };
+struct WordBF16 {
+  using S = __nv_bfloat16;
+  __device__ static float to_f(S s) { return __bfloat162float(s); }
+  __device__ static S of(float v) { return __float2bfloat16_rn(v); }
+};
+using StF16 = StDev<WordF16>;    // binary16 words
+using StBF16 = StDev<WordBF16>;  // bfloat16 words
+
+// Host side: the reference of inlet velocity u_ref and relaxation rate omega.
+inline StoreRef make_store_ref(float u_ref, float omega) {
+  StoreRef R;
+  const double vx = (double)u_ref, vy = 0.0;
+  const double u2 = vx * vx + vy * vy;
+  for (int q = 0; q < 9; q++) {
+    const double wd = q == 4 ? 4.0 / 9.0 : ((q & 1) ? 1.0 / 9.0 : 1.0 / 36.0);
+    const double cu = (double)cx(q) * vx - (double)cy(q) * vy;  // cy is the row step: north is -1
+    R.d[q] = (float)(wd * (3.0 * cu + 4.5 * cu * cu - 1.5 * u2));
+    R.r[q] = weight<float>(q) + R.d[q];
+    R.nk[q] = -(omega * R.d[q]);
+  }
+  for (int q = 0; q < 9; q++) R.bb[q] = R.d[8 - q] - R.d[q];
+  R.ux = (float)vx;
+  R.uy = (float)vy;
+  return R;
+}
 
 // Device layout of one lattice.
 //   populations: two sets f[0], f[1] of 8 planes (moving directions), plus one

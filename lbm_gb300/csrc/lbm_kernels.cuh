@@ -40,6 +40,7 @@ template <class S, class C> struct StepArgs {
   const __half2* __restrict__ closure;
   float tau0, drift;
   unsigned long long* __restrict__ fallback;  // cells that fell back to plain BGK, or null
+  StoreRef ref;  // reference state of 16-bit storage (inlet velocity, lattice omega)
 };
 
 // Relaxation rate of a cell under the closure record `rec`: 1 / (tau0 +
@@ -150,9 +151,8 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
         // upstream (x - cx, y - cy): row y+1 for cy=-1, y-1 for cy=+1
         const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
         const bool solid_up = (trip >> (1 - cx(q))) & 1u;
-        const S* p = solid_up ? a.src + (long long)slot(8 - q) * L.ps + own
-                              : a.src + (long long)slot(q) * L.ps + own - cx(q) - (long long)cy(q) * L.pitch;
-        f[q] = St::load(*p, q);
+        f[q] = solid_up ? St::bounce(a.src[(long long)slot(8 - q) * L.ps + own], q, a.ref)
+                        : St::load(a.src[(long long)slot(q) * L.ps + own - cx(q) - (long long)cy(q) * L.pitch], q);
       }
     }
   } else {
@@ -165,9 +165,8 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
         int ux_, uy_;
         upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
         const bool solid_up = mask_bit(a.mask, L.mw, ux_, uy_);
-        const S* p = solid_up ? a.src + (long long)slot(8 - q) * L.ps + own
-                              : a.src + (long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_;
-        f[q] = St::load(*p, q);
+        f[q] = solid_up ? St::bounce(a.src[(long long)slot(8 - q) * L.ps + own], q, a.ref)
+                        : St::load(a.src[(long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_], q);
       }
     }
   }
@@ -181,7 +180,7 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
   f[4] = St::load(a.rest[own], 4);
   C rho, jx, jy;
   C aux;
-    St::moments(f, rho, aux, jx, jy);
+  St::moments(f, rho, aux, jx, jy, a.ref);
   if (!(rho == rho) || rho - rho != C(0)) atomicOr(a.flag, 1);  // NaN or Inf
   if (a.rho_out) {
     a.rho_out[own] = rho;
@@ -189,7 +188,7 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
     a.jy_out[own] = jy;
   }
   if (frozen) return;  // channel inlet: fixed equilibrium, never collided
-  St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy));
+  St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy), a.ref);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     if (q == 4) continue;
@@ -223,6 +222,7 @@ __global__ void __launch_bounds__(128) k_step(StepArgs<typename St::S, typename 
 // the cell is not streamed), one per moving direction in slot order.
 struct CellSrc {
   uint32_t off[8];
+  uint32_t bounced;  // bit q: direction q takes the cell's own 8 - q (bounce-back)
   bool from_dst;
 };
 
@@ -239,6 +239,7 @@ __device__ __forceinline__ void cell_sources(const Layout& L, const uint32_t* __
     streamed = !materialised && !own_solid && x != 0 && !(EDGE == EDGE_REF && y == L.ny - 1);
   }
   cs.from_dst = !streamed;
+  cs.bounced = 0u;
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     if (q == 4) continue;
@@ -248,12 +249,14 @@ __device__ __forceinline__ void cell_sources(const Layout& L, const uint32_t* __
       if (interior) {
         const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
         const bool solid_up = (trip >> (1 - cx(q))) & 1u;
+        cs.bounced |= (solid_up ? 1u : 0u) << q;
         o = solid_up ? (uint32_t)slot(8 - q) * (uint32_t)L.ps + own
                      : base + own - (uint32_t)cx(q) - (uint32_t)(cy(q) * L.pitch);
       } else {
         int ux_, uy_;
         upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
         const bool solid_up = mask_bit(mask, L.mw, ux_, uy_);
+        cs.bounced |= (solid_up ? 1u : 0u) << q;
         o = solid_up ? (uint32_t)slot(8 - q) * (uint32_t)L.ps + own
                      : base + (uint32_t)uy_ * (uint32_t)L.pitch + (uint32_t)ux_;
       }
@@ -324,6 +327,7 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
     // channel mode: the inlet column and solid cells are inert
     const bool frozen = EDGE == EDGE_CHANNEL &&
                         (x == 0 || (interior ? ((t0 >> 1) & 1u) != 0u : mask_bit(a.mask, L.mw, x, y) != 0u));
+    uint32_t bounced = 0u;  // directions that took the cell's own opposite population
     if (interior) {
       if ((t0 >> 1) & 1u) {  // solid: not streamed, own previous values
 #pragma unroll
@@ -334,7 +338,10 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
         for (int q = 0; q < 9; q++) {
           if (q == 4) continue;
           const uint32_t trip = cy(q) < 0 ? tp : (cy(q) > 0 ? tm : t0);
-          if ((trip >> (1 - cx(q))) & 1u) cur[q] = __ldg(a.src + (long long)slot(8 - q) * L.ps + own);
+          if ((trip >> (1 - cx(q))) & 1u) {
+            cur[q] = __ldg(a.src + (long long)slot(8 - q) * L.ps + own);
+            bounced |= 1u << q;
+          }
         }
       }
     } else {  // edge cell: resolve every population by the edge rules
@@ -344,14 +351,15 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
 #pragma unroll
       for (int q = 0; q < 9; q++)
         if (q != 4) cur[q] = base[cs.off[slot(q)]];
+      bounced = cs.from_dst ? 0u : cs.bounced;
     }
     tm = t0; t0 = tp; tp = tn; tn = t3;
     C f[9];
 #pragma unroll
-    for (int q = 0; q < 9; q++) f[q] = St::load(cur[q], q);
+    for (int q = 0; q < 9; q++) f[q] = ((bounced >> q) & 1u) ? St::bounce(cur[q], q, a.ref) : St::load(cur[q], q);
     C rho, jx, jy;
     C aux;
-    St::moments(f, rho, aux, jx, jy);
+    St::moments(f, rho, aux, jx, jy, a.ref);
     if (!(rho - rho == C(0))) atomicOr(a.flag, 1);
     if (a.rho_out) {
       a.rho_out[own] = rho;
@@ -359,7 +367,7 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
       a.jy_out[own] = jy;
     }
     if (!frozen) {
-      St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy));
+      St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy), a.ref);
 #pragma unroll
       for (int q = 0; q < 9; q++) {
         if (q == 4) continue;
@@ -376,10 +384,12 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
 
 // Stream-only pass: turns the fused representation into the reference's
 // pre-collision state S_k in dst (streamed cells pull from src with
-// bounce-back; the others keep their own dst value).  Raw words are copied.
-template <class S, int EDGE>
-__global__ void k_materialise(Layout L, const S* __restrict__ src, S* __restrict__ dst,
-                              const uint32_t* __restrict__ mask) {
+// bounce-back; the others keep their own dst value).  Pulled words are
+// copied; a bounced 16-bit word is re-expressed for its new direction.
+template <class St, int EDGE>
+__global__ void k_materialise(Layout L, const typename St::S* __restrict__ src, typename St::S* __restrict__ dst,
+                              const uint32_t* __restrict__ mask, StoreRef ref) {
+  using S = typename St::S;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= L.nx) return;
@@ -393,7 +403,7 @@ __global__ void k_materialise(Layout L, const S* __restrict__ src, S* __restrict
     int ux_, uy_;
     upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
     const bool solid_up = mask_bit(mask, L.mw, ux_, uy_);
-    v[q] = solid_up ? src[(long long)slot(8 - q) * L.ps + own]
+    v[q] = solid_up ? St::store(St::bounce(src[(long long)slot(8 - q) * L.ps + own], q, ref), q)
                     : src[(long long)slot(q) * L.ps + (long long)uy_ * L.pitch + ux_];
   }
 #pragma unroll
@@ -409,7 +419,8 @@ __global__ void k_materialise(Layout L, const S* __restrict__ src, S* __restrict
 template <class St>
 __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
                        typename St::C rho0, typename St::C ux0, typename St::C uy0, typename St::C amp,
-                       uint64_t seed, int channel, typename St::C u_in, int single, long long single_cell) {
+                       uint64_t seed, int channel, typename St::C u_in, int single, long long single_cell,
+                       StoreRef ref) {
   using C = typename St::C;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
@@ -427,7 +438,7 @@ __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typenam
   if (single >= 0 && (long long)cell == single_cell) eq[single] = C(4.0);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::of_f(eq[q], q);
+    const auto v = St::of_f(eq[q], q, ref);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -437,7 +448,7 @@ __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typenam
 // Column-0 inlet rewrite: set_equil(u_in, 0, 1) into both sets and the rest plane.
 template <class St>
 __global__ void k_inlet(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
-                        typename St::C u_in) {
+                        typename St::C u_in, StoreRef ref) {
   using C = typename St::C;
   const int y = blockIdx.x * blockDim.x + threadIdx.x;
   if (y >= L.ny) return;
@@ -446,7 +457,7 @@ __global__ void k_inlet(Layout L, typename St::S* f0, typename St::S* f1, typena
   set_equil<C>(u_in, C(0), C(1), eq);
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::of_f(eq[q], q);
+    const auto v = St::of_f(eq[q], q, ref);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -456,7 +467,7 @@ __global__ void k_inlet(Layout L, typename St::S* f0, typename St::S* f1, typena
 // Populations of a materialised set (plus the rest plane) to a compact
 // plane-major array of 9 * nx * ny values in the reference order.
 template <class St, class O>
-__global__ void k_read_pops(Layout L, const typename St::S* f, const typename St::S* rest, O* out) {
+__global__ void k_read_pops(Layout L, const typename St::S* f, const typename St::S* rest, O* out, StoreRef ref) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= L.nx) return;
@@ -465,7 +476,7 @@ __global__ void k_read_pops(Layout L, const typename St::S* f, const typename St
 #pragma unroll
   for (int q = 0; q < 9; q++) {
     const auto s = q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own];
-    out[q * n + c] = (O)St::f_of(s, q);
+    out[q * n + c] = (O)St::f_of(s, q, ref);
   }
 }
 
@@ -482,10 +493,32 @@ static __global__ void k_pack_mask(Layout L, const uint8_t* __restrict__ bytes, 
   words[(long long)y * L.mw + w] = v;
 }
 
+// 16-bit words re-expressed from reference `from` to reference `to` (a new
+// inlet velocity), h' = of_f(f_of(h, from), to), in both sets and the rest
+// plane, over every cell.
+template <class St>
+__global__ void k_rebase(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest, StoreRef from,
+                         StoreRef to) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= L.nx) return;
+  const long long own = (long long)y * L.pitch + x;
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) {
+      rest[own] = St::of_f(St::f_of(rest[own], 4, from), 4, to);
+      continue;
+    }
+    const long long i = (long long)slot(q) * L.ps + own;
+    f0[i] = St::of_f(St::f_of(f0[i], q, from), q, to);
+    f1[i] = St::of_f(St::f_of(f1[i], q, from), q, to);
+  }
+}
+
 // Compact plane-major populations into both sets and the rest plane.
 template <class St, class I>
 __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
-                             const I* in) {
+                             const I* in, StoreRef ref) {
   using C = typename St::C;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
@@ -494,7 +527,7 @@ __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, t
   const long long n = (long long)L.nx * L.ny, c = (long long)y * L.nx + x;
 #pragma unroll
   for (int q = 0; q < 9; q++) {
-    const auto v = St::of_f((C)in[q * n + c], q);
+    const auto v = St::of_f((C)in[q * n + c], q, ref);
     if (q == 4) { rest[own] = v; continue; }
     f0[(long long)slot(q) * L.ps + own] = v;
     f1[(long long)slot(q) * L.ps + own] = v;
@@ -509,7 +542,8 @@ __global__ void k_write_pops(Layout L, typename St::S* f0, typename St::S* f1, t
 // x is +x, y is north (row - 1) positive.
 template <class St, int EDGE>
 __global__ void __launch_bounds__(256) k_force_partial(Layout L, const typename St::S* __restrict__ P,
-                                                      const uint32_t* __restrict__ mask, double* __restrict__ partial) {
+                                                      const uint32_t* __restrict__ mask, double* __restrict__ partial,
+                                                      StoreRef ref) {
   __shared__ double sh[2][256];
   double fx = 0.0, fy = 0.0;
   const long long n = (long long)L.nx * L.ny;
@@ -524,7 +558,7 @@ __global__ void __launch_bounds__(256) k_force_partial(Layout L, const typename 
       upstream_edge<EDGE>(L, x, y, q, ux_, uy_);
       if (!mask_bit(mask, L.mw, ux_, uy_)) continue;
       const int p = 8 - q;
-      const double f = (double)St::f_of(P[(long long)slot(p) * L.ps + own], p);
+      const double f = (double)St::f_of(P[(long long)slot(p) * L.ps + own], p, ref);
       fx += 2.0 * f * (double)cx(p);
       fy -= 2.0 * f * (double)cy(p);
     }
@@ -547,7 +581,7 @@ __global__ void __launch_bounds__(256) k_force_partial(Layout L, const typename 
 // first step after an initialisation.
 template <class St>
 __global__ void k_moments(Layout L, const typename St::S* f, const typename St::S* rest, typename St::C* rho_out,
-                          typename St::C* jx_out, typename St::C* jy_out) {
+                          typename St::C* jx_out, typename St::C* jy_out, StoreRef ref) {
   using C = typename St::C;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
@@ -557,7 +591,7 @@ __global__ void k_moments(Layout L, const typename St::S* f, const typename St::
 #pragma unroll
   for (int q = 0; q < 9; q++) v[q] = St::load(q == 4 ? rest[own] : f[(long long)slot(q) * L.ps + own], q);
   C rho, aux, jx, jy;
-  St::moments(v, rho, aux, jx, jy);
+  St::moments(v, rho, aux, jx, jy, ref);
   rho_out[own] = rho;
   jx_out[own] = jx;
   jy_out[own] = jy;

@@ -324,14 +324,14 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         if (q != 4) f[q] = St::load(a.dstp[slot(q)][own], q);
       f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[tid], 4);
       C rho, jx, jy, aux;
-      St::moments(f, rho, aux, jx, jy);
+      St::moments(f, rho, aux, jx, jy, a.ref);
       rho_sum += rho;
       if (a.rho_out) {
         a.rho_out[own] = rho;
         a.jx_out[own] = jx;
         a.jy_out[own] = jy;
       }
-      St::collide(f, rho, aux, jx, jy, a.omega);
+      St::collide(f, rho, aux, jx, jy, a.omega, a.ref);
 #pragma unroll
       for (int q = 0; q < 9; q++)
         if (q != 4) a.dstp[slot(q)][own] = St::store(f[q], q);
@@ -403,7 +403,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 #pragma unroll
           for (int j = 0; j < CPT; j++) {
             const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);
-            if ((rowwin >> (j + 1 + dx)) & 1u) f[q][j] = St::load(opp[e + j], q);
+            if ((rowwin >> (j + 1 + dx)) & 1u) f[q][j] = St::bounce(opp[e + j], q, a.ref);
           }
         }
       }
@@ -414,7 +414,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 #pragma unroll
         for (int q = 0; q < 9; q++) g[q] = f[q][j];
         C rho, jx, jy, aux;
-        St::moments(g, rho, aux, jx, jy);
+        St::moments(g, rho, aux, jx, jy, a.ref);
         if (act[j]) rho_sum += rho;
         m_rho[j] = rho;
         m_jx[j] = jx;
@@ -423,9 +423,9 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           bool fell_back;
           const C w = closure_omega(a, rec[j], rho, jx, jy, fell_back);
           fallbacks += (fell_back && act[j]) ? 1u : 0u;
-          St::collide(g, rho, aux, jx, jy, w);
+          St::collide(g, rho, aux, jx, jy, w, a.ref);
         } else {
-          St::collide(g, rho, aux, jx, jy, om);
+          St::collide_u(g, rho, aux, jx, jy, om, a.ref);
         }
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
@@ -489,7 +489,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
             if (q != 4) f[q] = St::load(a.dstp[slot(q)][own + j], q);
           f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
           C rho, jx, jy, aux;
-          St::moments(f, rho, aux, jx, jy);
+          St::moments(f, rho, aux, jx, jy, a.ref);
           a.rho_out[own + j] = rho;
           a.jx_out[own + j] = jx;
           a.jy_out[own + j] = jy;

@@ -118,28 +118,60 @@ template <class C> inline C weight(int q) {
   return (q & 1) ? C(1.0) / C(9.0) : C(1.0) / C(36.0);
 }
 
+// Reference state of the 16-bit storage modes: the stored word of direction q
+// is h_q = f_q - r_q, r_q = f_q^eq(rho = 1, u = (u_ref, 0)), the equilibrium of
+// the channel's inlet velocity u_ref.  In most of a channel the flow stays
+// near the inlet velocity, so h_q is several times smaller than f_q - w_q and
+// its 16-bit rounding error is as much smaller.  d_q = r_q - w_q =
+// w_q (3 c.u + 4.5 (c.u)^2 - 1.5 u^2) is evaluated in double and rounded to
+// f32; r_q = w_q + d_q in f32.  u_ref = 0 gives d_q = 0, i.e. h_q = f_q - w_q.
+// In exact arithmetic sum_q d_q = 0 and sum_q c_q d_q = u_ref, which the
+// collision uses (moments_dev, collide_dev).  Opposite directions have
+// different references, so a population bounced back into direction q (from
+// the cell's own 8 - q) is re-expressed: h_q = h_{8-q} + bb_q, bb_q = d_{8-q} -
+// d_q (f32), rounded to the storage format.
+struct StoreRef {
+  float d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float r[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float bb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  float ux = 0.0f, uy = 0.0f;
+  void set(double vx, double vy) {
+    const double wd[9] = {1.0 / 36, 1.0 / 9, 1.0 / 36, 1.0 / 9, 4.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 9, 1.0 / 36};
+    const double u2 = vx * vx + vy * vy;
+    for (int q = 0; q < 9; q++) {
+      const double cu = (double)CX[q] * vx - (double)CY[q] * vy;  // CY is the row step: north is -1
+      d[q] = (float)(wd[q] * (3.0 * cu + 4.5 * cu * cu - 1.5 * u2));
+      r[q] = weight<float>(q) + d[q];
+    }
+    for (int q = 0; q < 9; q++) bb[q] = d[8 - q] - d[q];
+    ux = (float)vx;
+    uy = (float)vy;
+  }
+};
+
 // Storage policies.  load / store convert between the stored word and the
 // working value of the collision; f_of / of_f between the stored word and the
 // population value f_q.  f32 / f64 work on f_q with the reference's
-// arithmetic (kDev = false).  16-bit storage keeps g_q = f_q - w_q and works
-// on g_q with the engine's own deviation-form collision (kDev = true; see
-// moments_dev / collide_dev below), which has no counterpart in the reference.
+// arithmetic (kDev = false).  16-bit storage keeps h_q = f_q - r_q (StoreRef)
+// and works on it with the engine's own deviation-form collision (kDev = true;
+// see moments_dev / collide_dev below), which has no counterpart in the
+// reference.
 struct StF32 { using S = float; using C = float; static constexpr bool kDev = false;
   static C load(S s, int) { return s; } static S store(C v, int) { return v; }
-  static C f_of(S s, int) { return s; } static S of_f(C v, int) { return v; } };
+  static C f_of(S s, int, const StoreRef&) { return s; } static S of_f(C v, int, const StoreRef&) { return v; } };
 struct StF64 { using S = double; using C = double; static constexpr bool kDev = false;
   static C load(S s, int) { return s; } static S store(C v, int) { return v; }
-  static C f_of(S s, int) { return s; } static S of_f(C v, int) { return v; } };
+  static C f_of(S s, int, const StoreRef&) { return s; } static S of_f(C v, int, const StoreRef&) { return v; } };
 struct StF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
   static C load(S s, int) { return half_to_float(s); }
   static S store(C v, int) { return float_to_half_rn(v); }
-  static C f_of(S s, int q) { return weight<float>(q) + half_to_float(s); }
-  static S of_f(C v, int q) { return float_to_half_rn(v - weight<float>(q)); } };
+  static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + half_to_float(s); }
+  static S of_f(C v, int q, const StoreRef& R) { return float_to_half_rn((v - weight<float>(q)) - R.d[q]); } };
 struct StBF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
   static C load(S s, int) { return bf16_to_float(s); }
   static S store(C v, int) { return float_to_bf16_rn(v); }
-  static C f_of(S s, int q) { return weight<float>(q) + bf16_to_float(s); }
-  static S of_f(C v, int q) { return float_to_bf16_rn(v - weight<float>(q)); } };
+  static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + bf16_to_float(s); }
+  static S of_f(C v, int q, const StoreRef& R) { return float_to_bf16_rn((v - weight<float>(q)) - R.d[q]); } };
 
 // Reciprocal by Newton's method, as the GPU kernels compute it: the seed
 // 0x7EF311C2 - bits(x) (a linear approximation of 1/x per binade), then three
@@ -154,43 +186,46 @@ inline float recip_newton(float x) {
   return r;
 }
 
-// Deviation-form BGK of the 16-bit storage modes, on g_q = f_q - w_q, with
-// rho = 1 + drho, one reciprocal (recip_newton) and fused multiply-adds:
-// f_q^eq - w_q = w_q (c0 + rho (t + t^2/2)), t = 3 c_q.u, c0 = drho - 1.5 rho u^2,
-// written in j = rho u: rho (t + t^2/2) = T + (T / (2 rho)) T with T = 3 c_q.j,
-// c0 = drho - 1.5 |j|^2 / rho; relaxed as
-// g_q' = (omega w_q) X_q + ((1 - omega) g_q + (omega w_q) c0).  The moments sum
-// the columns c_x = -1, 0, +1 first.  Operation order is part of the
-// definition (the GPU kernels use the same).
-inline void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy) {
+// Deviation-form BGK of the 16-bit storage modes, on h_q = f_q - r_q
+// (StoreRef), with rho = 1 + drho, one reciprocal (recip_newton) and fused
+// multiply-adds.  The moments: drho = sum h_q, j = u_ref + sum c_q h_q (the
+// reference state's moments are 1 and u_ref).  f_q^eq - w_q = w_q (c0 + rho
+// (t + t^2/2)), t = 3 c_q.u, c0 = drho - 1.5 rho u^2, written in j = rho u:
+// rho (t + t^2/2) = T + (T / (2 rho)) T with T = 3 c_q.j, c0 = drho - 1.5
+// |j|^2 / rho; relaxed as h_q' = (1 - omega) h_q + omega (f_q^eq - r_q) =
+// (omega w_q) X_q + ((1 - omega) h_q + b_q), b_q = (omega w_q) c0 - omega
+// d_q.  The moments sum the columns c_x = -1, 0, +1 first.  Operation order
+// is part of the definition (the GPU kernels use the same); with u_ref = 0 the
+// terms in d_q and u_ref add zeros and change nothing.
+inline void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy, const StoreRef& R) {
   const float cw = (g[0] + g[3]) + g[6];
   const float ce = (g[2] + g[5]) + g[8];
   const float cm = (g[1] + g[7]) + g[4];
   drho = (cw + ce) + cm;
-  jx = ce - cw;
-  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  jx = (ce - cw) + R.ux;
+  jy = (((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8])) + R.uy;
   rho = 1.0f + drho;
 }
 inline float relax_dev(float g, float aw, float h, float t, float sign, float omw, float b) {
   return std::fma(aw, std::fma(h * t, t, sign * t), std::fma(omw, g, b));
 }
-inline void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega) {
+inline void collide_dev(float g[9], float rho, float drho, float jx, float jy, float omega, const StoreRef& R) {
   const float h = 0.5f * recip_newton(rho);
   const float c0 = std::fma(std::fma(jx, jx, jy * jy), -3.0f * h, drho);
   const float tx = 3.0f * jx, ty = 3.0f * jy;
   const float tp = tx + ty, tm = tx - ty;
   const float omw = 1.0f - omega;
   const float aw1 = omega * (1.0f / 9.0f), aw2 = omega * (1.0f / 36.0f), aw0 = omega * (4.0f / 9.0f);
-  const float b1 = aw1 * c0, b2 = aw2 * c0;
-  g[5] = relax_dev(g[5], aw1, h, tx, 1.0f, omw, b1);
-  g[3] = relax_dev(g[3], aw1, h, tx, -1.0f, omw, b1);
-  g[1] = relax_dev(g[1], aw1, h, ty, 1.0f, omw, b1);
-  g[7] = relax_dev(g[7], aw1, h, ty, -1.0f, omw, b1);
-  g[2] = relax_dev(g[2], aw2, h, tp, 1.0f, omw, b2);
-  g[6] = relax_dev(g[6], aw2, h, tp, -1.0f, omw, b2);
-  g[8] = relax_dev(g[8], aw2, h, tm, 1.0f, omw, b2);
-  g[0] = relax_dev(g[0], aw2, h, tm, -1.0f, omw, b2);
-  g[4] = std::fma(omw, g[4], aw0 * c0);
+  auto b = [&](float aw, int q) { return std::fma(aw, c0, -(omega * R.d[q])); };
+  g[5] = relax_dev(g[5], aw1, h, tx, 1.0f, omw, b(aw1, 5));
+  g[3] = relax_dev(g[3], aw1, h, tx, -1.0f, omw, b(aw1, 3));
+  g[1] = relax_dev(g[1], aw1, h, ty, 1.0f, omw, b(aw1, 1));
+  g[7] = relax_dev(g[7], aw1, h, ty, -1.0f, omw, b(aw1, 7));
+  g[2] = relax_dev(g[2], aw2, h, tp, 1.0f, omw, b(aw2, 2));
+  g[6] = relax_dev(g[6], aw2, h, tp, -1.0f, omw, b(aw2, 6));
+  g[8] = relax_dev(g[8], aw2, h, tm, 1.0f, omw, b(aw2, 8));
+  g[0] = relax_dev(g[0], aw2, h, tm, -1.0f, omw, b(aw2, 0));
+  g[4] = std::fma(omw, g[4], b(aw0, 4));
 }
 
 // splitmix64 finaliser; the seeded per-cell noise of the initial state.
@@ -238,9 +273,10 @@ struct SimBase {
   int X = 0, Y = 0, edge = 0, prec = 0, threads = 1;
   size_t N = 0;
   uint64_t step = 0;                 // compute_step, lbm.rs:1115
-  double u_in = 0.1;                 // channel inlet velocity
+  double u_in = 0.1;                 // channel inlet velocity (and the 16-bit storage reference)
   std::vector<uint8_t> barrier;      // 1 = solid (the reference's u32 barrier buffer)
   virtual void set_omega(double w) = 0;
+  virtual void set_inlet_velocity(double u) = 0;
   virtual void init_equilibrium(double rho, double ux, double uy, double amp, uint64_t seed) = 0;
   virtual void single_cell(int dir) = 0;
   virtual void set_inlet_columns(bool any_mode = false) = 0;
@@ -257,6 +293,7 @@ template <class St> struct Sim : SimBase {
   C omega = C(1.0);
   std::vector<S> f[2][9];  // f[set][q]; f[1][4] is never used (rest lives in set 0)
   std::vector<C> ux, uy, rho;  // density_bg: momenta and density (lbm.rs:779-781)
+  StoreRef ref;            // the 16-bit storage reference, at (u_in, 0)
 
   Sim(int X_, int Y_, int edge_, int prec_) {
     X = X_; Y = Y_; edge = edge_; prec = prec_;
@@ -264,6 +301,7 @@ template <class St> struct Sim : SimBase {
     for (int s = 0; s < 2; s++) for (int q = 0; q < 9; q++) f[s][q].assign(N, S());
     ux.assign(N, C(0)); uy.assign(N, C(0)); rho.assign(N, C(0));
     barrier.assign(N, 0);
+    ref.set((float)u_in, 0.0);
     if (edge == EDGE_REF) {  // init_barrier, lbm.rs:595-605
       for (int x = 0; x < X; x++) { barrier[(size_t)x] = 1; barrier[(size_t)x + (size_t)(Y - 1) * X] = 1; }
     }
@@ -271,13 +309,29 @@ template <class St> struct Sim : SimBase {
 
   void set_omega(double w) override { omega = (C)w; }
 
+  // A new inlet velocity is also the 16-bit storage's new reference state:
+  // every stored word (both sets, rest plane) is re-expressed against it,
+  // h' = of_f(f_of(h, old), new).  f32 / f64 store f_q and are unchanged.
+  void set_inlet_velocity(double u) override {
+    u_in = u;
+    if (!St::kDev || (float)u == ref.ux) return;
+    StoreRef nr;
+    nr.set((float)u, 0.0);
+    for (int s = 0; s < 2; s++)
+      for (int q = 0; q < 9; q++) {
+        if (s == 1 && q == 4) continue;
+        for (S& v : f[s][q]) v = St::of_f(St::f_of(v, q, ref), q, nr);
+      }
+    ref = nr;
+  }
+
   // Channel mode: the inlet column and solid cells are inert (never
   // collided); the reference mode collides every cell, solids included.
   bool frozen(size_t i) const { return edge == EDGE_CHANNEL && ((i % (size_t)X) == 0 || barrier[i] == 1); }
 
   void fill_cell(size_t i, const C eq[9]) {
     for (int q = 0; q < 9; q++) {
-      S v = St::of_f(eq[q], q);
+      S v = St::of_f(eq[q], q, ref);
       f[0][q][i] = v;
       f[1][q][i] = v;
     }
@@ -333,7 +387,7 @@ template <class St> struct Sim : SimBase {
     }
     if (dir >= 0) {
       size_t i = x + y * (size_t)X;
-      S v = St::of_f(C(4.0), dir);
+      S v = St::of_f(C(4.0), dir, ref);
       f[0][dir][i] = v; f[1][dir][i] = v;
     }
     set_inlet_columns();
@@ -376,12 +430,12 @@ template <class St> struct Sim : SimBase {
         float g[9];
         for (int q = 0; q < 9; q++) g[q] = St::load(q == 4 ? origin[i] : F[q][i], q);
         float r, dr, jxv, jyv;
-        moments_dev(g, r, dr, jxv, jyv);
+        moments_dev(g, r, dr, jxv, jyv, ref);
         ux[i] = jxv;
         uy[i] = jyv;
         rho[i] = r;
         if (frozen(i)) continue;
-        collide_dev(g, r, dr, jxv, jyv, (float)w);
+        collide_dev(g, r, dr, jxv, jyv, (float)w, ref);
         for (int q = 0; q < 9; q++) (q == 4 ? origin[i] : F[q][i]) = St::store(g[q], q);
       }
     } else {
@@ -469,7 +523,9 @@ template <class St> struct Sim : SimBase {
       for (int q = 0; q < 9; q++) {
         if (q == 4) continue;
         size_t j = upstream(i, q);
-        G[q][i] = barrier[j] == 1 ? F[8 - q][i] : F[q][j];
+        if (barrier[j] != 1) G[q][i] = F[q][j];
+        else if constexpr (St::kDev) G[q][i] = St::store(St::load(F[8 - q][i], 8 - q) + ref.bb[q], q);  // re-expressed
+        else G[q][i] = F[8 - q][i];
       }
     }
     step++;
@@ -483,7 +539,7 @@ template <class St> struct Sim : SimBase {
     const int cur = (int)(step % 2);
     for (int q = 0; q < 9; q++) {
       const std::vector<S>& src = (q == 4) ? f[0][4] : f[cur][q];
-      if (pops9) for (size_t i = 0; i < N; i++) pops9[(size_t)q * N + i] = (double)St::f_of(src[i], q);
+      if (pops9) for (size_t i = 0; i < N; i++) pops9[(size_t)q * N + i] = (double)St::f_of(src[i], q, ref);
     }
     for (size_t i = 0; i < N; i++) {
       if (r) r[i] = (double)rho[i];
@@ -518,7 +574,7 @@ template <class St> struct Sim : SimBase {
         if (q == 4) continue;
         if (barrier[upstream(i, q)] != 1) continue;
         const int p = 8 - q;
-        const double v = (double)St::f_of(P[p][i], p);
+        const double v = (double)St::f_of(P[p][i], p, ref);
         fx += 2.0 * v * CX[p];
         fy -= 2.0 * v * CY[p];
       }
@@ -561,7 +617,9 @@ orc_sim* orc_create(int X, int Y, double omega, int edge, int prec) {
 void orc_destroy(orc_sim* h) { delete (SimBase*)h; }
 void orc_set_threads(orc_sim* h, int t) { ((SimBase*)h)->threads = t < 1 ? 1 : t; }
 void orc_set_omega(orc_sim* h, double w) { ((SimBase*)h)->set_omega(w); }
-void orc_set_inlet(orc_sim* h, double u) { ((SimBase*)h)->u_in = u; }
+// The inlet velocity (and, for 16-bit storage, the reference state, which
+// re-expresses the stored words; lbm_set_inlet_velocity).
+void orc_set_inlet(orc_sim* h, double u) { ((SimBase*)h)->set_inlet_velocity(u); }
 void orc_init_equilibrium(orc_sim* h, double rho, double ux, double uy, double amp, uint64_t seed) {
   ((SimBase*)h)->init_equilibrium(rho, ux, uy, amp, seed);
 }
