@@ -344,9 +344,20 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     bands = (span + rows - 1) / rows;
   }
   a.rows = rows;
-  dim3 grid((s->L.nx + W - 1) / W, bands);
-  kern<<<grid, TPB, smem, s->stream>>>(a);
-  CK_LAUNCH();
+  // Programmatic dependent launch: the grid may be scheduled while the
+  // previous step's grid drains; the kernel waits for that grid to complete
+  // (griddepcontrol.wait) before it touches global memory.
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((s->L.nx + W - 1) / W, bands);
+  cfg.blockDim = dim3(TPB);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, a));
   return LBM_OK;
 }
 

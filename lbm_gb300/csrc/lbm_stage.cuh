@@ -523,6 +523,13 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NS];
   __shared__ __align__(8) uint64_t empty[NS];
+  // Launched with programmatic stream serialisation: let the next step's grid
+  // be scheduled now (its CTAs can only take the slots this grid's CTAs free,
+  // as every CTA of this one-wave grid is resident once it gets here), then
+  // wait until the previous grid has completed and its writes are visible.
+  // Nothing before this line reads or writes global memory.
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   const int xb = blockIdx.x * W;
   const int y0 = a.row0 + blockIdx.y * a.rows;
   const int y1 = min(y0 + a.rows, a.row_end);
