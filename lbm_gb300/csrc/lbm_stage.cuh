@@ -316,6 +316,69 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       act[j] = in_row[j] && xin[j] && yin && !(EDGE == EDGE_CHANNEL && own_solid);
       any_act |= act[j];
     }
+    // pulled populations of this thread's cells; every lane loads (stage
+    // indices stay inside the stage), lanes without an active cell discard them
+    C f[9][CPT];
+    if constexpr (CPT == 4) {
+      // 16-bit words, four consecutive cells: e is a multiple of 4, so each
+      // plane is read as aligned 8- and 4-byte words and the x-1 / x+1
+      // windows are assembled with byte permutes
+#pragma unroll
+      for (int q = 0; q < 9; q++) {
+        if (q == 4) continue;
+        const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+        const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+        const uint2 mid = *reinterpret_cast<const uint2*>(seg + e);  // columns x0 .. x0+3
+        uint32_t p0 = mid.x, p1 = mid.y;
+        // (the neighbour words are read as aligned 8-byte words too: a
+        // 4-byte read at an 8-byte lane stride would be 2-way bank-conflicted)
+        if (cx(q) > 0) {  // pull from x-1: columns x0-1 .. x0+2
+          const uint32_t left = reinterpret_cast<const uint2*>(seg + e - 4)->y;
+          p0 = __byte_perm(left, mid.x, 0x5432);
+          p1 = __byte_perm(mid.x, mid.y, 0x5432);
+        } else if (cx(q) < 0) {  // pull from x+1: columns x0+1 .. x0+4
+          const uint32_t right = reinterpret_cast<const uint2*>(seg + e + 4)->x;
+          p0 = __byte_perm(mid.x, mid.y, 0x5432);
+          p1 = __byte_perm(mid.y, right, 0x5432);
+        }
+        load_pair(seg, p0, f[q][0], f[q][1]);
+        load_pair(seg, p1, f[q][2], f[q][3]);
+      }
+      if (has_out) {  // the outflow column pulls its x+1 populations from its own column
+#pragma unroll
+        for (int q = 0; q < 9; q++) {
+          if (cx(q) >= 0) continue;
+          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+#pragma unroll
+          for (int j = 0; j < CPT; j++)
+            if (dxr[j] == 0) f[q][j] = St::load(seg[e + j], q);
+        }
+      }
+      const S* rest = reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes);
+      const uint2 rv = *reinterpret_cast<const uint2*>(rest + CPT * tid);
+      load_pair(rest, rv.x, f[4][0], f[4][1]);
+      load_pair(rest, rv.y, f[4][2], f[4][3]);
+    } else {
+#pragma unroll
+      for (int q = 0; q < 9; q++) {  // plain pulls
+        if (q == 4) continue;
+        const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
+        const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
+#pragma unroll
+        for (int j = 0; j < CPT; j++) {
+          const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);  // pull column offset
+          f[q][j] = St::load(seg[e + j + dx], q);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < CPT; j++)
+        f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
+    }
+    // this warp reads the oldest staged row no more: release it before the
+    // collisions, so the producer can refill it one row's work earlier
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
     if (CPT == 1 && EDGE == EDGE_REF && act[0] && ((w0 >> 1) & 1u)) {
       // reference mode: solids collide their own previous values (global memory)
       C f[9];
@@ -337,63 +400,6 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         if (q != 4) a.dstp[slot(q)][own] = St::store(f[q], q);
       a.rest[own] = St::store(f[4], 4);
     } else if (any_act) {
-      C f[9][CPT];
-      if constexpr (CPT == 4) {
-        // 16-bit words, four consecutive cells: e is a multiple of 4, so each
-        // plane is read as aligned 8- and 4-byte words and the x-1 / x+1
-        // windows are assembled with byte permutes
-#pragma unroll
-        for (int q = 0; q < 9; q++) {
-          if (q == 4) continue;
-          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
-          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
-          const uint2 mid = *reinterpret_cast<const uint2*>(seg + e);  // columns x0 .. x0+3
-          uint32_t p0 = mid.x, p1 = mid.y;
-          // (the neighbour words are read as aligned 8-byte words too: a
-          // 4-byte read at an 8-byte lane stride would be 2-way bank-conflicted)
-          if (cx(q) > 0) {  // pull from x-1: columns x0-1 .. x0+2
-            const uint32_t left = reinterpret_cast<const uint2*>(seg + e - 4)->y;
-            p0 = __byte_perm(left, mid.x, 0x5432);
-            p1 = __byte_perm(mid.x, mid.y, 0x5432);
-          } else if (cx(q) < 0) {  // pull from x+1: columns x0+1 .. x0+4
-            const uint32_t right = reinterpret_cast<const uint2*>(seg + e + 4)->x;
-            p0 = __byte_perm(mid.x, mid.y, 0x5432);
-            p1 = __byte_perm(mid.y, right, 0x5432);
-          }
-          load_pair(seg, p0, f[q][0], f[q][1]);
-          load_pair(seg, p1, f[q][2], f[q][3]);
-        }
-        if (has_out) {  // the outflow column pulls its x+1 populations from its own column
-#pragma unroll
-          for (int q = 0; q < 9; q++) {
-            if (cx(q) >= 0) continue;
-            const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
-            const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
-#pragma unroll
-            for (int j = 0; j < CPT; j++)
-              if (dxr[j] == 0) f[q][j] = St::load(seg[e + j], q);
-          }
-        }
-        const S* rest = reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes);
-        const uint2 rv = *reinterpret_cast<const uint2*>(rest + CPT * tid);
-        load_pair(rest, rv.x, f[4][0], f[4][1]);
-        load_pair(rest, rv.y, f[4][2], f[4][3]);
-      } else {
-#pragma unroll
-        for (int q = 0; q < 9; q++) {  // plain pulls
-          if (q == 4) continue;
-          const unsigned char* st = cy(q) < 0 ? sp : (cy(q) > 0 ? sm : s0);
-          const S* seg = reinterpret_cast<const S*>(st + slot(q) * G::kSegBytes);
-#pragma unroll
-          for (int j = 0; j < CPT; j++) {
-            const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);  // pull column offset
-            f[q][j] = St::load(seg[e + j + dx], q);
-          }
-        }
-#pragma unroll
-        for (int j = 0; j < CPT; j++)
-          f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
-      }
       if (near_solid) {  // half-way bounce-back: upstream solid -> own opposite population
 #pragma unroll
         for (int q = 0; q < 9; q++) {
@@ -498,9 +504,6 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         step_cell<St, EDGE>(a, x0 + j, y);
       }
     }
-    // the oldest staged row is no longer needed by this warp
-    __syncwarp();
-    if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
     wa = w0;
     w0 = wn;
     slot_m = slot_0;
