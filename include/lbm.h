@@ -45,8 +45,11 @@ typedef struct lbm_sim lbm_sim;
 
 /* population storage */
 #define LBM_STORE_F32 0
-#define LBM_STORE_F16 1    /* binary16 deviations f_i - w_i, f32 arithmetic */
-#define LBM_STORE_BF16 2   /* bfloat16 deviations f_i - w_i, f32 arithmetic */
+/* The 16-bit modes store the deviation of each population from the
+ * equilibrium of the lattice's inlet velocity, f_i - f_i^eq(1, (u_in, 0)),
+ * and collide in f32 arithmetic.  The inlet velocity is 0.1 at creation. */
+#define LBM_STORE_F16 1    /* binary16 deviations, f32 arithmetic */
+#define LBM_STORE_BF16 2   /* bfloat16 deviations, f32 arithmetic */
 #define LBM_STORE_F64 3    /* f64 storage and arithmetic (oracle-grade runs) */
 
 /* readback fields (lbm_read_field) */
@@ -130,7 +133,10 @@ int lbm_set_viscosity(lbm_sim* sim, float nu);
 /* custom_speed (lbm.rs:1090-1102) when reset_field != 0: the whole field is
  * re-initialised to set_equil(ux, 0, 1) and the step count restarts at 0.
  * With reset_field == 0 only the inlet changes: in LBM_EDGE_CHANNEL the frozen
- * inlet column, in LBM_EDGE_REF column 0 (its de-facto inlet). */
+ * inlet column, in LBM_EDGE_REF column 0 (its de-facto inlet).  In the 16-bit
+ * modes the inlet velocity is also the storage's reference state: a new one
+ * without a reset re-expresses every stored word against it (one pass over
+ * both buffer sets; its rounding is part of the state). */
 int lbm_set_inlet_velocity(lbm_sim* sim, float ux, int reset_field);
 
 /* reset_to_equilibrium (lbm.rs:1076-1088): set_equil(0.1, 0, 1) everywhere. */
@@ -247,7 +253,9 @@ int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy,
  * in the reference, which runs one lattice on one adapter).  Copies rows
  * y .. y + nrows - 1 of the moving-population planes selected by slot_mask
  * (bit s = slot s: 0 nw, 1 n, 2 ne, 3 w, 4 e, 5 sw, 6 s, 7 se) of the state
- * the next step pulls from, in the storage's own words (4, 2 or 8 bytes),
+ * the next step pulls from, in the storage's own words (4, 2 or 8 bytes;
+ * 16-bit words are relative to the lattice's inlet velocity, so lattices
+ * that exchange rows must share it),
  * planes in slot order, each nrows * nx words row-major.  on_device != 0:
  * `out` / `in` is device memory and the copy is queued on the lattice's
  * stream; otherwise host memory and the call synchronises. */
