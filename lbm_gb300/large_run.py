@@ -36,7 +36,11 @@ from . import EDGE_CHANNEL, F16, F32, LBMError, Lattice, _check, load_library
 from .geometry import random_circles
 
 
-def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, drift=1.0, seed=1):
+def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, drift=1.0, seed=1, ramp=0):
+    """One run (see the module docstring).  ramp > 0 starts the fluid at rest
+    and raises the inlet velocity linearly to u over the first `ramp` steps
+    (lbm_set_inlet_velocity between samples, outside the timing) instead of
+    starting the whole field at u."""
     import torch
     lib = load_library()
     stream = torch.cuda.Stream()
@@ -44,11 +48,12 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
     acc = torch.zeros((2, ny, nx), dtype=torch.float32, device=dev)
     tmp = torch.empty((ny, nx), dtype=torch.float32, device=dev)
     active = int((mask[:, 1:] == 0).sum())
-    out = {"storage": "f32" if storage == F32 else "f16", "closure": params is not None}
+    out = {"storage": "f32" if storage == F32 else "f16", "closure": params is not None, "ramp": ramp}
     with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
         lat.set_stream(stream.cuda_stream)
-        lat.set_inlet_velocity(u)
-        lat.init_equilibrium(1.0, u, 0.0, 1e-4, seed)
+        u0 = 0.0 if ramp else u
+        lat.set_inlet_velocity(u0)
+        lat.init_equilibrium(1.0, u0, 0.0, 1e-4, seed)
         lat.draw_mask(mask)
         if params is not None:
             p = np.ascontiguousarray(params, np.float32)
@@ -73,6 +78,8 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
             torch.cuda.synchronize()
             dev_ms += e0.elapsed_time(e1)
             done += k
+            if ramp and done - k < ramp:
+                lat.set_inlet_velocity(u * min(1.0, done / ramp))
             if first_bad is None:  # the step kernels' non-finite flag, outside the timing
                 try:
                     lat.synchronize()
@@ -147,7 +154,22 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
                 done += c
                 k -= c
 
-        advance(start - 1)
+        # growth before the failure: the lowest density and the largest speed
+        # over the fluid, every `every` / 5 steps from the start
+        history = []
+        hstep = max(every // 5, 1)
+        while done + hstep <= start:
+            advance(hstep)
+            with torch.cuda.stream(stream):
+                rho = _field(lat, lib, 0, tmp).clone()
+                spd = _field(lat, lib, 7, tmp).clone()
+                rr = torch.where(fl, rho, torch.full_like(rho, float("inf")))
+                sp = torch.where(fl & torch.isfinite(spd), spd, torch.zeros_like(spd))
+            torch.cuda.synchronize()
+            i_sp, i_rho = int(torch.argmax(sp)), int(torch.argmin(rr))
+            history.append([done, round(float(rr.view(-1)[i_rho]), 6), [i_rho % nx, i_rho // nx],
+                            round(float(sp.view(-1)[i_sp]), 6), [i_sp % nx, i_sp // nx]])
+        advance(start - done)
         prev = None
         while done < first_bad + 1:
             with torch.cuda.stream(stream):  # the reads are queued on the lattice's stream
@@ -178,7 +200,8 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
                "x_range": [int(xs.min()), int(xs.max())], "y_range": [int(ys.min()), int(ys.max())],
                "distance_to_inlet": int(xs.min()), "distance_to_outflow": int(nx - 1 - xs.max()),
                "distance_to_nearest_solid": [float(d.min()), float(np.median(d)), float(d.max())],
-               "state_one_step_earlier": prev}
+               "state_one_step_earlier": prev,
+               "history (step, min rho, at, max speed, at)": history}
     return rep
 
 
@@ -194,6 +217,8 @@ def main(argv=None):
     ap.add_argument("--drift", type=float, default=1.0, help="closure drift bound (multiples of the predicted |u|)")
     ap.add_argument("--closure-only", action="store_true", help="skip the plain f32 and f16 runs")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--ramp", type=int, default=0,
+                    help="start at rest and raise the inlet velocity to --u over this many steps")
     ap.add_argument("--diagnose", action="store_true",
                     help="for each run that goes non-finite, locate the first non-finite step and cells")
     a = ap.parse_args(argv)
@@ -214,20 +239,20 @@ def main(argv=None):
         return float(np.linalg.norm(d) / np.linalg.norm(u32[:, fl])) if np.isfinite(d).all() else float("inf")
 
     def diag(r, storage, params=None):
-        if a.diagnose and r["first_nonfinite_by_step"] is not None:
+        if a.diagnose and r["first_nonfinite_by_step"] is not None and not a.ramp:
             r["diagnosis"] = diagnose(nx, ny, a.tau, a.u, mask, storage, r["first_nonfinite_by_step"], a.every,
                                       params=params, refresh=a.refresh, drift=a.drift, seed=a.seed)
 
     if not a.closure_only:
-        r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed)
+        r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed, ramp=a.ramp)
         diag(r32, F32)
-        r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed)
+        r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed, ramp=a.ramp)
         diag(r16, F16)
         r16["vel_err_vs_f32"] = err(u16)
         rep["runs"] = [r32, r16]
     if a.closure:
         params = np.load(a.closure)["params"]
-        rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh,
+        rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh, ramp=a.ramp,
                      drift=a.drift, seed=a.seed)
         diag(rc, F16, params)
         rc["vel_err_vs_f32"] = err(uc)
