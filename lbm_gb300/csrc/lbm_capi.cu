@@ -910,12 +910,20 @@ static int read_field(lbm_sim* s, int field, float* out, bool device_out) {
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
   float* mapped = device_out ? nullptr : (float*)mapped_host(out);
   float* tmp = device_out ? out : (mapped ? mapped : s->staging_d);
-  if (s->storage == STORE_F64)
-    k_field<double><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const double*)mom_plane(s, 0),
-                                                    (const double*)mom_plane(s, 1), (const double*)mom_plane(s, 2), tmp);
-  else
-    k_field<float><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, (const float*)mom_plane(s, 0),
-                                                   (const float*)mom_plane(s, 1), (const float*)mom_plane(s, 2), tmp);
+  // four cells per thread (16-byte stores) where rows and the output allow it
+  const bool v4 = s->L.nx % 4 == 0 && ((uintptr_t)tmp & 15u) == 0;
+  dim3 grid4((s->L.nx / 4 + kBlockX - 1) / kBlockX, s->L.ny);
+  if (s->storage == STORE_F64) {
+    const double *r = (const double*)mom_plane(s, 0), *jx = (const double*)mom_plane(s, 1),
+                 *jy = (const double*)mom_plane(s, 2);
+    if (v4) k_field4<double><<<grid4, kBlockX, 0, s->stream>>>(s->L, s->edge, field, r, jx, jy, tmp);
+    else k_field<double><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, r, jx, jy, tmp);
+  } else {
+    const float *r = (const float*)mom_plane(s, 0), *jx = (const float*)mom_plane(s, 1),
+                *jy = (const float*)mom_plane(s, 2);
+    if (v4) k_field4<float><<<grid4, kBlockX, 0, s->stream>>>(s->L, s->edge, field, r, jx, jy, tmp);
+    else k_field<float><<<grid, kBlockX, 0, s->stream>>>(s->L, s->edge, field, r, jx, jy, tmp);
+  }
   CK_LAUNCH();
   s->launches++;
   if (device_out) return LBM_OK;
@@ -978,12 +986,18 @@ static int write_pops(lbm_sim* s, const void* in, bool f64) {
     src = s->staging_d;
   }
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  // f32 input: four cells per thread (16-byte loads) where rows and the input allow it
+  const bool v4 = !f64 && s->L.nx % 4 == 0 && ((uintptr_t)src & 15u) == 0;
+  dim3 grid4((s->L.nx / 4 + kBlockX - 1) / kBlockX, s->L.ny);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
     if (f64)
       k_write_pops<St, double><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
                                                                  (const double*)src, store_ref(s));
+    else if (v4)
+      k_write_pops4<St><<<grid4, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
+                                                           (const float*)src, store_ref(s));
     else
       k_write_pops<St, float><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest,
                                                                 (const float*)src, store_ref(s));

@@ -17,11 +17,12 @@ pytestmark = pytest.mark.gpu
 
 
 @pytest.mark.parametrize("storage", [0, 1, 3])
-def test_gpu_pinned_and_pageable_transfers_agree(lbm, cuda_ok, storage):
+@pytest.mark.parametrize("nx", [203, 204])  # 204: rows of whole 16-byte words, read and written four cells at a time
+def test_gpu_pinned_and_pageable_transfers_agree(lbm, cuda_ok, storage, nx):
     import torch
     L = lbm.load_library()
     from lbm_gb300 import geometry
-    nx, ny = 203, 77
+    ny = 77
     mask = geometry.random_layout(nx, ny, 0.08, 3, rmin=2.0, inlet_clearance=6)
     src = lbm.Lattice(nx, ny, 1.0 / 0.6, lbm.EDGE_CHANNEL, storage)
     src.set_inlet_velocity(0.06)
