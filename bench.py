@@ -163,11 +163,14 @@ def workload_mask():
     return geometry.random_circles(NX, NY, NCIRC, 4, 32, seed=SEED, inlet_clearance=64)
 
 
-def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0):
+def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0, store_inlet=True):
     """Device-resident MLUPS of one storage format, timed like `value` (the
     K-step call made untimed first, then repeated for `min_seconds`, median
-    call); returns (ms_per_step, launches per call)."""
+    call); returns (ms_per_step, launches per call).  store_inlet=False keeps
+    16-bit words relative to the rest weights (lbm_set_storage_reference 0)."""
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, storage)
+    if not store_inlet:
+        lat.set_storage_reference(False)
     stream = torch.cuda.Stream()
     lat.set_stream(stream.cuda_stream)
     lat.set_inlet_velocity(UX)
@@ -260,8 +263,9 @@ def time_slab(lbm, torch, steps, warmup, min_seconds, rank=0, world=1, dist=None
 
 def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     """Storage precision on the 4096 x 2048 workload: the same seeded run in
-    f64 (the GPU's FP64 run is the reference), f32, f16 (f - w) and bf16
-    (f - w) for `steps` steps.  For each: the relative L2 error over fluid
+    f64 (the GPU's FP64 run is the reference), f32, f16 and bf16 (words
+    relative to the inlet equilibrium) and f16_rest / bf16_rest (relative to
+    the rest weights) for `steps` steps.  For each: the relative L2 error over fluid
     cells, against f64, of the velocity at step `short` (before the unsteady
     wake amplifies rounding differences into different vortex trajectories),
     of the velocity time-averaged over the second half (samples every `every`
@@ -277,13 +281,14 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     fl[:, 0] = False  # the inlet column is set, not computed
     tmp = torch.empty((NY, NX), dtype=torch.float32, device=dev)
     runs = {}
-    for name, st in (("f64", lbm.F64), ("f32", lbm.F32), ("f16", lbm.F16), ("bf16", lbm.BF16)):
+    for name, st, inlet in STORAGE_RUNS:
         stream = torch.cuda.Stream()
         acc = torch.zeros((2, NY, NX), dtype=torch.float64, device=dev)
         fin = torch.empty((2, NY, NX), dtype=torch.float64, device=dev)
         early = torch.empty((2, NY, NX), dtype=torch.float64, device=dev)
         n_avg = 0
         with lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, st) as lat:
+            lat.set_storage_reference(inlet)
             lat.set_stream(stream.cuda_stream)
             lat.set_inlet_velocity(UX)
             lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
@@ -335,6 +340,10 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     return out
 
 
+# (name, storage, 16-bit words relative to the inlet equilibrium)
+STORAGE_RUNS = (("f64", 3, True), ("f32", 0, True), ("f16", 1, True), ("bf16", 2, True), ("f16_rest", 1, False),
+                ("bf16_rest", 2, False))
+
 STEADY = {"nx": 1024, "ny": 512, "cx": 256, "cy": 256, "r": 24, "ux": 0.05, "tau": 0.8}
 
 
@@ -355,9 +364,10 @@ def steady_precision(lbm, steps=20000, every=1000):
     fl = mask == 0
     fl[:, 0] = False
     res = {}
-    for name, st in (("f64", lbm.F64), ("f32", lbm.F32), ("f16", lbm.F16), ("bf16", lbm.BF16)):
+    for name, st, inlet in STORAGE_RUNS:
         acc, n = 0.0, 0
         with lbm.Lattice(c["nx"], c["ny"], 1.0 / c["tau"], lbm.EDGE_CHANNEL, st) as lat:
+            lat.set_storage_reference(inlet)
             lat.set_inlet_velocity(c["ux"])
             lat.init_equilibrium(1.0, c["ux"], 0.0, 0.0, 0)
             lat.draw_mask(mask)
@@ -376,7 +386,7 @@ def steady_precision(lbm, steps=20000, every=1000):
 
     out = {"workload": "steady cylinder wake (Re 24): 1024x512 channel, r 24, tau 0.8, ux 0.05, %d steps" % steps,
            "reference": "f64 storage on the GPU"}
-    for name in ("f32", "f16", "bf16"):
+    for name in ("f32", "f16", "bf16", "f16_rest", "bf16_rest"):
         out[name] = {"rel_err_final_velocity": _finite_or_str(rel(res[name][0], res["f64"][0]), 7),
                      "rel_err_time_avg_velocity": _finite_or_str(rel(res[name][1], res["f64"][1]), 7)}
     return out
@@ -468,7 +478,8 @@ def run_ours(args):
         return
     if args.kernel_only:
         st = {"f32": lbm.F32, "f16": lbm.F16, "bf16": lbm.BF16, "f64": lbm.F64}[args.kernel_only]
-        ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds)
+        ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds,
+                                    not args.rest_reference)
         gbs = BYTES_PER_CELL[args.kernel_only] * active / (ms * 1e-3) / 1e9
         print(json.dumps({"kernel_only": args.kernel_only, "ms_per_step": round(ms, 5),
                           "mlups": round(n / (ms * 1e-3) / 1e6, 1), "achieved_gbs": round(gbs, 1),
@@ -563,9 +574,9 @@ def run_ours(args):
     # --- storage variants (same workload) -----------------------------------------
     variants = {}
     if not args.no_variants:
-        for name, st in (("f16", lbm.F16), ("bf16", lbm.BF16)):
-            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds)
-            gbs = BYTES_PER_CELL[name] * active / (vms * 1e-3) / 1e9
+        for name, st, inlet in STORAGE_RUNS[2:]:
+            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds, inlet)
+            gbs = BYTES_PER_CELL[name.split("_")[0]] * active / (vms * 1e-3) / 1e9
             variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
                               "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
 
@@ -797,6 +808,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--min-seconds", type=float, default=1.0,
                     help="repeat the timed K-step call until this much wall time has passed (median reported)")
+    ap.add_argument("--rest-reference", action="store_true",
+                    help="with --kernel-only f16 / bf16: words relative to the rest weights")
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
                     help="time only the step kernel of one storage format (profiling runs)")
     ap.add_argument("--case", choices=["batched64", "closure2048"], default=None,

@@ -139,6 +139,16 @@ int lbm_set_viscosity(lbm_sim* sim, float nu);
  * both buffer sets; its rounding is part of the state). */
 int lbm_set_inlet_velocity(lbm_sim* sim, float ux, int reset_field);
 
+/* 16-bit storage only (no reference counterpart: the reference stores f32).
+ * inlet = 1 (the default) keeps the words relative to the inlet equilibrium,
+ * which makes them small wherever the flow is near the inlet velocity;
+ * inlet = 0 keeps them relative to the rest weights w_q, whose collision
+ * needs one product fewer per direction (faster, coarser in a moving flow).
+ * Switching re-expresses the stored state, like a new inlet velocity; a
+ * no-op for f32 / f64.  The setting travels with checkpoints. */
+int lbm_set_storage_reference(lbm_sim* sim, int inlet);
+int lbm_get_storage_reference(const lbm_sim* sim, int* inlet);
+
 /* reset_to_equilibrium (lbm.rs:1076-1088): set_equil(0.1, 0, 1) everywhere. */
 int lbm_reset_to_equilibrium(lbm_sim* sim);
 

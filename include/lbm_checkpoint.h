@@ -5,7 +5,8 @@
  * state, so that a lattice loaded from it continues bit for bit as the saved
  * one would have: both buffer sets and the rest plane in their storage words
  * (f32, f64, or the 16-bit words relative to the equilibrium of the saved
- * inlet velocity u_in), which buffer is current and whether
+ * inlet velocity u_in, or to the rest weights when store_inlet is 0), which
+ * buffer is current and whether
  * it is materialised, the step count, omega, the inlet velocity, the solid
  * mask and, when the learned closure is on, its per-cell records.
  *
@@ -13,7 +14,8 @@
  *   char magic[8] = "LBMGB3CK"; u32 version = 2, nx, ny; i32 edge, storage;
  *   f32 omega, u_in, drift; u64 steps; u32 cur, materialised, closure,
  *   elem_bytes; u64 payload_bytes; u32 crc32 (zlib's CRC-32 of the header
- *   with this field zero, continued over the payload); u32 reserved[5]
+ *   with this field zero, continued over the payload); u32 store_inlet
+ *   (lbm_set_storage_reference); u32 reserved[4]
  * then the payload, every plane dense row-major (nx * ny, row 0 first):
  *   mask (u8 per cell); buffer 0 (8 planes, direction slots 0..3 = nw, n, ne,
  *   w and 4..7 = e, sw, s, se); buffer 1 (8 planes); rest plane; closure
@@ -35,7 +37,7 @@ int lbm_checkpoint_size(const lbm_sim* sim, size_t* bytes);
 int lbm_checkpoint_save(lbm_sim* sim, void* buf, size_t len);
 /* From a buffer; LBM_ERR_ARG, before any device work, on a size / mode
  * mismatch, a CRC error, or a header field out of range (cur, materialised
- * and closure must be 0 or 1; omega in (0, 2); u_in finite; drift finite and
+ * closure and store_inlet must be 0 or 1; omega in (0, 2); u_in finite; drift finite and
  * > 0). */
 int lbm_checkpoint_load(lbm_sim* sim, const void* buf, size_t len);
 /* The same through a file. */

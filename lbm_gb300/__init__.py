@@ -72,6 +72,8 @@ _SIGS = [
     ("lbm_set_omega", ctypes.c_int, [_P, ctypes.c_float]),
     ("lbm_set_viscosity", ctypes.c_int, [_P, ctypes.c_float]),
     ("lbm_set_inlet_velocity", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
+    ("lbm_set_storage_reference", ctypes.c_int, [_P, ctypes.c_int]),
+    ("lbm_get_storage_reference", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     ("lbm_reset_to_equilibrium", ctypes.c_int, [_P]),
     ("lbm_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_uint64]),
@@ -246,6 +248,20 @@ class Lattice:
 
     def set_inlet_velocity(self, ux, reset_field=False):
         _check(_lib.lbm_set_inlet_velocity(self._h, float(ux), 1 if reset_field else 0))
+
+    def set_storage_reference(self, inlet):
+        """16-bit storage: keep the words relative to the inlet equilibrium
+        (True, the default: smaller words in a flow near the inlet velocity)
+        or to the rest weights (False: one product fewer per direction in
+        the collision).  The stored state is re-expressed; f32 / f64 storage
+        is unaffected."""
+        _check(_lib.lbm_set_storage_reference(self._h, 1 if inlet else 0))
+
+    @property
+    def storage_reference(self):
+        v = ctypes.c_int()
+        _check(_lib.lbm_get_storage_reference(self._h, ctypes.byref(v)))
+        return bool(v.value)
 
     def reset_to_equilibrium(self):
         _check(_lib.lbm_reset_to_equilibrium(self._h))

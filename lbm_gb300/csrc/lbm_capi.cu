@@ -71,11 +71,13 @@ constexpr int kRunGraphMax = 64; // longest call captured whole
 
 struct StepGraphKey {
   float omega = 0.0f, drift = 0.0f, u_in = 0.0f;
+  bool store_inlet = true;
   int kernel = -1, rows = 0, bands = 0, staged_rows = 0;
   const void* closure = nullptr;
   cudaStream_t stream = nullptr;
   bool operator==(const StepGraphKey& o) const {
-    return omega == o.omega && drift == o.drift && u_in == o.u_in && kernel == o.kernel && rows == o.rows &&
+    return omega == o.omega && drift == o.drift && u_in == o.u_in && store_inlet == o.store_inlet &&
+           kernel == o.kernel && rows == o.rows &&
            bands == o.bands &&
            staged_rows == o.staged_rows && closure == o.closure && stream == o.stream;
   }
@@ -85,6 +87,7 @@ struct lbm_sim {
   int device = 0;
   int edge = 0, storage = 0;
   float omega = 1.0f, u_in = 0.1f;
+  bool store_inlet = true;  // 16-bit words relative to the inlet equilibrium (else to the rest weights)
   Layout L{};
   size_t es = 4;   // bytes per stored population
   size_t cs = 4;   // bytes of the arithmetic type (moments)
@@ -141,7 +144,7 @@ namespace {
 void* mom_plane(lbm_sim* s, int k) { return (char*)s->mom + (size_t)k * s->L.ps * s->cs; }
 
 // Reference state of 16-bit storage: the inlet velocity, and the lattice's omega.
-StoreRef store_ref(const lbm_sim* s) { return make_store_ref(s->u_in, s->omega); }
+StoreRef store_ref(const lbm_sim* s) { return make_store_ref(s->store_inlet ? s->u_in : 0.0f, s->omega); }
 
 template <class F> int dispatch_storage(int storage, F&& f) {
   switch (storage) {
@@ -151,6 +154,24 @@ template <class F> int dispatch_storage(int storage, F&& f) {
     case STORE_F64: return f(StF64{});
   }
   return fail(LBM_ERR_ARG, "bad storage %d", storage);
+}
+
+// Re-express every stored 16-bit word (both sets, rest plane) from reference
+// `from` to reference `to`; f32 / f64 storage is unaffected.
+int rebase(lbm_sim* s, const StoreRef& from, const StoreRef& to) {
+  if (s->storage != STORE_F16 && s->storage != STORE_BF16) return LBM_OK;
+  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  auto launch = [&](auto tag) -> int {
+    using St = decltype(tag);
+    using S = typename St::S;
+    if constexpr (St::kDev) {
+      k_rebase<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, from, to);
+      CK_LAUNCH();
+      s->launches++;
+    }
+    return LBM_OK;
+  };
+  return dispatch_storage(s->storage, launch);
 }
 
 void pack_words(lbm_sim* s, uint32_t y0, uint32_t y1) {
@@ -634,21 +655,14 @@ int lbm_set_inlet_velocity(lbm_sim* s, float ux, int reset_field) {
   int rc = materialise(s);
   if (rc) return rc;
   const StoreRef from = store_ref(s);
-  const bool rebase = (s->storage == STORE_F16 || s->storage == STORE_BF16) && ux != s->u_in;
+  const bool moved = s->store_inlet && ux != s->u_in;
   s->u_in = ux;
   const StoreRef to = store_ref(s);
-  dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
+  if (moved && (rc = rebase(s, from, to))) return rc;
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
     using S = typename St::S;
     using C = typename St::C;
-    if constexpr (St::kDev) {
-      if (rebase) {
-        k_rebase<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, from, to);
-        CK_LAUNCH();
-        s->launches++;
-      }
-    }
     k_inlet<St><<<(s->L.ny + 127) / 128, 128, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)ux,
                                                                to);
     CK_LAUNCH();
@@ -657,6 +671,23 @@ int lbm_set_inlet_velocity(lbm_sim* s, float ux, int reset_field) {
   rc = dispatch_storage(s->storage, launch);
   if (!rc) s->launches++;
   return rc;
+}
+
+int lbm_set_storage_reference(lbm_sim* s, int inlet) {
+  CHECK_SIM(s);
+  if (inlet != 0 && inlet != 1) return fail(LBM_ERR_ARG, "storage reference %d: 1 inlet equilibrium, 0 rest weights", inlet);
+  if ((inlet != 0) == s->store_inlet) return LBM_OK;
+  int rc = materialise(s);
+  if (rc) return rc;
+  const StoreRef from = store_ref(s);
+  s->store_inlet = inlet != 0;
+  return rebase(s, from, store_ref(s));
+}
+
+int lbm_get_storage_reference(const lbm_sim* s, int* inlet) {
+  if (!s || !inlet) return fail(LBM_ERR_ARG, "null argument");
+  *inlet = s->store_inlet ? 1 : 0;
+  return LBM_OK;
 }
 
 int lbm_reset_to_equilibrium(lbm_sim* s) {
@@ -761,6 +792,7 @@ static StepGraphKey graph_key(const lbm_sim* s) {
   StepGraphKey k;
   k.omega = s->omega;
   k.u_in = s->u_in;
+  k.store_inlet = s->store_inlet;
   k.kernel = s->kernel;
   k.rows = s->rows;
   k.closure = s->closure_on ? (const void*)s->closure_d : nullptr;
@@ -1298,7 +1330,9 @@ struct CkHeader {  // 96 bytes, little-endian, written as is
   uint64_t steps;
   uint32_t cur, materialised, closure, elem_bytes;
   uint64_t payload_bytes;
-  uint32_t crc32, reserved[5];  // crc32: over the header (with this field zero), then the payload
+  uint32_t crc32;  // over the header (with this field zero), then the payload
+  uint32_t store_inlet;  // 16-bit words relative to the inlet equilibrium (1) or the rest weights (0)
+  uint32_t reserved[4];
 };
 static_assert(sizeof(CkHeader) == 96, "checkpoint header layout");
 
@@ -1377,6 +1411,7 @@ int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
   h.materialised = s->materialised ? 1u : 0u;
   h.closure = closure ? 1u : 0u;
   h.elem_bytes = (uint32_t)e;
+  h.store_inlet = s->store_inlet ? 1u : 0u;
   h.payload_bytes = need - sizeof(CkHeader);
   uint8_t* p = (uint8_t*)buf + sizeof(CkHeader);
   std::memcpy(p, s->mask_h.data(), cells);
@@ -1404,9 +1439,9 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
                 h.edge, h.storage, s->L.nx, s->L.ny, s->edge, s->storage);
   // Every header field that steers device work is checked before any of it:
   // `cur` selects a buffer set, so anything but 0 or 1 would index past them.
-  if (h.cur > 1u || h.materialised > 1u || h.closure > 1u)
-    return fail(LBM_ERR_ARG, "checkpoint header: cur %u, materialised %u, closure %u (each must be 0 or 1)", h.cur,
-                h.materialised, h.closure);
+  if (h.cur > 1u || h.materialised > 1u || h.closure > 1u || h.store_inlet > 1u)
+    return fail(LBM_ERR_ARG, "checkpoint header: cur %u, materialised %u, closure %u, storage reference %u (each "
+                "must be 0 or 1)", h.cur, h.materialised, h.closure, h.store_inlet);
   if (!(h.omega > 0.0f && h.omega < 2.0f) || !std::isfinite(h.u_in) || !(h.drift > 0.0f) || !std::isfinite(h.drift))
     return fail(LBM_ERR_ARG, "checkpoint header: omega %g, inlet %g, drift %g out of range", (double)h.omega,
                 (double)h.u_in, (double)h.drift);
@@ -1434,6 +1469,7 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
   CK(cudaStreamSynchronize(s->stream));
   s->omega = h.omega;
   s->u_in = h.u_in;
+  s->store_inlet = h.store_inlet != 0;
   s->drift = h.drift;
   s->closure_on = closure;
   s->steps = h.steps;

@@ -274,9 +274,11 @@ struct SimBase {
   size_t N = 0;
   uint64_t step = 0;                 // compute_step, lbm.rs:1115
   double u_in = 0.1;                 // channel inlet velocity (and the 16-bit storage reference)
+  bool store_inlet = true;           // 16-bit words relative to (u_in, 0); false: to the rest weights
   std::vector<uint8_t> barrier;      // 1 = solid (the reference's u32 barrier buffer)
   virtual void set_omega(double w) = 0;
   virtual void set_inlet_velocity(double u) = 0;
+  virtual void set_storage_reference(bool inlet) = 0;
   virtual void init_equilibrium(double rho, double ux, double uy, double amp, uint64_t seed) = 0;
   virtual void single_cell(int dir) = 0;
   virtual void set_inlet_columns(bool any_mode = false) = 0;
@@ -309,20 +311,30 @@ template <class St> struct Sim : SimBase {
 
   void set_omega(double w) override { omega = (C)w; }
 
-  // A new inlet velocity is also the 16-bit storage's new reference state:
-  // every stored word (both sets, rest plane) is re-expressed against it,
-  // h' = of_f(f_of(h, old), new).  f32 / f64 store f_q and are unchanged.
-  void set_inlet_velocity(double u) override {
-    u_in = u;
-    if (!St::kDev || (float)u == ref.ux) return;
+  // Re-express every stored word (both sets, rest plane) against the
+  // reference at (vx, 0): h' = of_f(f_of(h, old), new).  f32 / f64 store f_q
+  // and are unchanged.
+  void rebase(float vx) {
+    if (!St::kDev || vx == ref.ux) return;
     StoreRef nr;
-    nr.set((float)u, 0.0);
+    nr.set(vx, 0.0);
     for (int s = 0; s < 2; s++)
       for (int q = 0; q < 9; q++) {
         if (s == 1 && q == 4) continue;
         for (S& v : f[s][q]) v = St::of_f(St::f_of(v, q, ref), q, nr);
       }
     ref = nr;
+  }
+  // A new inlet velocity is also the 16-bit storage's new reference state
+  // (unless the words are kept relative to the rest weights).
+  void set_inlet_velocity(double u) override {
+    u_in = u;
+    if (store_inlet) rebase((float)u);
+  }
+  // lbm_set_storage_reference: words relative to (u_in, 0) or to the rest weights.
+  void set_storage_reference(bool inlet) override {
+    store_inlet = inlet;
+    rebase(inlet ? (float)u_in : 0.0f);
   }
 
   // Channel mode: the inlet column and solid cells are inert (never
@@ -620,6 +632,7 @@ void orc_set_omega(orc_sim* h, double w) { ((SimBase*)h)->set_omega(w); }
 // The inlet velocity (and, for 16-bit storage, the reference state, which
 // re-expresses the stored words; lbm_set_inlet_velocity).
 void orc_set_inlet(orc_sim* h, double u) { ((SimBase*)h)->set_inlet_velocity(u); }
+void orc_set_storage_reference(orc_sim* h, int inlet) { ((SimBase*)h)->set_storage_reference(inlet != 0); }
 void orc_init_equilibrium(orc_sim* h, double rho, double ux, double uy, double amp, uint64_t seed) {
   ((SimBase*)h)->init_equilibrium(rho, ux, uy, amp, seed);
 }

@@ -59,6 +59,7 @@ def lib():
         L.orc_set_threads.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_set_omega.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_set_inlet.argtypes = [ctypes.c_void_p, ctypes.c_double]
+        L.orc_set_storage_reference.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_init_equilibrium.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_uint64]
         L.orc_single_cell.argtypes = [ctypes.c_void_p, ctypes.c_int]
@@ -115,6 +116,10 @@ class Oracle:
         lib().orc_set_inlet(self.h, u)
         if apply:
             lib().orc_apply_inlet(self.h)
+
+    def set_storage_reference(self, inlet):
+        """16-bit words relative to the inlet equilibrium (True) or the rest weights."""
+        lib().orc_set_storage_reference(self.h, 1 if inlet else 0)
 
     def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
         lib().orc_init_equilibrium(self.h, rho, ux, uy, noise, seed)

@@ -128,7 +128,7 @@ def _forge(ck, fmt, offset, *values):
 @pytest.mark.parametrize("field,fmt,offset,value", [
     ("cur", "<I", 48, 2), ("materialised", "<I", 52, 7), ("closure", "<I", 56, 2),
     ("omega", "<f", 28, float("nan")), ("omega", "<f", 28, 2.5), ("u_in", "<f", 32, float("inf")),
-    ("drift", "<f", 36, float("nan")), ("drift", "<f", 36, -1.0)])
+    ("drift", "<f", 36, float("nan")), ("drift", "<f", 36, -1.0), ("store_inlet", "<I", 76, 2)])
 def test_gpu_checkpoint_header_fields_are_range_checked(lbm, cuda_ok, field, fmt, offset, value):
     """A header whose fields steer device work (the buffer index `cur`, the
     flags, omega, the inlet and the drift bound) is refused with LBM_ERR_ARG

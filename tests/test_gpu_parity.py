@@ -73,10 +73,13 @@ def test_gpu_matches_reference_single_cell_fixture(lbm, cuda_ok):
 
 
 def run_pair(lbm, P, nx, ny, omega, edge, storage, prec, steps, mask, ux=0.1, noise=1e-3, seed=0, rows=8,
-             chunks=None, edits=None, kernel=1):
+             chunks=None, edits=None, kernel=1, store_inlet=True):
     lat = lbm.Lattice(nx, ny, omega, edge, storage)
     lat.set_tuning(rows, kernel)
     o = P.Oracle(nx, ny, float(np.float32(omega)), edge, prec)
+    if not store_inlet:
+        lat.set_storage_reference(False)
+        o.set_storage_reference(False)
     lat.set_inlet_velocity(ux)  # channel inlet speed (no field reset)
     o.set_inlet(float(np.float32(ux)), apply=False)
     lat.init_equilibrium(1.0, ux, 0.0, noise, seed)
@@ -137,9 +140,14 @@ def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, ed
 
 
 @pytest.mark.parametrize("edge", [0, 1])
-def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge):
+@pytest.mark.parametrize("storage,store_inlet", [(0, True), (1, True), (2, True), (1, False), (2, False)])
+def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge, storage, store_inlet):
     """Barrier edits, omega and inlet changes between iterate calls keep the
-    reference's step semantics (the fused state is materialised first)."""
+    reference's step semantics (the fused state is materialised first).  In
+    16-bit storage the inlet change re-expresses the stored words against the
+    new inlet equilibrium (or, with the rest-weight reference, leaves them),
+    and the last edit switches the storage reference; every step of it
+    matches the oracle bit for bit."""
     P = oracle_mod
     nx, ny = 64, 40
     rng = np.random.default_rng(5 + edge)
@@ -163,10 +171,34 @@ def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge):
         lat.reset_barrier()
         o.reset_barrier()
 
-    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.7, edge, lbm.F32, P.P_F32, 0, mask, chunks=[7, 5, 1, 9, 4, 6],
-                      edits=[draw, omega, inlet, draw, reset_barrier])
+    def switch_reference(lat, o):
+        lat.set_storage_reference(not store_inlet)
+        o.set_storage_reference(not store_inlet)
+        assert lat.storage_reference == (not store_inlet)
+
+    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.7, edge, storage, storage, 0, mask, chunks=[7, 5, 1, 9, 4, 6, 5],
+                      edits=[draw, omega, inlet, draw, reset_barrier, switch_reference], store_inlet=store_inlet)
     assert_same_state(lat, o)
     assert lat.get_compute_num() == o.step_count
+    lat.close()
+
+
+@pytest.mark.parametrize("storage", [1, 2])
+@pytest.mark.parametrize("edge", [0, 1])
+@pytest.mark.parametrize("nx,ny,rows", [(33, 17, 4), (129, 64, 5), (1100, 700, 9), (2048, 96, 2)])
+@pytest.mark.parametrize("kernel", [1, 3, 7, 9, 11, 12, 13])
+def test_gpu_rest_reference_16bit(lbm, cuda_ok, oracle_mod, storage, edge, nx, ny, rows, kernel):
+    """16-bit words relative to the rest weights (lbm_set_storage_reference
+    0): the collision's shorter form matches the oracle bit for bit in every
+    kernel variant, f16 and bf16."""
+    P = oracle_mod
+    rng = np.random.default_rng(nx * 31 + ny + 5 * storage + edge)
+    omega = float(np.float32(rng.uniform(0.7, 1.9)))
+    mask = (rng.random((ny, nx)) < 0.1).astype(np.uint8)
+    lat, o = run_pair(lbm, P, nx, ny, omega, edge, storage, storage, 50, mask, ux=0.08, noise=1e-2,
+                      seed=int(rng.integers(1 << 30)), rows=rows, kernel=kernel, store_inlet=False)
+    assert not lat.storage_reference
+    assert_same_state(lat, o)
     lat.close()
 
 
