@@ -554,9 +554,13 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
           if (x0 + j < a.L.nx) step_cell<St, EDGE>(a, x0 + j, y);
     return;
   }
-  // odd bands walk downwards: each band edge is then crossed by its two bands
-  // at the same time (both at the start, or both at the end of the launch)
-  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty, (blockIdx.y & 1u) != 0u);
+  // f32: odd bands walk downwards, so each band edge is crossed by its two
+  // bands at the same time (both at the start, or both at the end of the
+  // launch) and its halo rows are read while still in L2 (1 % faster at
+  // 4096 x 2048).  16-bit storage: every band walks upwards (1.5 % faster;
+  // its halo rows are half the bytes).
+  const bool down = sizeof(typename St::S) == 4 && (blockIdx.y & 1u) != 0u;
+  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty, down);
 }
 
 }  // namespace lbm

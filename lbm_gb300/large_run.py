@@ -11,7 +11,8 @@ radii 8-64), inlet ux 0.05, tau 0.51, run three ways on one GPU:
 For each run it reports MLUPS, achieved HBM GB/s on the step kernel
 (algorithmic bytes: 72 B per active cell in f32, 36 B in f16, +4 B of
 closure records), the relative FP64 drift of the fluid mass and momentum
-sums from the first to the last step, and the time-averaged velocity over
+sums from the first step (with --ramp: the first sample after the ramp) to
+the last, and the time-averaged velocity over
 the second half, and the first sample by which a step kernel had seen a
 non-finite density.  The f16 runs' time-averaged velocities are compared
 with the f32 run's (relative L2 over fluid cells).  Velocity averages stay on the
@@ -60,7 +61,7 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
             _check(lib.lbm_closure_set_weights(lat.handle, p.ctypes.data_as(ctypes.c_void_p), p.size))
             _check(lib.lbm_closure_enable(lat.handle, float(drift)))
         lat.iterate(1)
-        c0 = lat.conservation()
+        c0 = None if ramp else lat.conservation()
         done, n_avg, dev_ms, first_bad = 1, 0, 0.0, None
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         while done < steps:
@@ -80,6 +81,8 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
             done += k
             if ramp and done - k < ramp:
                 lat.set_inlet_velocity(u * min(1.0, done / ramp))
+            if c0 is None and done >= ramp:
+                c0 = lat.conservation()
             if first_bad is None:  # the step kernels' non-finite flag, outside the timing
                 try:
                     lat.synchronize()
@@ -107,8 +110,8 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
     bpc = (72 if storage == F32 else 36) + (4 if params is not None else 0)
     out.update({"steps": steps, "ms_per_step": dev_ms / timed, "mlups": nx * ny * timed / (dev_ms * 1e-3) / 1e6,
                 "achieved_gbs": bpc * active * timed / (dev_ms * 1e-3) / 1e9,
-                "mass_drift": float((c1[0] - c0[0]) / c0[0]),
-                "momentum_x_drift": float((c1[1] - c0[1]) / c0[1]) if c0[1] else None})
+                "mass_drift": float((c1[0] - c0[0]) / c0[0]) if c0 is not None else None,
+                "momentum_x_drift": float((c1[1] - c0[1]) / c0[1]) if c0 is not None and c0[1] else None})
     return out, (acc / max(n_avg, 1)).cpu().numpy()
 
 
@@ -117,12 +120,13 @@ def _field(lat, lib, code, tmp):
     return tmp
 
 
-def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refresh=20, drift=1.0, seed=1):
+def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refresh=20, drift=1.0, seed=1, ramp=0):
     """Where and how a run first goes non-finite (see the module docstring).
     `first_bad` is the sample at which the step kernels' flag was first seen
     set; the run is repeated to `first_bad - every` and then stepped singly.
     The repeat follows run()'s schedule exactly (one step, then the closure
-    inferred before steps 1, 1 + refresh, ...), so it retraces the same
+    inferred before steps 1, 1 + refresh, ..., and with a ramp the inlet
+    raised after steps 1 + every, 1 + 2 every, ...), so it retraces the same
     states bit for bit."""
     import torch
     from scipy import ndimage
@@ -132,8 +136,9 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
     rep = {}
     with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
         lat.set_stream(stream.cuda_stream)
-        lat.set_inlet_velocity(u)
-        lat.init_equilibrium(1.0, u, 0.0, 1e-4, seed)
+        u0 = 0.0 if ramp else u
+        lat.set_inlet_velocity(u0)
+        lat.init_equilibrium(1.0, u0, 0.0, 1e-4, seed)
         lat.draw_mask(mask)
         if params is not None:
             p = np.ascontiguousarray(params, np.float32)
@@ -148,11 +153,15 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
             nonlocal done
             while k > 0:
                 c = min(k, refresh - (done - 1) % refresh) if params is not None else k
+                if ramp:  # stop at each sample, where run() raises the inlet
+                    c = min(c, every - (done - 1) % every)
                 if params is not None and (done - 1) % refresh == 0:
                     _check(lib.lbm_closure_infer(lat.handle))
                 lat.iterate(c)
                 done += c
                 k -= c
+                if ramp and (done - 1) % every == 0 and done - every < ramp:
+                    lat.set_inlet_velocity(u * min(1.0, done / ramp))
 
         # growth before the failure: the lowest density and the largest speed
         # over the fluid, every `every` / 5 steps from the start
@@ -239,9 +248,9 @@ def main(argv=None):
         return float(np.linalg.norm(d) / np.linalg.norm(u32[:, fl])) if np.isfinite(d).all() else float("inf")
 
     def diag(r, storage, params=None):
-        if a.diagnose and r["first_nonfinite_by_step"] is not None and not a.ramp:
+        if a.diagnose and r["first_nonfinite_by_step"] is not None:
             r["diagnosis"] = diagnose(nx, ny, a.tau, a.u, mask, storage, r["first_nonfinite_by_step"], a.every,
-                                      params=params, refresh=a.refresh, drift=a.drift, seed=a.seed)
+                                      params=params, refresh=a.refresh, drift=a.drift, seed=a.seed, ramp=a.ramp)
 
     if not a.closure_only:
         r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed, ramp=a.ramp)
