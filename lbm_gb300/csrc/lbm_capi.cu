@@ -106,6 +106,7 @@ struct lbm_sim {
   std::vector<uint32_t> words_h;
   bool mask_h_valid = true;        // mask_h mirrors mask_d (lbm_set_mask packs on the device only)
   cudaEvent_t copied = nullptr;    // marks the end of a copy from a caller's host buffer
+  cudaEvent_t switched = nullptr;  // the end of the previous stream's work, for lbm_set_stream
   cudaStream_t own_stream = nullptr, stream = nullptr;
   int cur = 0;               // buffer holding the latest state
   bool materialised = true;  // cur holds a pre-collision state
@@ -325,6 +326,7 @@ void release(lbm_sim* s) {
   cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
   cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
   if (s->copied) cudaEventDestroy(s->copied);
+  if (s->switched) cudaEventDestroy(s->switched);
   if (s->own_stream) cudaStreamDestroy(s->own_stream);
 }
 
@@ -509,7 +511,8 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   s->staging_bytes = (size_t)9 * nx * ny * 8;
   if ((rc = alloc((void**)&s->staging_d, s->staging_bytes))) return rc;
   if (cudaStreamCreateWithFlags(&s->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&s->copied, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&s->copied, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&s->switched, cudaEventDisableTiming) != cudaSuccess) {
     release(s);
     delete s;
     return fail(LBM_ERR_CUDA, "cudaStreamCreate / cudaEventCreate failed");
@@ -553,7 +556,21 @@ int lbm_get_info(const lbm_sim* s, uint32_t* nx, uint32_t* ny, int* edge, int* s
 
 int lbm_set_stream(lbm_sim* s, void* stream) {
   CHECK_SIM_ANY(s);
-  s->stream = (cudaStream_t)stream;  // NULL is CUDA's legacy default stream
+  cudaStream_t next = (cudaStream_t)stream;  // NULL is CUDA's legacy default stream
+  if (next != s->stream) {
+    // Work already queued on the previous stream (the creation's
+    // initialisation, a re-base, a caller's steps) comes before anything
+    // queued on the new one: the new stream waits for it on the device.
+    // While either stream is being captured the caller orders the two.
+    cudaStreamCaptureStatus a = cudaStreamCaptureStatusNone, b = cudaStreamCaptureStatusNone;
+    CK(cudaStreamIsCapturing(s->stream, &a));
+    CK(cudaStreamIsCapturing(next, &b));
+    if (a == cudaStreamCaptureStatusNone && b == cudaStreamCaptureStatusNone) {
+      CK(cudaEventRecord(s->switched, s->stream));
+      CK(cudaStreamWaitEvent(next, s->switched, 0));
+    }
+  }
+  s->stream = next;
   return LBM_OK;
 }
 

@@ -58,18 +58,23 @@ def single_circle(nx, ny, cx, cy, r):
     return disk(np.zeros((ny, nx), np.uint8), cx, cy, r)
 
 
-def random_circles(nx, ny, count, rmin, rmax, seed, inlet_clearance=64, target_fraction=None):
+def random_circles(nx, ny, count, rmin, rmax, seed, inlet_clearance=64, target_fraction=None,
+                   outlet_clearance=None):
     """`count` seeded circles with radii uniform in [rmin, rmax] and centres
     uniform over the grid, none within `inlet_clearance` cells of the inlet
-    (centre x - r >= clearance).  If target_fraction is given, drawing stops
-    once that solid fraction is reached."""
+    (centre x - r >= clearance).  With `outlet_clearance` none comes within
+    that many cells of the outflow column either (centre x + r <= nx - 1 -
+    clearance); without it circles may reach the outflow edge.  If
+    target_fraction is given, drawing stops once that solid fraction is
+    reached."""
     rng = SplitMix64(seed)
     m = np.zeros((ny, nx), np.uint8)
     placed = 0
     solid = 0  # running count of solid cells (only the disk's bounding box changes)
     while placed < count:
         r = rng.uniform(rmin, rmax)
-        cx = rng.uniform(inlet_clearance + r, nx - 1)
+        hi = nx - 1 if outlet_clearance is None else nx - 1 - outlet_clearance - r
+        cx = rng.uniform(inlet_clearance + r, hi)
         cy = rng.uniform(0, ny - 1)
         y0, y1 = max(int(np.floor(cy - r)), 0), min(int(np.ceil(cy + r)), ny - 1) + 1
         x0, x1 = max(int(np.floor(cx - r)), 0), min(int(np.ceil(cx + r)), nx - 1) + 1

@@ -228,13 +228,17 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--ramp", type=int, default=0,
                     help="start at rest and raise the inlet velocity to --u over this many steps")
+    ap.add_argument("--outlet-clearance", type=int, default=None,
+                    help="keep the circles this many cells from the outflow column (default: they may touch it)")
     ap.add_argument("--diagnose", action="store_true",
                     help="for each run that goes non-finite, locate the first non-finite step and cells")
     a = ap.parse_args(argv)
     nx, ny = a.size
-    mask = random_circles(nx, ny, 10 ** 7, 8, 64, a.seed, inlet_clearance=64, target_fraction=0.08)
-    rep = {"workload": "D2Q9 channel %dx%d, circles r 8-64, %.1f%% solid, tau %.2f, ux %.2f" %
-           (nx, ny, 100 * mask.mean(), a.tau, a.u)}
+    mask = random_circles(nx, ny, 10 ** 7, 8, 64, a.seed, inlet_clearance=64, target_fraction=0.08,
+                          outlet_clearance=a.outlet_clearance)
+    rep = {"workload": "D2Q9 channel %dx%d, circles r 8-64, %.1f%% solid, tau %.2f, ux %.2f%s" %
+           (nx, ny, 100 * mask.mean(), a.tau, a.u,
+            "" if a.outlet_clearance is None else ", outflow clearance %d" % a.outlet_clearance)}
     t0 = time.time()
     rep["runs"] = []
     u32 = None

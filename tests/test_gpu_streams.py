@@ -1,0 +1,76 @@
+"""GPU: work queued on a lattice's stream before lbm_set_stream comes first.
+
+A handle starts on its own non-blocking stream; a caller that moves it to
+another stream (a torch stream, the legacy default stream) expects the steps,
+re-bases and initialisations already queued to finish before the new
+stream's work touches the same buffers.  lbm_set_stream makes the new stream
+wait for the old one on the device.  Each case queues milliseconds of work,
+switches at once, and compares with the same calls on one stream: bit for
+bit."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NX, NY = 2048, 1024
+
+
+def _layout():
+    from lbm_gb300 import geometry
+    return geometry.random_circles(NX, NY, 60, 4, 24, seed=3, inlet_clearance=64)
+
+
+def _start(lbm, storage, mask):
+    lat = lbm.Lattice(NX, NY, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
+    lat.set_inlet_velocity(0.08)
+    lat.init_equilibrium(1.0, 0.08, 0.0, 1e-3, 7)
+    lat.draw_mask(mask)
+    return lat
+
+
+@pytest.mark.parametrize("storage", [0, 1])
+def test_gpu_steps_queued_before_a_stream_switch_come_first(lbm, cuda_ok, storage):
+    import torch
+    mask = _layout()
+    ref = _start(lbm, storage, mask)
+    ref.iterate(300)
+    ref.iterate(7)
+    want = ref.populations()
+    ref.close()
+
+    lat = _start(lbm, storage, mask)
+    lat.iterate(300)  # ~10 ms queued on the handle's own stream
+    s = torch.cuda.Stream()
+    lat.set_stream(s.cuda_stream)
+    lat.iterate(7)  # on the new stream: must follow the 300 steps
+    np.testing.assert_array_equal(lat.populations(), want)
+    lat.close()
+
+
+@pytest.mark.parametrize("storage", [1, 2])
+def test_gpu_rebase_queued_before_a_stream_switch_comes_first(lbm, cuda_ok, storage):
+    """lbm_set_storage_reference re-expresses every stored word (one pass on
+    the handle's stream); an initialisation queued on a new stream right
+    after must not race it."""
+    import torch
+    mask = _layout()
+    ref = lbm.Lattice(NX, NY, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
+    ref.set_storage_reference(False)
+    ref.set_inlet_velocity(0.08)
+    ref.init_equilibrium(1.0, 0.08, 0.0, 1e-3, 7)
+    ref.draw_mask(mask)
+    ref.iterate(20)
+    want = ref.populations()
+    ref.close()
+
+    lat = lbm.Lattice(NX, NY, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
+    lat.iterate(100)  # keep the handle's own stream busy before the re-base
+    lat.set_storage_reference(False)
+    s = torch.cuda.Stream()
+    lat.set_stream(s.cuda_stream)
+    lat.set_inlet_velocity(0.08)
+    lat.init_equilibrium(1.0, 0.08, 0.0, 1e-3, 7)
+    lat.draw_mask(mask)
+    lat.iterate(20)
+    np.testing.assert_array_equal(lat.populations(), want)
+    lat.close()
