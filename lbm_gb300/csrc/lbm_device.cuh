@@ -116,6 +116,58 @@ __device__ __forceinline__ void collide_dev(float g[9], float rho, float drho, f
   g[4] = __fmaf_rn(o.omw, g[4], __fmaf_rn(o.aw0, c0, nk(4)));                                            // rest
 }
 
+// Two cells at once.  The packed f32x2 operations of sm_100 and later
+// (add / mul / fma .rn.f32x2) round each component exactly as the scalar
+// operation does, so a pair of cells evaluated with them gives what two calls
+// of moments_dev / collide_dev give, bit for bit, in about half the
+// instructions.  Subtraction is addition of the negation (exact in IEEE
+// arithmetic, signed zeros included).
+__device__ __forceinline__ float2 dup2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 neg2(float2 a) { return make_float2(-a.x, -a.y); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a, neg2(b)); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void moments_dev2(const float2 g[9], float2& rho, float2& drho, float2& jx, float2& jy,
+                                             const StoreRef& R) {
+  const float2 cw = add2(add2(g[0], g[3]), g[6]);
+  const float2 ce = add2(add2(g[2], g[5]), g[8]);
+  const float2 cm = add2(add2(g[1], g[7]), g[4]);
+  drho = add2(add2(cw, ce), cm);
+  jx = add2(sub2(ce, cw), dup2(R.ux));
+  jy = add2(sub2(add2(add2(g[0], g[1]), g[2]), add2(add2(g[6], g[7]), g[8])), dup2(R.uy));
+  rho = add2(dup2(1.0f), drho);
+}
+__device__ __forceinline__ float2 recip_newton2(float2 x) {
+  float2 r = make_float2(__uint_as_float(0x7EF311C2u - __float_as_uint(x.x)),
+                         __uint_as_float(0x7EF311C2u - __float_as_uint(x.y)));
+  const float2 nx = neg2(x), one = dup2(1.0f);
+  r = fma2(r, fma2(nx, r, one), r);
+  r = fma2(r, fma2(nx, r, one), r);
+  return fma2(r, fma2(nx, r, one), r);
+}
+// collide_dev on two cells; NK(q) returns the pair of -(omega d_q).
+template <class NK>
+__device__ __forceinline__ void collide_dev2(float2 g[9], float2 rho, float2 drho, float2 jx, float2 jy,
+                                             const DevOmega& o, NK nk) {
+  const float2 h = mul2(dup2(0.5f), recip_newton2(rho));
+  const float2 c0 = fma2(fma2(jx, jx, mul2(jy, jy)), mul2(dup2(-3.0f), h), drho);
+  const float2 tx = mul2(dup2(3.0f), jx), ty = mul2(dup2(3.0f), jy);
+  const float2 tp = add2(tx, ty), tm = sub2(tx, ty);
+  const float2 hx = mul2(h, tx), hy = mul2(h, ty), hp = mul2(h, tp), hm = mul2(h, tm);
+  const float2 a1 = dup2(o.aw1), a2 = dup2(o.aw2), a0 = dup2(o.aw0), om = dup2(o.omw);
+  g[5] = fma2(a1, fma2(hx, tx, tx), fma2(om, g[5], fma2(a1, c0, nk(5))));
+  g[3] = fma2(a1, fma2(hx, tx, neg2(tx)), fma2(om, g[3], fma2(a1, c0, nk(3))));
+  g[1] = fma2(a1, fma2(hy, ty, ty), fma2(om, g[1], fma2(a1, c0, nk(1))));
+  g[7] = fma2(a1, fma2(hy, ty, neg2(ty)), fma2(om, g[7], fma2(a1, c0, nk(7))));
+  g[2] = fma2(a2, fma2(hp, tp, tp), fma2(om, g[2], fma2(a2, c0, nk(2))));
+  g[6] = fma2(a2, fma2(hp, tp, neg2(tp)), fma2(om, g[6], fma2(a2, c0, nk(6))));
+  g[8] = fma2(a2, fma2(hm, tm, tm), fma2(om, g[8], fma2(a2, c0, nk(8))));
+  g[0] = fma2(a2, fma2(hm, tm, neg2(tm)), fma2(om, g[0], fma2(a2, c0, nk(0))));
+  g[4] = fma2(om, g[4], fma2(a0, c0, nk(4)));
+}
+
 // Storage policies.  S is the stored word, C the arithmetic type, and a
 // "working value" is what the step kernels carry per population: f_i for
 // f32 / f64 (the reference's arithmetic), g_i = f_i - w_i for 16-bit storage.
@@ -178,6 +230,16 @@ template <class Word> struct StDev {
   __device__ static void collide_u(C v[9], C rho, C aux, C jx, C jy, const Om& o, const StoreRef& R) {
     if (R.shift) collide_dev(v, rho, aux, jx, jy, o, [&](int q) { return R.nk[q]; });
     else collide_dev(v, rho, aux, jx, jy, o, [](int) { return -0.0f; });
+  }
+  // the same for two cells (packed f32x2 arithmetic, identical results)
+  __device__ static void moments2(const float2 v[9], float2& rho, float2& aux, float2& jx, float2& jy,
+                                  const StoreRef& R) {
+    moments_dev2(v, rho, aux, jx, jy, R);
+  }
+  __device__ static void collide_u2(float2 v[9], float2 rho, float2 aux, float2 jx, float2 jy, const Om& o,
+                                    const StoreRef& R) {
+    if (R.shift) collide_dev2(v, rho, aux, jx, jy, o, [&](int q) { return dup2(R.nk[q]); });
+    else collide_dev2(v, rho, aux, jx, jy, o, [](int) { return dup2(-0.0f); });
   }
 };
 struct WordF16 {

@@ -419,6 +419,33 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         }
       }
       C m_rho[CPT], m_jx[CPT], m_jy[CPT];
+      if constexpr (St::kDev && !CL && CPT == 2) {
+        // 16-bit storage, uniform omega: the two cells as a pair on the packed
+        // f32x2 operations (the same values as one cell at a time, fewer
+        // issues; with four cells per thread the pairs spilled registers)
+#pragma unroll
+        for (int j = 0; j < CPT; j += 2) {
+          float2 g[9];
+#pragma unroll
+          for (int q = 0; q < 9; q++) g[q] = make_float2(f[q][j], f[q][j + 1]);
+          float2 rho, jx, jy, aux;
+          St::moments2(g, rho, aux, jx, jy, a.ref);
+          if (act[j]) rho_sum += rho.x;
+          if (act[j + 1]) rho_sum += rho.y;
+          m_rho[j] = rho.x;
+          m_rho[j + 1] = rho.y;
+          m_jx[j] = jx.x;
+          m_jx[j + 1] = jx.y;
+          m_jy[j] = jy.x;
+          m_jy[j + 1] = jy.y;
+          St::collide_u2(g, rho, aux, jx, jy, om, a.ref);
+#pragma unroll
+          for (int q = 0; q < 9; q++) {
+            f[q][j] = g[q].x;
+            f[q][j + 1] = g[q].y;
+          }
+        }
+      } else {
 #pragma unroll
       for (int j = 0; j < CPT; j++) {
         C g[9];
@@ -440,6 +467,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         }
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
+      }
       }
       if (a.rho_out) {  // one uniform test per row, not one per cell
 #pragma unroll
