@@ -40,6 +40,20 @@ int lbm_checkpoint_save(lbm_sim* sim, void* buf, size_t len);
  * closure and store_inlet must be 0 or 1; omega in (0, 2); u_in finite; drift finite and
  * > 0). */
 int lbm_checkpoint_load(lbm_sim* sim, const void* buf, size_t len);
+
+/* Host only (no device work, no lattice): check a checkpoint buffer as
+ * lbm_checkpoint_load does before it touches a lattice (magic, version,
+ * header ranges, a grid, edge mode, storage and element size the engine
+ * knows, the payload size those imply, the CRC) and, when `info` is not
+ * NULL, report what it holds.  LBM_ERR_ARG when any check fails. */
+typedef struct lbm_checkpoint_info {
+  uint32_t nx, ny;
+  int edge, storage;
+  float omega, u_in, drift;
+  uint64_t steps;
+  int closure, store_inlet;
+} lbm_checkpoint_info;
+int lbm_checkpoint_inspect(const void* buf, size_t len, lbm_checkpoint_info* info);
 /* The same through a file. */
 int lbm_checkpoint_write(lbm_sim* sim, const char* path);
 int lbm_checkpoint_read(lbm_sim* sim, const char* path);

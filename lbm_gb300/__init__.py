@@ -109,6 +109,7 @@ _SIGS = [
     ("lbm_checkpoint_load", ctypes.c_int, [_P, _P, ctypes.c_size_t]),
     ("lbm_checkpoint_write", ctypes.c_int, [_P, ctypes.c_char_p]),
     ("lbm_checkpoint_read", ctypes.c_int, [_P, ctypes.c_char_p]),
+    ("lbm_checkpoint_inspect", ctypes.c_int, [_P, ctypes.c_size_t, _P]),
     # include/lbm_cnn.h
     ("lbm_cnn_conv_forward", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, _P, _P,
                                             ctypes.c_int, ctypes.c_int, _P, _P]),
@@ -144,6 +145,24 @@ _SIGS = [
     ("lbm_batch_set_schedule", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P]),
     ("lbm_batch_autotune", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]),
 ]
+
+
+class CheckpointInfo(ctypes.Structure):
+    """lbm_checkpoint_info (include/lbm_checkpoint.h)."""
+    _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("edge", ctypes.c_int), ("storage", ctypes.c_int),
+                ("omega", ctypes.c_float), ("u_in", ctypes.c_float), ("drift", ctypes.c_float),
+                ("steps", ctypes.c_uint64), ("closure", ctypes.c_int), ("store_inlet", ctypes.c_int)]
+
+
+def checkpoint_info(buf):
+    """Check a checkpoint (bytes) on the host, as loading it would, and return
+    its header fields as a dict; raises LBMError if any check fails.  Needs
+    no GPU and no lattice."""
+    load_library()
+    b = np.frombuffer(buf, np.uint8)
+    info = CheckpointInfo()
+    _check(_lib.lbm_checkpoint_inspect(ctypes.c_void_p(b.ctypes.data), b.size, ctypes.byref(info)))
+    return {name: getattr(info, name) for name, _ in CheckpointInfo._fields_}
 
 
 def load_library(path=None):

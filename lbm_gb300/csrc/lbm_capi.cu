@@ -1444,16 +1444,13 @@ int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
   return LBM_OK;
 }
 
-int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
-  CHECK_SIM(s);
+// The checks of lbm_checkpoint_inspect, on the host only: the header and
+// the CRC over header and payload.  `h` receives the header.
+int ck_check(const void* buf, size_t len, CkHeader& h) {
   if (!buf || len < sizeof(CkHeader)) return fail(LBM_ERR_ARG, "checkpoint too short");
-  CkHeader h;
   std::memcpy(&h, buf, sizeof h);
   if (std::memcmp(h.magic, kCkMagic, 8) != 0 || h.version != kCkVersion)
     return fail(LBM_ERR_ARG, "not a version-%u lattice checkpoint", kCkVersion);
-  if ((int)h.nx != s->L.nx || (int)h.ny != s->L.ny || h.edge != s->edge || h.storage != s->storage)
-    return fail(LBM_ERR_ARG, "checkpoint is %ux%u edge %d storage %d, the lattice %dx%d edge %d storage %d", h.nx, h.ny,
-                h.edge, h.storage, s->L.nx, s->L.ny, s->edge, s->storage);
   // Every header field that steers device work is checked before any of it:
   // `cur` selects a buffer set, so anything but 0 or 1 would index past them.
   if (h.cur > 1u || h.materialised > 1u || h.closure > 1u || h.store_inlet > 1u)
@@ -1462,12 +1459,51 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
   if (!(h.omega > 0.0f && h.omega < 2.0f) || !std::isfinite(h.u_in) || !(h.drift > 0.0f) || !std::isfinite(h.drift))
     return fail(LBM_ERR_ARG, "checkpoint header: omega %g, inlet %g, drift %g out of range", (double)h.omega,
                 (double)h.u_in, (double)h.drift);
+  const int es = h.storage == STORE_F32 ? 4 : h.storage == STORE_F64 ? 8 : 2;
+  if (h.nx < 3 || h.ny < 3 || (h.edge != EDGE_REF && h.edge != EDGE_CHANNEL) || h.storage < STORE_F32 ||
+      h.storage > STORE_F64 || h.elem_bytes != (uint32_t)es)
+    return fail(LBM_ERR_ARG, "checkpoint header: grid %ux%u, edge %d, storage %d, element bytes %u", h.nx, h.ny,
+                h.edge, h.storage, h.elem_bytes);
+  const uint64_t cells = (uint64_t)h.nx * h.ny;
+  if (cells > (uint64_t)1 << 34) return fail(LBM_ERR_ARG, "checkpoint header: grid %ux%u too large", h.nx, h.ny);
+  const uint64_t payload = cells + 17 * cells * (uint64_t)es + (h.closure ? cells * 4 : 0);
+  if (h.payload_bytes != payload || len - sizeof(CkHeader) < payload)
+    return fail(LBM_ERR_ARG, "checkpoint size mismatch");
+  if (ck_crc(h, (const uint8_t*)buf + sizeof(CkHeader)) != h.crc32) return fail(LBM_ERR_ARG, "checkpoint CRC mismatch");
+  return LBM_OK;
+}
+
+int lbm_checkpoint_inspect(const void* buf, size_t len, lbm_checkpoint_info* info) {
+  CkHeader h;
+  int rc = ck_check(buf, len, h);
+  if (rc) return rc;
+  if (info) {
+    info->nx = h.nx;
+    info->ny = h.ny;
+    info->edge = h.edge;
+    info->storage = h.storage;
+    info->omega = h.omega;
+    info->u_in = h.u_in;
+    info->drift = h.drift;
+    info->steps = h.steps;
+    info->closure = (int)h.closure;
+    info->store_inlet = (int)h.store_inlet;
+  }
+  return LBM_OK;
+}
+
+int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
+  CHECK_SIM(s);
+  CkHeader h;
+  int rc0 = ck_check(buf, len, h);
+  if (rc0) return rc0;
+  if ((int)h.nx != s->L.nx || (int)h.ny != s->L.ny || h.edge != s->edge || h.storage != s->storage)
+    return fail(LBM_ERR_ARG, "checkpoint is %ux%u edge %d storage %d, the lattice %dx%d edge %d storage %d", h.nx, h.ny,
+                h.edge, h.storage, s->L.nx, s->L.ny, s->edge, s->storage);
   const bool closure = h.closure != 0;
-  if (h.elem_bytes != s->es || h.payload_bytes != ck_payload_bytes(s, closure) ||
-      len < sizeof(CkHeader) + h.payload_bytes)
+  if (h.elem_bytes != s->es || h.payload_bytes != ck_payload_bytes(s, closure))
     return fail(LBM_ERR_ARG, "checkpoint size mismatch");
   const uint8_t* p = (const uint8_t*)buf + sizeof(CkHeader);
-  if (ck_crc(h, p) != h.crc32) return fail(LBM_ERR_ARG, "checkpoint CRC mismatch");
   if (closure && !s->closure_base) {
     int rc = lbm_closure_enable(s, h.drift);
     if (rc) return rc;

@@ -118,3 +118,49 @@ def test_gpu_step_rows_matches_lbm_step_and_guards_the_state(lbm, cuda_ok, oracl
     np.testing.assert_array_equal(b.populations(), a.populations())
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("storage,kernel,slabs", [(0, 3, 2), (1, 11, 3), (2, 7, 2)])
+def test_gpu_overlapped_slabs_follow_inlet_changes(lbm, cuda_ok, storage, kernel, slabs):
+    """An inlet ramp between steps (lbm_set_inlet_velocity on every slab,
+    which materialises the state and, in 16-bit storage, re-expresses the
+    words against the new inlet equilibrium, ghost rows included): the slabs
+    still match the undivided lattice bit for bit."""
+    import torch
+    from lbm_gb300 import geometry
+    from lbm_gb300.slab import LocalExchanger, SlabLattice, run_local
+    nx, ny = 300, 96
+    mask = geometry.random_layout(nx, ny, 0.1, 5, rmin=3.0, inlet_clearance=10)
+    ref = lbm.Lattice(nx, ny, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
+    ref.set_tuning(8, kernel)
+    ref.set_inlet_velocity(0.0)
+    ref.init_equilibrium(1.0, 0.0, 0.0, 1e-3, 9)
+    ref.draw_mask(mask)
+    start = ref.populations(f64=True)
+    stream = torch.cuda.Stream()
+    ss = [SlabLattice(nx, ny, 1.0 / 0.56, r, slabs, storage=storage, u_in=0.0) for r in range(slabs)]
+    for s in ss:
+        s.lat.set_stream(stream.cuda_stream)
+        s.lat.set_tuning(8, kernel)
+        s.set_mask(mask)
+        s.write_populations(start)
+    ex = LocalExchanger(ss, device=True)
+    for s in ss:
+        s.attach(ex)
+    ref.write_populations(start)
+    for i in range(1, 5):
+        ref.iterate(7)
+        run_local(ss, 7)
+        u = 0.02 * i
+        ref.set_inlet_velocity(u)
+        for s in ss:
+            s.lat.set_inlet_velocity(u)
+    ref.iterate(5)
+    run_local(ss, 5)
+    got = np.concatenate([s.populations() for s in ss], axis=1)
+    np.testing.assert_array_equal(got, ref.populations())
+    for name in ("rho", "jx", "jy"):
+        np.testing.assert_array_equal(np.concatenate([s.field(name) for s in ss]), ref.field(name))
+    for s in ss:
+        s.lat.close()
+    ref.close()
