@@ -45,9 +45,10 @@ typedef struct lbm_sim lbm_sim;
 
 /* population storage */
 #define LBM_STORE_F32 0
-/* The 16-bit modes store the deviation of each population from the
- * equilibrium of the lattice's inlet velocity, f_i - f_i^eq(1, (u_in, 0)),
- * and collide in f32 arithmetic.  The inlet velocity is 0.1 at creation. */
+/* The 16-bit modes store the deviation of each population from the rest
+ * weights, f_i - w_i, and collide in f32 arithmetic; with
+ * lbm_set_storage_reference(sim, 1) the deviation from the equilibrium of
+ * the lattice's inlet velocity instead, f_i - f_i^eq(1, (u_in, 0)). */
 #define LBM_STORE_F16 1    /* binary16 deviations, f32 arithmetic */
 #define LBM_STORE_BF16 2   /* bfloat16 deviations, f32 arithmetic */
 #define LBM_STORE_F64 3    /* f64 storage and arithmetic (oracle-grade runs) */
@@ -136,18 +137,20 @@ int lbm_set_viscosity(lbm_sim* sim, float nu);
  * re-initialised to set_equil(ux, 0, 1) and the step count restarts at 0.
  * With reset_field == 0 only the inlet changes: in LBM_EDGE_CHANNEL the frozen
  * inlet column, in LBM_EDGE_REF column 0 (its de-facto inlet).  In the 16-bit
- * modes the inlet velocity is also the storage's reference state: a new one
- * without a reset re-expresses every stored word against it (one pass over
- * both buffer sets; its rounding is part of the state). */
+ * modes with the inlet storage reference (lbm_set_storage_reference) the
+ * inlet velocity is also the storage's reference state: a new one without a
+ * reset re-expresses every stored word against it (one pass over both
+ * buffer sets; its rounding is part of the state). */
 int lbm_set_inlet_velocity(lbm_sim* sim, float ux, int reset_field);
 
 /* 16-bit storage only (no reference counterpart: the reference stores f32).
- * inlet = 1 (the default) keeps the words relative to the inlet equilibrium,
- * which makes them small wherever the flow is near the inlet velocity;
- * inlet = 0 keeps them relative to the rest weights w_q, whose collision
- * needs one product fewer per direction (faster, coarser in a moving flow).
- * Switching re-expresses the stored state, like a new inlet velocity; a
- * no-op for f32 / f64.  The setting travels with checkpoints. */
+ * inlet = 0 (the default) keeps the words relative to the rest weights w_q,
+ * f_i - w_i; inlet = 1 keeps them relative to the inlet equilibrium, which
+ * makes them small wherever the flow is near the inlet velocity (several
+ * times less rounding error in a moving flow, a few per cent slower: one
+ * fused operation more per direction, bounced words re-expressed for their
+ * new direction).  Switching re-expresses the stored state; a no-op for
+ * f32 / f64.  The setting travels with checkpoints. */
 int lbm_set_storage_reference(lbm_sim* sim, int inlet);
 int lbm_get_storage_reference(const lbm_sim* sim, int* inlet);
 
@@ -266,8 +269,9 @@ int lbm_conservation_noalloc(const float* rho, const float* jx, const float* jy,
  * y .. y + nrows - 1 of the moving-population planes selected by slot_mask
  * (bit s = slot s: 0 nw, 1 n, 2 ne, 3 w, 4 e, 5 sw, 6 s, 7 se) of the state
  * the next step pulls from, in the storage's own words (4, 2 or 8 bytes;
- * 16-bit words are relative to the lattice's inlet velocity, so lattices
- * that exchange rows must share it),
+ * 16-bit words are relative to the lattice's storage reference, so lattices
+ * that exchange rows must share it and, with the inlet reference, the inlet
+ * velocity),
  * planes in slot order, each nrows * nx words row-major.  on_device != 0:
  * `out` / `in` is device memory and the copy is queued on the lattice's
  * stream; otherwise host memory and the call synchronises. */

@@ -4,8 +4,8 @@
  * life of the page, lbm.rs:32-98).  A checkpoint here holds the exact device
  * state, so that a lattice loaded from it continues bit for bit as the saved
  * one would have: both buffer sets and the rest plane in their storage words
- * (f32, f64, or the 16-bit words relative to the equilibrium of the saved
- * inlet velocity u_in, or to the rest weights when store_inlet is 0), which
+ * (f32, f64, or the 16-bit words relative to the rest weights, or with
+ * store_inlet = 1 to the equilibrium of the saved inlet velocity u_in), which
  * buffer is current and whether
  * it is materialised, the step count, omega, the inlet velocity, the solid
  * mask and, when the learned closure is on, its per-cell records.

@@ -269,11 +269,11 @@ class Lattice:
         _check(_lib.lbm_set_inlet_velocity(self._h, float(ux), 1 if reset_field else 0))
 
     def set_storage_reference(self, inlet):
-        """16-bit storage: keep the words relative to the inlet equilibrium
-        (True, the default: smaller words in a flow near the inlet velocity)
-        or to the rest weights (False: one product fewer per direction in
-        the collision).  The stored state is re-expressed; f32 / f64 storage
-        is unaffected."""
+        """16-bit storage: keep the words relative to the rest weights (False,
+        the default: f - w) or to the inlet equilibrium (True: smaller words,
+        and several times less rounding error, in a flow near the inlet
+        velocity; a few per cent slower).  The stored state is re-expressed;
+        f32 / f64 storage is unaffected."""
         _check(_lib.lbm_set_storage_reference(self._h, 1 if inlet else 0))
 
     @property

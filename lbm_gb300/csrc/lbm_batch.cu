@@ -124,7 +124,12 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
           for (int j = 0; j < CPT; j++)
             if (x0 + j < sa.L.nx) step_cell<St, EDGE_CHANNEL>(sa, x0 + j, y);
     } else {
-      ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W>(sa, xb, T.z, T.w, smem, full, empty, down);
+      if constexpr (St::kDev) {
+        if (sa.ref.shift) ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(sa, xb, T.z, T.w, smem, full, empty, down);
+        else ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
+      } else {
+        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
+      }
       __syncthreads();  // every arrival and copy of this tile is complete
       if (threadIdx.x == 0)
         for (int i = 0; i < NS; i++) {  // the next tile initialises them again
@@ -143,6 +148,10 @@ struct DomainHost {
   size_t off_f[2], off_rest, off_mask, off_mom;  // byte offsets into the arena
   std::vector<uint8_t> mask;
 };
+
+// 16-bit words of a batched domain are relative to the rest weights (f - w),
+// the single lattice's default storage reference.
+StoreRef domain_ref(const DomainHost& h) { return make_store_ref(0.0f, h.omega); }
 
 struct Config {
   int variant = 0;     // index into kVariants
@@ -340,7 +349,7 @@ int materialise_all(lbm_batch* b) {
       dim3 grid((h.nx + kBlock - 1) / kBlock, h.ny);
       k_materialise<St, EDGE_CHANNEL><<<grid, kBlock, 0, b->stream>>>(
           h.L, (const S*)(b->arena + h.off_f[b->cur]), (S*)(b->arena + h.off_f[dst]),
-          (const uint32_t*)(b->arena + h.off_mask), make_store_ref(h.u_in, h.omega));
+          (const uint32_t*)(b->arena + h.off_mask), domain_ref(h));
     }
     BCK(cudaGetLastError());
     return LBM_OK;
@@ -458,7 +467,7 @@ int lbm_batch_create(uint32_t count, const uint32_t* nx, const uint32_t* ny, con
     dd[d].mask = (uint32_t*)(b->arena + h.off_mask);
     dd[d].mom = b->arena + h.off_mom;
     dd[d].omega = h.omega;
-    dd[d].ref = make_store_ref(h.u_in, h.omega);
+    dd[d].ref = domain_ref(h);
   }
   cudaMemcpyAsync(b->d_doms, dd.data(), count * sizeof(DomainDev), cudaMemcpyHostToDevice, b->stream);
   if ((e = cudaStreamSynchronize(b->stream)) != cudaSuccess) return cleanup(LBM_ERR_CUDA, "setup", e);
@@ -518,7 +527,7 @@ int lbm_batch_init_equilibrium(lbm_batch* b, float noise_amp, uint64_t seed) {
       k_init<St><<<grid, kBlock, 0, b->stream>>>(h.L, (S*)(b->arena + h.off_f[0]), (S*)(b->arena + h.off_f[1]),
                                                   (S*)(b->arena + h.off_rest), 1.0f, h.u_in, 0.0f, noise_amp,
                                                   seed + (uint64_t)d, 1, h.u_in, -1, -1,
-                                                  make_store_ref(h.u_in, h.omega));
+                                                  domain_ref(h));
     }
     BCK(cudaGetLastError());
     return LBM_OK;
@@ -579,7 +588,7 @@ int lbm_batch_read_field(lbm_batch* b, uint32_t domain, int field, float* out) {
       using S = typename St::S;
       k_moments<St><<<grid, kBlock, 0, b->stream>>>(h.L, (const S*)(b->arena + h.off_f[b->cur]),
                                                    (const S*)(b->arena + h.off_rest), mom, mom + h.L.ps,
-                                                   mom + 2 * h.L.ps, make_store_ref(h.u_in, h.omega));
+                                                   mom + 2 * h.L.ps, domain_ref(h));
       BCK(cudaGetLastError());
       return LBM_OK;
     };
@@ -607,7 +616,7 @@ int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
     using S = typename St::S;
     k_read_pops<St, float><<<grid, kBlock, 0, b->stream>>>(h.L, (const S*)(b->arena + h.off_f[b->cur]),
                                                            (const S*)(b->arena + h.off_rest), b->d_staging,
-                                                           make_store_ref(h.u_in, h.omega));
+                                                           domain_ref(h));
     BCK(cudaGetLastError());
     return LBM_OK;
   };

@@ -40,14 +40,19 @@ template <class C> __device__ __forceinline__ void bgk(C f[9], C rho, C jx, C jy
 //          the storage format (opposite directions have different references)
 //   nk_q = -(omega d_q) (f32) for the lattice's uniform omega (the collision
 //          computes the same product itself where omega varies per cell)
-// u_ref = 0 gives d = bb = nk = 0 and the plain f_q - w_q words.  f32 / f64
-// storage ignores it.
+// u_ref = 0 (no shift, the default) gives d = bb = nk = 0 and the plain
+// f_q - w_q words: the moments then add no u_ref, bounced words are taken as
+// they are, and the collision forms b once per weight class.  f32 / f64
+// storage ignores all of it.
 struct StoreRef {
   float d[9], r[9], bb[9], nk[9];
   float ux, uy;
-  int shift;  // u_ref != 0; with 0 every term above is zero (or -0) and the
-              // collision takes its shorter form, with the same results
+  int shift;  // u_ref != 0
 };
+// Shift modes of the policies' arithmetic: 0 and 1 fix StoreRef::shift at
+// compile time (the staged kernels instantiate both and branch once per
+// CTA), 2 reads it at run time.
+template <int M> __device__ __forceinline__ bool shifted(const StoreRef& R) { return M == 2 ? R.shift != 0 : M == 1; }
 
 // Deviation-form BGK on the 16-bit storage words h_i = f_i - r_i (StoreRef),
 // in f32 arithmetic with explicit FMA and one reciprocal by Newton's method
@@ -64,14 +69,19 @@ struct StoreRef {
 // b_i = (omega w_i) c0 - omega d_i: four fused operations per moving
 // direction.  The moments sum the three columns (c_x = -1, 0, +1) first, so
 // jx and drho share them.
+template <bool SH>
 __device__ __forceinline__ void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy,
                                             const StoreRef& R) {
   const float cw = (g[0] + g[3]) + g[6];  // c_x = -1
   const float ce = (g[2] + g[5]) + g[8];  // c_x = +1
   const float cm = (g[1] + g[7]) + g[4];  // c_x = 0
   drho = (cw + ce) + cm;
-  jx = (ce - cw) + R.ux;
-  jy = (((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8])) + R.uy;
+  jx = ce - cw;
+  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  if (SH) {  // the reference state's momentum
+    jx = jx + R.ux;
+    jy = jy + R.uy;
+  }
   rho = 1.0f + drho;
 }
 // 1 / x for a positive normal x: a seed from the float's bits (a linear
@@ -129,14 +139,19 @@ __device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __fadd2_rn(a
 __device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
 __device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
+template <bool SH>
 __device__ __forceinline__ void moments_dev2(const float2 g[9], float2& rho, float2& drho, float2& jx, float2& jy,
                                              const StoreRef& R) {
   const float2 cw = add2(add2(g[0], g[3]), g[6]);
   const float2 ce = add2(add2(g[2], g[5]), g[8]);
   const float2 cm = add2(add2(g[1], g[7]), g[4]);
   drho = add2(add2(cw, ce), cm);
-  jx = add2(sub2(ce, cw), dup2(R.ux));
-  jy = add2(sub2(add2(add2(g[0], g[1]), g[2]), add2(add2(g[6], g[7]), g[8])), dup2(R.uy));
+  jx = sub2(ce, cw);
+  jy = sub2(add2(add2(g[0], g[1]), g[2]), add2(add2(g[6], g[7]), g[8]));
+  if (SH) {
+    jx = add2(jx, dup2(R.ux));
+    jy = add2(jy, dup2(R.uy));
+  }
   rho = add2(dup2(1.0f), drho);
 }
 __device__ __forceinline__ float2 recip_newton2(float2 x) {
@@ -185,9 +200,11 @@ struct StF32 {
   __device__ static S store(C v, int) { return v; }
   __device__ static C f_of(S s, int, const StoreRef&) { return s; }
   __device__ static S of_f(C f, int, const StoreRef&) { return f; }
-  __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  template <int M = 2> __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  template <int M = 2>
   __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef&) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
   __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
+  template <int M = 2>
   __device__ static void collide_u(C v[9], C rho, C, C jx, C jy, const Om& w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
 };
 struct StF64 {
@@ -198,9 +215,11 @@ struct StF64 {
   __device__ static S store(C v, int) { return v; }
   __device__ static C f_of(S s, int, const StoreRef&) { return s; }
   __device__ static S of_f(C f, int, const StoreRef&) { return f; }
-  __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  template <int M = 2> __device__ static C bounce(S s, int, const StoreRef&) { return s; }
+  template <int M = 2>
   __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef&) { lbm::moments<C>(v, rho, jx, jy); aux = C(0); }
   __device__ static void collide(C v[9], C rho, C, C jx, C jy, C w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
+  template <int M = 2>
   __device__ static void collide_u(C v[9], C rho, C, C jx, C jy, const Om& w, const StoreRef&) { bgk<C>(v, rho, jx, jy, w); }
 };
 // 16-bit words relative to the reference state (StoreRef); `Word` supplies
@@ -213,11 +232,15 @@ template <class Word> struct StDev {
   __device__ static S store(C v, int) { return Word::of(v); }
   __device__ static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + Word::to_f(s); }
   __device__ static S of_f(C f, int q, const StoreRef& R) { return Word::of((f - weight<float>(q)) - R.d[q]); }
-  // the own population 8 - q bounced back into direction q: re-expressed
-  // against q's reference and rounded to the storage format
-  __device__ static C bounce(S s, int q, const StoreRef& R) { return Word::to_f(Word::of(Word::to_f(s) + R.bb[q])); }
-  __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef& R) {
-    moments_dev(v, rho, aux, jx, jy, R);
+  // the own population 8 - q bounced back into direction q: with a shift,
+  // re-expressed against q's reference and rounded to the storage format
+  template <int M = 2> __device__ static C bounce(S s, int q, const StoreRef& R) {
+    if (shifted<M>(R)) return Word::to_f(Word::of(Word::to_f(s) + R.bb[q]));
+    return Word::to_f(s);
+  }
+  template <int M = 2> __device__ static void moments(const C v[9], C& rho, C& aux, C& jx, C& jy, const StoreRef& R) {
+    if (shifted<M>(R)) moments_dev<true>(v, rho, aux, jx, jy, R);
+    else moments_dev<false>(v, rho, aux, jx, jy, R);
   }
   // per-cell omega: -(omega d_q) formed here
   __device__ static void collide(C v[9], C rho, C aux, C jx, C jy, C w, const StoreRef& R) {
@@ -225,20 +248,24 @@ template <class Word> struct StDev {
   }
   // the lattice's uniform omega: its constants, and -(omega d_q) from R.nk.
   // Without a shift every -(omega d_q) is -0 and fma(aw, c0, -0) = aw c0
-  // exactly, so the branch that uses the constant -0 computes the same
-  // values with one product per weight class instead of one per direction.
+  // exactly, so that form uses the constant -0: one product per weight
+  // class instead of one per direction, the same values.
+  template <int M = 2>
   __device__ static void collide_u(C v[9], C rho, C aux, C jx, C jy, const Om& o, const StoreRef& R) {
-    if (R.shift) collide_dev(v, rho, aux, jx, jy, o, [&](int q) { return R.nk[q]; });
+    if (shifted<M>(R)) collide_dev(v, rho, aux, jx, jy, o, [&](int q) { return R.nk[q]; });
     else collide_dev(v, rho, aux, jx, jy, o, [](int) { return -0.0f; });
   }
   // the same for two cells (packed f32x2 arithmetic, identical results)
+  template <int M = 2>
   __device__ static void moments2(const float2 v[9], float2& rho, float2& aux, float2& jx, float2& jy,
                                   const StoreRef& R) {
-    moments_dev2(v, rho, aux, jx, jy, R);
+    if (shifted<M>(R)) moments_dev2<true>(v, rho, aux, jx, jy, R);
+    else moments_dev2<false>(v, rho, aux, jx, jy, R);
   }
+  template <int M = 2>
   __device__ static void collide_u2(float2 v[9], float2 rho, float2 aux, float2 jx, float2 jy, const Om& o,
                                     const StoreRef& R) {
-    if (R.shift) collide_dev2(v, rho, aux, jx, jy, o, [&](int q) { return dup2(R.nk[q]); });
+    if (shifted<M>(R)) collide_dev2(v, rho, aux, jx, jy, o, [&](int q) { return dup2(R.nk[q]); });
     else collide_dev2(v, rho, aux, jx, jy, o, [](int) { return dup2(-0.0f); });
   }
 };

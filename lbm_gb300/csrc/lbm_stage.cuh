@@ -175,8 +175,10 @@ template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / C
 // alternate direction meet in time: two neighbouring bands start, or end,
 // together at their shared edge, so the halo rows one of them copies are read
 // by the other at about the same moment and come from L2 rather than HBM.
-// The order of rows does not change any cell's result.
-template <class St, int EDGE, int NS, int CPT, bool CL, int W, class A>
+// The order of rows does not change any cell's result.  KM is the storage
+// reference's shift mode (`shifted`): 0 or 1 where the caller has branched on
+// StoreRef::shift once for the whole tile.
+template <class St, int EDGE, int NS, int CPT, bool CL, int W, int KM, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
                                         uint64_t* empty, bool down = false) {
   using S = typename St::S;
@@ -375,15 +377,6 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       for (int j = 0; j < CPT; j++)
         f[4][j] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
     }
-    // 16-bit storage: this warp reads the oldest staged row no more, so it
-    // releases it before the collisions and the producer refills it one row's
-    // work earlier (measured 1.6 % faster; for f32, which already keeps HBM
-    // busy, it was 6 % slower, so f32 releases after the row as before)
-    constexpr bool kEarlyRelease = sizeof(S) == 2;
-    if constexpr (kEarlyRelease) {
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
-    }
     if (CPT == 1 && EDGE == EDGE_REF && act[0] && ((w0 >> 1) & 1u)) {
       // reference mode: solids collide their own previous values (global memory)
       C f[9];
@@ -392,7 +385,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         if (q != 4) f[q] = St::load(a.dstp[slot(q)][own], q);
       f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[tid], 4);
       C rho, jx, jy, aux;
-      St::moments(f, rho, aux, jx, jy, a.ref);
+      St::template moments<KM>(f, rho, aux, jx, jy, a.ref);
       rho_sum += rho;
       if (a.rho_out) {
         a.rho_out[own] = rho;
@@ -414,7 +407,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 #pragma unroll
           for (int j = 0; j < CPT; j++) {
             const int dx = cx(q) > 0 ? -1 : (cx(q) < 0 ? dxr[j] : 0);
-            if ((rowwin >> (j + 1 + dx)) & 1u) f[q][j] = St::bounce(opp[e + j], q, a.ref);
+            if ((rowwin >> (j + 1 + dx)) & 1u) f[q][j] = St::template bounce<KM>(opp[e + j], q, a.ref);
           }
         }
       }
@@ -429,7 +422,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 #pragma unroll
           for (int q = 0; q < 9; q++) g[q] = make_float2(f[q][j], f[q][j + 1]);
           float2 rho, jx, jy, aux;
-          St::moments2(g, rho, aux, jx, jy, a.ref);
+          St::template moments2<KM>(g, rho, aux, jx, jy, a.ref);
           if (act[j]) rho_sum += rho.x;
           if (act[j + 1]) rho_sum += rho.y;
           m_rho[j] = rho.x;
@@ -438,7 +431,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           m_jx[j + 1] = jx.y;
           m_jy[j] = jy.x;
           m_jy[j + 1] = jy.y;
-          St::collide_u2(g, rho, aux, jx, jy, om, a.ref);
+          St::template collide_u2<KM>(g, rho, aux, jx, jy, om, a.ref);
 #pragma unroll
           for (int q = 0; q < 9; q++) {
             f[q][j] = g[q].x;
@@ -452,7 +445,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 #pragma unroll
         for (int q = 0; q < 9; q++) g[q] = f[q][j];
         C rho, jx, jy, aux;
-        St::moments(g, rho, aux, jx, jy, a.ref);
+        St::template moments<KM>(g, rho, aux, jx, jy, a.ref);
         if (act[j]) rho_sum += rho;
         m_rho[j] = rho;
         m_jx[j] = jx;
@@ -463,7 +456,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           fallbacks += (fell_back && act[j]) ? 1u : 0u;
           St::collide(g, rho, aux, jx, jy, w, a.ref);
         } else {
-          St::collide_u(g, rho, aux, jx, jy, om, a.ref);
+          St::template collide_u<KM>(g, rho, aux, jx, jy, om, a.ref);
         }
 #pragma unroll
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
@@ -528,7 +521,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
             if (q != 4) f[q] = St::load(a.dstp[slot(q)][own + j], q);
           f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
           C rho, jx, jy, aux;
-          St::moments(f, rho, aux, jx, jy, a.ref);
+          St::template moments<KM>(f, rho, aux, jx, jy, a.ref);
           a.rho_out[own + j] = rho;
           a.jx_out[own + j] = jx;
           a.jy_out[own + j] = jy;
@@ -537,10 +530,11 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         step_cell<St, EDGE>(a, x0 + j, y);
       }
     }
-    if constexpr (!kEarlyRelease) {  // the oldest staged row is no longer needed by this warp
-      __syncwarp();
-      if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
-    }
+    // the oldest staged row is no longer needed by this warp.  (Releasing it
+    // right after the pulls are loaded, before the collisions, was measured
+    // too: 6 % slower in f32 and no faster in 16-bit storage.)
+    __syncwarp();
+    if (lane == 0) mbar_arrive(smem_addr(&empty[slot_m]));
     wa = w0;
     w0 = wn;
     slot_m = slot_0;
@@ -588,7 +582,14 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
   // 4096 x 2048).  16-bit storage: every band walks upwards (1.5 % faster;
   // its halo rows are half the bytes).
   const bool down = sizeof(typename St::S) == 4 && (blockIdx.y & 1u) != 0u;
-  ws_tile<St, EDGE, NS, CPT, CL, W>(a, xb, y0, y1, smem, full, empty, down);
+  // 16-bit storage: the arithmetic of the lattice's storage reference is
+  // fixed per instantiation, chosen here once for the CTA
+  if constexpr (St::kDev) {
+    if (a.ref.shift) ws_tile<St, EDGE, NS, CPT, CL, W, 1>(a, xb, y0, y1, smem, full, empty, down);
+    else ws_tile<St, EDGE, NS, CPT, CL, W, 0>(a, xb, y0, y1, smem, full, empty, down);
+  } else {
+    ws_tile<St, EDGE, NS, CPT, CL, W, 0>(a, xb, y0, y1, smem, full, empty, down);
+  }
 }
 
 }  // namespace lbm

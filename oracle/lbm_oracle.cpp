@@ -119,22 +119,26 @@ template <class C> inline C weight(int q) {
 }
 
 // Reference state of the 16-bit storage modes: the stored word of direction q
-// is h_q = f_q - r_q, r_q = f_q^eq(rho = 1, u = (u_ref, 0)), the equilibrium of
-// the channel's inlet velocity u_ref.  In most of a channel the flow stays
-// near the inlet velocity, so h_q is several times smaller than f_q - w_q and
-// its 16-bit rounding error is as much smaller.  d_q = r_q - w_q =
+// is h_q = f_q - r_q.  By default (lbm_set_storage_reference 0) r_q = w_q,
+// the rest weights: u_ref = 0 and h_q = f_q - w_q.  With the inlet reference
+// r_q = f_q^eq(rho = 1, u = (u_ref, 0)), the equilibrium of the channel's
+// inlet velocity u_ref.  In most of a channel the flow stays near the inlet
+// velocity, so h_q is then several times smaller than f_q - w_q and its
+// 16-bit rounding error is as much smaller.  d_q = r_q - w_q =
 // w_q (3 c.u + 4.5 (c.u)^2 - 1.5 u^2) is evaluated in double and rounded to
-// f32; r_q = w_q + d_q in f32.  u_ref = 0 gives d_q = 0, i.e. h_q = f_q - w_q.
+// f32; r_q = w_q + d_q in f32.
 // In exact arithmetic sum_q d_q = 0 and sum_q c_q d_q = u_ref, which the
 // collision uses (moments_dev, collide_dev).  Opposite directions have
 // different references, so a population bounced back into direction q (from
 // the cell's own 8 - q) is re-expressed: h_q = h_{8-q} + bb_q, bb_q = d_{8-q} -
-// d_q (f32), rounded to the storage format.
+// d_q (f32), rounded to the storage format.  Without a shift (u_ref = 0)
+// neither the momentum term u_ref nor the re-expression is applied.
 struct StoreRef {
   float d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float r[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float bb[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   float ux = 0.0f, uy = 0.0f;
+  bool shift = false;  // u_ref != 0
   void set(double vx, double vy) {
     const double wd[9] = {1.0 / 36, 1.0 / 9, 1.0 / 36, 1.0 / 9, 4.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 9, 1.0 / 36};
     const double u2 = vx * vx + vy * vy;
@@ -146,6 +150,7 @@ struct StoreRef {
     for (int q = 0; q < 9; q++) bb[q] = d[8 - q] - d[q];
     ux = (float)vx;
     uy = (float)vy;
+    shift = vx != 0.0 || vy != 0.0;
   }
 };
 
@@ -196,14 +201,18 @@ inline float recip_newton(float x) {
 // (omega w_q) X_q + ((1 - omega) h_q + b_q), b_q = (omega w_q) c0 - omega
 // d_q.  The moments sum the columns c_x = -1, 0, +1 first.  Operation order
 // is part of the definition (the GPU kernels use the same); with u_ref = 0 the
-// terms in d_q and u_ref add zeros and change nothing.
+// terms in d_q are zeros (b_q = (omega w_q) c0 exactly) and u_ref is not added.
 inline void moments_dev(const float g[9], float& rho, float& drho, float& jx, float& jy, const StoreRef& R) {
   const float cw = (g[0] + g[3]) + g[6];
   const float ce = (g[2] + g[5]) + g[8];
   const float cm = (g[1] + g[7]) + g[4];
   drho = (cw + ce) + cm;
-  jx = (ce - cw) + R.ux;
-  jy = (((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8])) + R.uy;
+  jx = ce - cw;
+  jy = ((g[0] + g[1]) + g[2]) - ((g[6] + g[7]) + g[8]);
+  if (R.shift) {  // the reference state's momentum
+    jx = jx + R.ux;
+    jy = jy + R.uy;
+  }
   rho = 1.0f + drho;
 }
 inline float relax_dev(float g, float aw, float h, float t, float sign, float omw, float b) {
@@ -274,7 +283,7 @@ struct SimBase {
   size_t N = 0;
   uint64_t step = 0;                 // compute_step, lbm.rs:1115
   double u_in = 0.1;                 // channel inlet velocity (and the 16-bit storage reference)
-  bool store_inlet = true;           // 16-bit words relative to (u_in, 0); false: to the rest weights
+  bool store_inlet = false;          // 16-bit words relative to (u_in, 0); false (default): to the rest weights
   std::vector<uint8_t> barrier;      // 1 = solid (the reference's u32 barrier buffer)
   virtual void set_omega(double w) = 0;
   virtual void set_inlet_velocity(double u) = 0;
@@ -303,7 +312,7 @@ template <class St> struct Sim : SimBase {
     for (int s = 0; s < 2; s++) for (int q = 0; q < 9; q++) f[s][q].assign(N, S());
     ux.assign(N, C(0)); uy.assign(N, C(0)); rho.assign(N, C(0));
     barrier.assign(N, 0);
-    ref.set((float)u_in, 0.0);
+    ref.set(store_inlet ? (float)u_in : 0.0f, 0.0);
     if (edge == EDGE_REF) {  // init_barrier, lbm.rs:595-605
       for (int x = 0; x < X; x++) { barrier[(size_t)x] = 1; barrier[(size_t)x + (size_t)(Y - 1) * X] = 1; }
     }
@@ -536,7 +545,7 @@ template <class St> struct Sim : SimBase {
         if (q == 4) continue;
         size_t j = upstream(i, q);
         if (barrier[j] != 1) G[q][i] = F[q][j];
-        else if constexpr (St::kDev) G[q][i] = St::store(St::load(F[8 - q][i], 8 - q) + ref.bb[q], q);  // re-expressed
+        else if (St::kDev && ref.shift) G[q][i] = St::store(St::load(F[8 - q][i], 8 - q) + ref.bb[q], q);  // re-expressed
         else G[q][i] = F[8 - q][i];
       }
     }

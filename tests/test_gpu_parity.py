@@ -73,13 +73,13 @@ def test_gpu_matches_reference_single_cell_fixture(lbm, cuda_ok):
 
 
 def run_pair(lbm, P, nx, ny, omega, edge, storage, prec, steps, mask, ux=0.1, noise=1e-3, seed=0, rows=8,
-             chunks=None, edits=None, kernel=1, store_inlet=True):
+             chunks=None, edits=None, kernel=1, store_inlet=None):
     lat = lbm.Lattice(nx, ny, omega, edge, storage)
     lat.set_tuning(rows, kernel)
     o = P.Oracle(nx, ny, float(np.float32(omega)), edge, prec)
-    if not store_inlet:
-        lat.set_storage_reference(False)
-        o.set_storage_reference(False)
+    if store_inlet is not None:  # else both keep their default (16-bit words relative to the rest weights)
+        lat.set_storage_reference(store_inlet)
+        o.set_storage_reference(store_inlet)
     lat.set_inlet_velocity(ux)  # channel inlet speed (no field reset)
     o.set_inlet(float(np.float32(ux)), apply=False)
     lat.init_equilibrium(1.0, ux, 0.0, noise, seed)
@@ -187,17 +187,17 @@ def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge, storage, 
 @pytest.mark.parametrize("edge", [0, 1])
 @pytest.mark.parametrize("nx,ny,rows", [(33, 17, 4), (129, 64, 5), (1100, 700, 9), (2048, 96, 2)])
 @pytest.mark.parametrize("kernel", [1, 3, 7, 9, 11, 12, 13])
-def test_gpu_rest_reference_16bit(lbm, cuda_ok, oracle_mod, storage, edge, nx, ny, rows, kernel):
-    """16-bit words relative to the rest weights (lbm_set_storage_reference
-    0): the collision's shorter form matches the oracle bit for bit in every
-    kernel variant, f16 and bf16."""
+def test_gpu_inlet_reference_16bit(lbm, cuda_ok, oracle_mod, storage, edge, nx, ny, rows, kernel):
+    """16-bit words relative to the inlet equilibrium (lbm_set_storage_reference
+    1): the shifted form of the collision, with bounced words re-expressed,
+    matches the oracle bit for bit in every kernel variant, f16 and bf16."""
     P = oracle_mod
     rng = np.random.default_rng(nx * 31 + ny + 5 * storage + edge)
     omega = float(np.float32(rng.uniform(0.7, 1.9)))
     mask = (rng.random((ny, nx)) < 0.1).astype(np.uint8)
     lat, o = run_pair(lbm, P, nx, ny, omega, edge, storage, storage, 50, mask, ux=0.08, noise=1e-2,
-                      seed=int(rng.integers(1 << 30)), rows=rows, kernel=kernel, store_inlet=False)
-    assert not lat.storage_reference
+                      seed=int(rng.integers(1 << 30)), rows=rows, kernel=kernel, store_inlet=True)
+    assert lat.storage_reference
     assert_same_state(lat, o)
     lat.close()
 

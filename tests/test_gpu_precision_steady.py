@@ -8,9 +8,11 @@ that does not shed), 20,000 steps, each storage against the f64 run of the
 same state.  The differences then grow smoothly (f32 linearly, from the
 rounding of the reference's own f32 arithmetic), not chaotically.  Bars
 (relative L2 velocity error over fluid cells, final and second-half
-average): f32 <= 2e-3, f16 <= 8e-3, bf16 <= 4e-2.  Measured: f32 7.1e-4 /
-5.5e-4, f16 4.6e-3 / 3.7e-3, bf16 2.4e-2 / 1.7e-2 with words stored against
-the inlet equilibrium (against the rest weights f16 was 2.2e-2 / 1.6e-2).
+average): f32 <= 2e-3; 16-bit words against the rest weights (the default)
+f16 <= 3e-2, bf16 <= 8e-2; against the inlet equilibrium f16 <= 8e-3,
+bf16 <= 4e-2, and f16 at least 3x below its rest-weight error.  Measured:
+f32 7.1e-4 / 5.5e-4; rest weights f16 2.2e-2 / 1.6e-2, bf16 6.1e-2 /
+5.0e-2; inlet equilibrium f16 4.6e-3 / 3.7e-3, bf16 2.4e-2 / 1.7e-2.
 """
 import os
 import sys
@@ -27,7 +29,9 @@ def test_gpu_storage_error_on_a_steady_wake(lbm, cuda_ok):
     import bench
     r = bench.steady_precision(lbm, steps=20000)
     print(r)
-    for name, bar in (("f32", 2e-3), ("f16", 8e-3), ("bf16", 4e-2)):
+    for name, bar in (("f32", 2e-3), ("f16", 3e-2), ("bf16", 8e-2), ("f16_inlet", 8e-3), ("bf16_inlet", 4e-2)):
         for k in ("rel_err_final_velocity", "rel_err_time_avg_velocity"):
             v = r[name][k]
             assert isinstance(v, float) and v <= bar, (name, k, v)
+    for k in ("rel_err_final_velocity", "rel_err_time_avg_velocity"):
+        assert 3 * r["f16_inlet"][k] <= r["f16"][k], k

@@ -55,7 +55,7 @@ def test_gpu_rebase_queued_before_a_stream_switch_comes_first(lbm, cuda_ok, stor
     import torch
     mask = _layout()
     ref = lbm.Lattice(NX, NY, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
-    ref.set_storage_reference(False)
+    ref.set_storage_reference(True)
     ref.set_inlet_velocity(0.08)
     ref.init_equilibrium(1.0, 0.08, 0.0, 1e-3, 7)
     ref.draw_mask(mask)
@@ -65,7 +65,7 @@ def test_gpu_rebase_queued_before_a_stream_switch_comes_first(lbm, cuda_ok, stor
 
     lat = lbm.Lattice(NX, NY, 1.0 / 0.56, lbm.EDGE_CHANNEL, storage)
     lat.iterate(100)  # keep the handle's own stream busy before the re-base
-    lat.set_storage_reference(False)
+    lat.set_storage_reference(True)
     s = torch.cuda.Stream()
     lat.set_stream(s.cuda_stream)
     lat.set_inlet_velocity(0.08)

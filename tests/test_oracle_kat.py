@@ -162,11 +162,11 @@ def test_low_precision_storage_tracks_f64(oracle_mod):
 # digests pin that definition: a change of its operation order, constants or
 # reciprocal changes them, and must come with new digests on purpose.
 DEVIATION_FORM_DIGESTS = {
-    # stored words relative to the inlet equilibrium (u_ref = u_in, the default)
+    # stored words relative to the inlet equilibrium (u_ref = u_in)
     (1, True): "943d4a54a4900d1d4400a1d38ffbc961345517099ff5dc4aaa61e362305d961d",  # f16
     (2, True): "288c6a41378f4dcef5d061287cc7cd0397a8c58ab8ce512a69e6e2deb7ae7475",  # bf16
-    # relative to the rest weights (lbm_set_storage_reference 0): the same
-    # digests as the form had before the inlet reference existed
+    # relative to the rest weights (the default): the same digests as the
+    # form had before the inlet reference existed
     (1, False): "6fb4472f739b93e861d02fe3583e58e3401610027c8468e3c70b516cc22c2806",
     (2, False): "b6ecdf327abfeaa188b6ad83dcd0633feec6441eb2ee5b4670b7606afc3d577a",
 }
@@ -180,8 +180,7 @@ def test_deviation_form_is_pinned(oracle_mod, prec, store_inlet):
     P = oracle_mod
     nx, ny = 48, 24
     o = P.Oracle(nx, ny, float(np.float32(1 / 0.56)), P.EDGE_CHANNEL, prec)
-    if not store_inlet:
-        o.set_storage_reference(False)
+    o.set_storage_reference(store_inlet)
     o.set_inlet(float(np.float32(0.08)), apply=False)
     o.init_equilibrium(1.0, float(np.float32(0.08)), 0.0, float(np.float32(1e-3)), 4)
     o.set_mask(geometry.single_circle(nx, ny, 14, 12, 4))
@@ -213,6 +212,7 @@ def test_inlet_reference_state_shrinks_the_storage_error(oracle_mod, prec):
 
     def run(p, uref):
         o = P.Oracle(nx, ny, float(np.float32(1 / 0.6)), P.EDGE_REF, p)
+        o.set_storage_reference(uref != 0.0)
         o.set_inlet(uref, apply=False)
         o.init_equilibrium(1.0, u, 0.0, 0.0, 0)
         o.set_mask(mask)
