@@ -764,13 +764,16 @@ def run_case(case):
     from lbm_gb300 import build as B
     B.build()
     lbm.load_library()
-    if case == "batched64":
+    if case in ("batched64", "batched64_f16"):
         from lbm_gb300 import batch
         nx, ny, om, u, masks = batch.batched_workload(64, 1)
-        with batch.Batch(nx, ny, om, u, lbm.F32) as b:
+        f16 = case == "batched64_f16"
+        with batch.Batch(nx, ny, om, u, lbm.F16 if f16 else lbm.F32) as b:
             for d, m in enumerate(masks):
                 b.set_mask(d, m)
-            b.set_schedule(0, 1, [32, 32, 32])
+            # f32: 4 stages, 1 cell per thread (variant 0); f16: 8 stages, 2 cells
+            # per thread (variant 3, the autotuner's choice on the full workload)
+            b.set_schedule(3 if f16 else 0, 1, [32, 32, 32])
             b.init_equilibrium(1e-3, 1)
             b.step(12)
             try:
@@ -820,7 +823,7 @@ def main():
                     help="with --kernel-only f16 / bf16: words relative to the inlet equilibrium")
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
                     help="time only the step kernel of one storage format (profiling runs)")
-    ap.add_argument("--case", choices=["batched64", "closure2048"], default=None,
+    ap.add_argument("--case", choices=["batched64", "batched64_f16", "closure2048"], default=None,
                     help="small fixed cases for kernel profiles: 64 batched domains (f32, 12 steps) or the "
                          "closure inference on a 2048x1024 lattice (4 launches)")
     args = ap.parse_args()
