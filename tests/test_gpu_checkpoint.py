@@ -53,6 +53,31 @@ def test_gpu_resume_is_bitwise_identical(lbm, cuda_ok, tmp_path, storage, edge, 
     b.close()
 
 
+@pytest.mark.parametrize("storage", [1, 2])
+def test_gpu_checkpoint_keeps_the_storage_reference(lbm, cuda_ok, storage):
+    """16-bit words saved relative to the inlet equilibrium load into a
+    lattice created with the default rest-weight reference: the setting is
+    restored with the words, the run continues bit for bit, and the host-side
+    inspection reports it."""
+    a = make(lbm, 120, 64, 1, storage, 11)
+    a.set_storage_reference(True)
+    a.iterate(19)
+    ck = a.checkpoint()
+    info = lbm.checkpoint_info(ck)
+    assert info["store_inlet"] == 1 and info["storage"] == storage and info["steps"] == 19
+    a.iterate(11)
+    want = a.populations()
+    b = lbm.Lattice(120, 64, 1.0, 1, storage)
+    assert not b.storage_reference
+    b.set_tuning(8, 11)
+    b.restore(ck)
+    assert b.storage_reference
+    b.iterate(11)
+    np.testing.assert_array_equal(b.populations(), want)
+    a.close()
+    b.close()
+
+
 def test_gpu_checkpoint_after_an_edit_and_with_the_closure(lbm, cuda_ok):
     import ctypes
     from lbm_gb300 import closure
