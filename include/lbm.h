@@ -161,6 +161,10 @@ int lbm_reset_to_equilibrium(lbm_sim* sim);
  * nx_i, ny_i are seeded uniform noise in [-noise_amp, noise_amp) from a
  * splitmix64 hash of (seed, cell, component).  Step count restarts at 0. */
 int lbm_init_equilibrium(lbm_sim* sim, float rho, float ux, float uy, float noise_amp, uint64_t seed);
+/* The same with the caller's noise: set_equil per cell at (rho, ux +
+ * noise[i], uy + noise[nx ny + i]), i = x + y nx, from 2 nx ny floats of
+ * host memory (NULL: no noise).  Returns once `noise` has been read. */
+int lbm_init_equilibrium_noise(lbm_sim* sim, float rho, float ux, float uy, const float* noise);
 
 /* single_cell (lbm.rs:1482-1515): rest state with population `direction` set
  * to 4.0 at the reference's cell for that direction. */

@@ -73,6 +73,7 @@ _SIGS = [
     ("lbm_set_viscosity", ctypes.c_int, [_P, ctypes.c_float]),
     ("lbm_set_inlet_velocity", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_int]),
     ("lbm_set_storage_reference", ctypes.c_int, [_P, ctypes.c_int]),
+    ("lbm_init_equilibrium_noise", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P]),
     ("lbm_get_storage_reference", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
     ("lbm_reset_to_equilibrium", ctypes.c_int, [_P]),
     ("lbm_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
@@ -287,6 +288,17 @@ class Lattice:
 
     def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
         _check(_lib.lbm_init_equilibrium(self._h, rho, ux, uy, noise, seed))
+
+    def init_equilibrium_noise(self, rho, ux, uy, noise):
+        """set_equil per cell at (rho, ux + noise[0], uy + noise[1]) with the
+        caller's float32 noise of shape (2, ny, nx); None for no noise."""
+        if noise is None:
+            _check(_lib.lbm_init_equilibrium_noise(self._h, rho, ux, uy, None))
+            return
+        n = np.ascontiguousarray(noise, np.float32)
+        if n.shape != (2, self.y, self.x):
+            raise ValueError("noise must have shape (2, %d, %d)" % (self.y, self.x))
+        _check(_lib.lbm_init_equilibrium_noise(self._h, rho, ux, uy, _ptr(n)))
 
     def single_cell(self, index):
         _check(_lib.lbm_single_cell(self._h, int(index)))

@@ -527,7 +527,7 @@ int lbm_batch_init_equilibrium(lbm_batch* b, float noise_amp, uint64_t seed) {
       k_init<St><<<grid, kBlock, 0, b->stream>>>(h.L, (S*)(b->arena + h.off_f[0]), (S*)(b->arena + h.off_f[1]),
                                                   (S*)(b->arena + h.off_rest), 1.0f, h.u_in, 0.0f, noise_amp,
                                                   seed + (uint64_t)d, 1, h.u_in, -1, -1,
-                                                  domain_ref(h));
+                                                  domain_ref(h), nullptr);
     }
     BCK(cudaGetLastError());
     return LBM_OK;

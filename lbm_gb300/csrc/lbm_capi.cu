@@ -272,7 +272,7 @@ int materialise(lbm_sim* s) {
 }
 
 int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64_t seed, int single,
-                long long single_cell) {
+                long long single_cell, const float* noise_d = nullptr) {
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
   auto launch = [&](auto tag) -> int {
     using St = decltype(tag);
@@ -280,7 +280,7 @@ int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64
     using C = typename St::C;
     k_init<St><<<grid, kBlockX, 0, s->stream>>>(s->L, (S*)s->f[0], (S*)s->f[1], (S*)s->rest, (C)rho, (C)ux, (C)uy,
                                                   (C)amp, seed, s->edge == EDGE_CHANNEL, (C)s->u_in, single,
-                                                  single_cell, store_ref(s));
+                                                  single_cell, store_ref(s), noise_d);
     CK_LAUNCH();
     return LBM_OK;
   };
@@ -718,6 +718,23 @@ int lbm_init_equilibrium(lbm_sim* s, float rho, float ux, float uy, float amp, u
   CHECK_SIM(s);
   if (!(amp >= 0.0f)) return fail(LBM_ERR_ARG, "noise amplitude %g", (double)amp);
   return launch_init(s, rho, ux, uy, amp, seed, -1, -1);
+}
+
+int lbm_init_equilibrium_noise(lbm_sim* s, float rho, float ux, float uy, const float* noise) {
+  CHECK_SIM(s);
+  if (!noise) return launch_init(s, rho, ux, uy, 0.0, 0, -1, -1);
+  const size_t n = 2 * (size_t)s->L.nx * s->L.ny;
+  const float* d = (const float*)mapped_host(noise);  // page-locked: read in place by the kernel
+  if (!d) {  // pageable: through the staging buffer (9 nx ny doubles, larger than 2 nx ny floats)
+    int rc = copy_from_host(s, s->staging_d, noise, n * sizeof(float));
+    if (rc) return rc;
+    d = (const float*)s->staging_d;
+  }
+  int rc = launch_init(s, rho, ux, uy, 0.0, 0, -1, -1, d);
+  if (rc) return rc;
+  if (d == (const float*)s->staging_d) return wait_host_copy(s);
+  CK(cudaStreamSynchronize(s->stream));  // the kernel has read the caller's buffer
+  return LBM_OK;
 }
 
 int lbm_single_cell(lbm_sim* s, int dir) {

@@ -413,14 +413,16 @@ __global__ void k_materialise(Layout L, const typename St::S* __restrict__ src, 
   }
 }
 
-// set_equil per cell with optional seeded noise, into both sets and the rest
-// plane.  In channel mode column 0 gets the inlet equilibrium (1, u_in, 0).
-// single >= 0 additionally sets population `single` of cell single_cell to 4.
+// set_equil per cell with optional seeded noise, or the caller's per-cell
+// velocity noise (noise[cell] on ux, noise[nx ny + cell] on uy, cell = x +
+// y nx), into both sets and the rest plane.  In channel mode column 0 gets
+// the inlet equilibrium (1, u_in, 0).  single >= 0 additionally sets
+// population `single` of cell single_cell to 4.
 template <class St>
 __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typename St::S* rest,
                        typename St::C rho0, typename St::C ux0, typename St::C uy0, typename St::C amp,
                        uint64_t seed, int channel, typename St::C u_in, int single, long long single_cell,
-                       StoreRef ref) {
+                       StoreRef ref, const float* noise) {
   using C = typename St::C;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
@@ -428,7 +430,10 @@ __global__ void k_init(Layout L, typename St::S* f0, typename St::S* f1, typenam
   const long long own = (long long)y * L.pitch + x;
   const uint64_t cell = (uint64_t)x + (uint64_t)y * (uint64_t)L.nx;
   C ux = ux0, uy = uy0, rho = rho0;
-  if (amp != C(0)) {
+  if (noise) {
+    ux = ux + (C)noise[cell];
+    uy = uy + (C)noise[(uint64_t)L.nx * (uint64_t)L.ny + cell];
+  } else if (amp != C(0)) {
     ux = ux + amp * (C(2.0) * noise_u01<C>(seed, cell, 0) - C(1.0));
     uy = uy + amp * (C(2.0) * noise_u01<C>(seed, cell, 1) - C(1.0));
   }

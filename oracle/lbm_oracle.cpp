@@ -289,6 +289,7 @@ struct SimBase {
   virtual void set_inlet_velocity(double u) = 0;
   virtual void set_storage_reference(bool inlet) = 0;
   virtual void init_equilibrium(double rho, double ux, double uy, double amp, uint64_t seed) = 0;
+  virtual void init_equilibrium_noise(double rho, double ux, double uy, const float* noise) = 0;
   virtual void single_cell(int dir) = 0;
   virtual void set_inlet_columns(bool any_mode = false) = 0;
   virtual void run(uint64_t n) = 0;
@@ -379,6 +380,25 @@ template <class St> struct Sim : SimBase {
         C n0 = (C)noise_u01(seed, i, 0), n1 = (C)noise_u01(seed, i, 1);
         cux = cux + a * (C(2.0) * n0 - C(1.0));
         cuy = cuy + a * (C(2.0) * n1 - C(1.0));
+      }
+      C eq[9];
+      set_equil_cell<C>(cux, cuy, (C)rho0, eq);
+      fill_cell(i, eq);
+    }
+    set_inlet_columns();
+    step = 0;
+  }
+
+  // lbm_init_equilibrium_noise: the caller's per-cell velocity noise,
+  // noise[i] on ux and noise[N + i] on uy (i = x + y X), or none.
+  void init_equilibrium_noise(double rho0, double ux0, double uy0, const float* noise) override {
+#pragma omp parallel for num_threads(threads) schedule(static)
+    for (long long ii = 0; ii < (long long)N; ii++) {
+      size_t i = (size_t)ii;
+      C cux = (C)ux0, cuy = (C)uy0;
+      if (noise) {
+        cux = cux + (C)noise[i];
+        cuy = cuy + (C)noise[N + i];
       }
       C eq[9];
       set_equil_cell<C>(cux, cuy, (C)rho0, eq);
@@ -644,6 +664,9 @@ void orc_set_inlet(orc_sim* h, double u) { ((SimBase*)h)->set_inlet_velocity(u);
 void orc_set_storage_reference(orc_sim* h, int inlet) { ((SimBase*)h)->set_storage_reference(inlet != 0); }
 void orc_init_equilibrium(orc_sim* h, double rho, double ux, double uy, double amp, uint64_t seed) {
   ((SimBase*)h)->init_equilibrium(rho, ux, uy, amp, seed);
+}
+void orc_init_equilibrium_noise(orc_sim* h, double rho, double ux, double uy, const float* noise) {
+  ((SimBase*)h)->init_equilibrium_noise(rho, ux, uy, noise);
 }
 void orc_single_cell(orc_sim* h, int dir) { ((SimBase*)h)->single_cell(dir); }
 // Rewrite column 0 at u_in in either edge mode (lbm_set_inlet_velocity without a field reset).

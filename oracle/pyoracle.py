@@ -62,6 +62,8 @@ def lib():
         L.orc_set_storage_reference.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_init_equilibrium.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_uint64]
+        L.orc_init_equilibrium_noise.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
+                                                 ctypes.c_double, ctypes.c_void_p]
         L.orc_single_cell.argtypes = [ctypes.c_void_p, ctypes.c_int]
         L.orc_apply_inlet.argtypes = [ctypes.c_void_p]
         L.orc_set_mask.argtypes = [ctypes.c_void_p, _c_u8p]
@@ -123,6 +125,14 @@ class Oracle:
 
     def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
         lib().orc_init_equilibrium(self.h, rho, ux, uy, noise, seed)
+
+    def init_equilibrium_noise(self, rho, ux, uy, noise):
+        """The caller's per-cell velocity noise: float32 (2, ny, nx) (ux, uy), or None."""
+        if noise is None:
+            lib().orc_init_equilibrium_noise(self.h, rho, ux, uy, None)
+            return
+        n = np.ascontiguousarray(noise, np.float32)
+        lib().orc_init_equilibrium_noise(self.h, rho, ux, uy, n.ctypes.data_as(ctypes.c_void_p))
 
     def single_cell(self, d):
         lib().orc_single_cell(self.h, d)

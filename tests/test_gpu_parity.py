@@ -104,6 +104,42 @@ def assert_same_state(lat, o, f64=False):
     np.testing.assert_array_equal(lat.field("jy"), jy.astype(np.float32))
 
 
+@pytest.mark.parametrize("storage,prec,f64", [(0, 0, False), (1, 1, False), (3, 3, True)])
+@pytest.mark.parametrize("pinned", [False, True])
+def test_gpu_caller_noise_initialisation(lbm, cuda_ok, oracle_mod, storage, prec, f64, pinned):
+    """lbm_init_equilibrium_noise (the survey's init with a caller noise
+    array) from pageable and from page-locked host memory: the same state as
+    the oracle's, and the same 30 steps after it."""
+    import torch
+    P = oracle_mod
+    nx, ny = 150, 70
+    rng = np.random.default_rng(11 + storage)
+    noise = (rng.uniform(-1e-2, 1e-2, (2, ny, nx))).astype(np.float32)
+    if pinned:
+        buf = torch.from_numpy(noise).pin_memory()
+        noise_in = buf.numpy()
+    else:
+        noise_in = noise
+    mask = (rng.random((ny, nx)) < 0.08).astype(np.uint8)
+    lat = lbm.Lattice(nx, ny, float(np.float32(1 / 0.6)), 1, storage)
+    o = P.Oracle(nx, ny, float(np.float32(1 / 0.6)), 1, prec)
+    lat.set_inlet_velocity(0.06)
+    o.set_inlet(float(np.float32(0.06)), apply=False)
+    lat.init_equilibrium_noise(1.0, 0.06, 0.0, noise_in)
+    o.init_equilibrium_noise(1.0, float(np.float32(0.06)), 0.0, noise)
+    t = np.float64 if f64 else np.float32
+    np.testing.assert_array_equal(lat.populations(f64=f64), o.state()[0].astype(t))
+    lat.draw_mask(mask)
+    o.set_mask(mask)
+    lat.iterate(30)
+    o.step(30)
+    assert_same_state(lat, o, f64=f64)
+    lat.init_equilibrium_noise(1.0, 0.06, 0.0, None)
+    o.init_equilibrium(1.0, float(np.float32(0.06)), 0.0, 0.0, 0)
+    np.testing.assert_array_equal(lat.populations(f64=f64), o.state()[0].astype(t))
+    lat.close()
+
+
 @pytest.mark.parametrize("edge", [0, 1])
 @pytest.mark.parametrize("kernel", [0, 1, 3, 6])
 def test_gpu_config0_both_edge_modes(lbm, cuda_ok, oracle_mod, edge, kernel):

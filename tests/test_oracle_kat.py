@@ -227,3 +227,27 @@ def test_inlet_reference_state_shrinks_the_storage_error(oracle_mod, prec):
         d = (run(prec, uref) - u64)[:, fl]
         err[uref] = float(np.linalg.norm(d) / np.linalg.norm(u64[:, fl]))
     assert err[u] * 2 <= err[0.0], err
+
+
+@pytest.mark.parametrize("prec", [0, 1, 3])
+def test_caller_noise_reproduces_the_seeded_noise(oracle_mod, prec):
+    """init_equilibrium_noise with the seeded noise written out by the caller
+    (amp (2 u - 1) per cell and component, in the arithmetic type) builds the
+    same state as init_equilibrium(amp, seed); with None it is the plain
+    equilibrium."""
+    P = oracle_mod
+    nx, ny, amp, seed = 23, 11, 1e-2, 9
+    t = np.float64 if prec == 3 else np.float32
+    u = np.array([[[P.lib().orc_noise_u01(seed, x + y * nx, c) for x in range(nx)] for y in range(ny)]
+                  for c in (0, 1)])
+    noise = (t(amp) * (t(2.0) * u.astype(t) - t(1.0))).astype(np.float32)
+    a = P.Oracle(nx, ny, 1.2, P.EDGE_CHANNEL, prec)
+    a.init_equilibrium(1.0, 0.07, 0.0, amp, seed)
+    b = P.Oracle(nx, ny, 1.2, P.EDGE_CHANNEL, prec)
+    b.init_equilibrium_noise(1.0, 0.07, 0.0, noise)
+    if prec != 3:  # the f64 arithmetic forms amp (2 u - 1) in f64, which f32 noise cannot carry
+        np.testing.assert_array_equal(a.state()[0], b.state()[0])
+    c = P.Oracle(nx, ny, 1.2, P.EDGE_CHANNEL, prec)
+    c.init_equilibrium(1.0, 0.07, 0.0, 0.0, 0)
+    b.init_equilibrium_noise(1.0, 0.07, 0.0, None)
+    np.testing.assert_array_equal(b.state()[0], c.state()[0])
