@@ -107,7 +107,7 @@ def assert_same_state(lat, o, f64=False):
 @pytest.mark.parametrize("storage,prec,f64", [(0, 0, False), (1, 1, False), (3, 3, True)])
 @pytest.mark.parametrize("pinned", [False, True])
 def test_gpu_caller_noise_initialisation(lbm, cuda_ok, oracle_mod, storage, prec, f64, pinned):
-    """lbm_init_equilibrium_noise (the survey's init with a caller noise
+    """lbm_init_equilibrium_noise (set_equil with a caller noise
     array) from pageable and from page-locked host memory: the same state as
     the oracle's, and the same 30 steps after it."""
     import torch
