@@ -465,6 +465,12 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     lbm.load_library()
+    if world > 1 and not args.slab:
+        # the scaling line is the replicated step and its e2e; the single-GPU
+        # workloads beside it (slab, storage variants, precision, closure,
+        # batched, CPU baseline) run at N = 1 only
+        args.no_slab = args.no_variants = args.no_precision = args.no_closure = args.no_batched = True
+        args.no_cpu_baseline = True
     mask = workload_mask()
     n = NX * NY
     # cells that move data: in channel mode the inlet column and solid cells are
