@@ -87,7 +87,8 @@ int lbm_get_info(const lbm_sim* sim, uint32_t* nx, uint32_t* ny, int* edge_mode,
  * NULL is CUDA's legacy default stream).  A new handle uses its own
  * non-blocking stream, which lbm_get_stream returns.  The new stream waits,
  * on the device, for the work already queued on the previous one (unless
- * either is being captured into a graph: the caller orders them then). */
+ * either is being captured into a graph: the caller orders them then), so
+ * the previous stream must still exist when the handle leaves it. */
 int lbm_set_stream(lbm_sim* sim, void* cuda_stream);
 int lbm_get_stream(const lbm_sim* sim, void** cuda_stream);
 
