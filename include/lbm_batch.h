@@ -60,6 +60,13 @@ int lbm_batch_synchronize(lbm_batch* batch);
 int lbm_batch_read_field(lbm_batch* batch, uint32_t domain, int field, float* out);
 int lbm_batch_read_populations(lbm_batch* batch, uint32_t domain, float* out);
 
+/* FP64 sums over each domain's fluid cells of the last step's density and
+ * momenta (as lbm_conservation per lattice): out[3 d .. 3 d + 2] = (mass,
+ * x momentum, y momentum) of domain d, 3 * count doubles; synchronises.
+ * Domains sharded across ranks add these up with one all-reduce; nothing
+ * else crosses between ranks. */
+int lbm_batch_conservation(lbm_batch* batch, double* out);
+
 /* Fix the schedule by hand: variant 0..5 = (ring stages, cells per thread,
  * strip columns) (4,1,256) (6,1,256) (4,2,256) (8,2,256) (6,2,512)
  * (4,2,512), the 512-column strips for f16 / bf16 only (f32 runs variants 4

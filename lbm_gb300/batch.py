@@ -4,6 +4,11 @@ persistent launch per step (include/lbm_batch.h).
 The reference has no batched form; each domain here behaves exactly like a
 `Lattice(nx, ny, omega, EDGE_CHANNEL, storage)` with `set_inlet_velocity(u)`,
 `init_equilibrium(1, u, 0, noise, seed + d)` and `draw_mask(mask)`.
+
+Across several GPUs the domains are dealt out whole (`partition`: longest
+processing time first, by cell count), each rank running a Batch of its
+share; nothing crosses between ranks but the FP64 conservation sums
+(`sharded_totals`).
 """
 import ctypes
 import json
@@ -84,6 +89,13 @@ class Batch:
         _check(self._lib.lbm_batch_read_populations(self._h, int(d), _ptr(out)))
         return out.reshape(9, int(self.ny[d]), int(self.nx[d]))
 
+    def conservation(self):
+        """FP64 (mass, x momentum, y momentum) over each domain's fluid cells,
+        shape (count, 3) (lbm_batch_conservation)."""
+        out = np.zeros(3 * len(self.nx), np.float64)
+        _check(self._lib.lbm_batch_conservation(self._h, _ptr(out)))
+        return out.reshape(-1, 3)
+
     def set_schedule(self, variant=0, dynamic=0, rows=None):
         r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
         _check(self._lib.lbm_batch_set_schedule(self._h, int(variant), int(dynamic), None if r is None else _ptr(r)))
@@ -92,6 +104,42 @@ class Batch:
         buf = ctypes.create_string_buffer(16384)
         _check(self._lib.lbm_batch_autotune(self._h, int(steps_per_trial), buf, len(buf)))
         return json.loads(buf.value.decode())
+
+
+def partition(nx, ny, world):
+    """Deal whole domains out to `world` ranks, longest processing time first:
+    domains in decreasing cell count (ties by index), each to the rank with
+    the fewest cells so far (ties to the lowest rank).  Returns one ascending
+    index array per rank.  No rank ends more than one domain's cells above
+    the mean."""
+    cells = np.asarray(nx, np.int64) * np.asarray(ny, np.int64)
+    order = sorted(range(len(cells)), key=lambda d: (-int(cells[d]), d))
+    load = [0] * world
+    parts = [[] for _ in range(world)]
+    for d in order:
+        r = min(range(world), key=lambda k: (load[k], k))
+        parts[r].append(d)
+        load[r] += int(cells[d])
+    return [np.array(sorted(p), np.int64) for p in parts]
+
+
+def sharded_totals(local, dist=None):
+    """Whole-batch FP64 totals from one rank's per-domain conservation sums
+    (Batch.conservation of its share): the ranks' column sums are gathered
+    and added in rank order, so every rank gets the same bits whatever the
+    transport.  Without a process group, the local column sums."""
+    mine = np.asarray(local, np.float64).reshape(-1, 3).sum(axis=0)
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return mine
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.from_numpy(mine).to(dev)
+    parts = [torch.empty_like(t) for _ in range(dist.get_world_size())]
+    dist.all_gather(parts, t)
+    total = np.zeros(3, np.float64)
+    for p in parts:
+        total = total + p.cpu().numpy()
+    return total
 
 
 def batched_workload(count, seed, wmin=128, wmax=1024, hmin=64, hmax=512, fmin=0.05, fmax=0.15, tau=(0.51, 0.8),

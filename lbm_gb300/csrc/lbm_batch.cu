@@ -604,6 +604,47 @@ int lbm_batch_read_field(lbm_batch* b, uint32_t domain, int field, float* out) {
   return LBM_OK;
 }
 
+int lbm_batch_conservation(lbm_batch* b, double* out) {
+  if (!b) return bfail(LBM_ERR_ARG, "null batch");
+  if (!out) return bfail(LBM_ERR_ARG, "out is null");
+  const uint32_t count = (uint32_t)b->doms.size();
+  constexpr int kBlocks = 64;  // partial sums per domain: (mass, x momentum, y momentum) x kBlocks
+  double* partial = (double*)b->d_staging;
+  double* res = partial + 3 * kBlocks;
+  if ((size_t)(3 * kBlocks + 3 * (size_t)count) * sizeof(double) > b->staging_bytes)
+    return bfail(LBM_ERR_NOMEM, "staging buffer too small for %u domains", count);
+  int rc;
+  if (!b->moments_valid && (rc = materialise_all(b))) return rc;
+  for (uint32_t d = 0; d < count; d++) {
+    const DomainHost& h = b->doms[d];
+    float* mom = (float*)(b->arena + h.off_mom);
+    if (!b->moments_valid) {  // no step since the last initialisation: moments of the current state
+      dim3 grid((h.nx + kBlock - 1) / kBlock, h.ny);
+      auto go = [&](auto tag) -> int {
+        using St = decltype(tag);
+        using S = typename St::S;
+        k_moments<St><<<grid, kBlock, 0, b->stream>>>(h.L, (const S*)(b->arena + h.off_f[b->cur]),
+                                                     (const S*)(b->arena + h.off_rest), mom, mom + h.L.ps,
+                                                     mom + 2 * h.L.ps, domain_ref(h));
+        BCK(cudaGetLastError());
+        return LBM_OK;
+      };
+      if ((rc = dispatch_st(b->storage, go))) return rc;
+      b->launches++;
+    }
+    // the partial buffer is reused domain after domain, in stream order
+    k_conservation_partial<float><<<kBlocks, 256, 0, b->stream>>>(
+        h.L, (const uint32_t*)(b->arena + h.off_mask), mom, mom + h.L.ps, mom + 2 * h.L.ps, partial);
+    BCK(cudaGetLastError());
+    k_conservation_final<<<1, 256, 0, b->stream>>>(partial, kBlocks, res + 3 * (size_t)d);
+    BCK(cudaGetLastError());
+    b->launches += 2;
+  }
+  BCK(cudaMemcpyAsync(out, res, 3 * (size_t)count * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
 int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
   int rc = check(b, domain);
   if (rc) return rc;

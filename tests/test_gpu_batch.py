@@ -161,3 +161,42 @@ def test_gpu_batch_argument_errors(lbm, cuda_ok):
         with pytest.raises(lbm.LBMError):
             b.set_schedule(7, 0)
         assert b.info()[:2] == (2, 64 * 32 + 80 * 40)
+
+
+def test_gpu_sharded_batch_matches_the_whole(lbm, cuda_ok):
+    """The domains dealt to two ranks (batch.partition), run as two batches one
+    after the other on this GPU: every domain's state and conservation sums
+    are those of the undivided batch bit for bit, the gathered totals agree
+    with its sums, and each domain's sums agree with a single lattice's
+    lbm_conservation of the same run."""
+    from lbm_gb300 import batch
+    whole, masks = make_batch(lbm, lbm.F32)
+    for d, m in enumerate(masks):
+        whole.set_mask(d, m)
+    whole.init_equilibrium(0.0, 0)
+    whole.step(33)
+    want = whole.conservation()
+    assert want.shape == (len(SIZES), 3) and np.isfinite(want).all()
+    parts = batch.partition(whole.nx, whole.ny, 2)
+    shards = []
+    for p in parts:
+        with batch.Batch(whole.nx[p], whole.ny[p], whole.omega[p], whole.u_in[p], lbm.F32) as b:
+            for i, d in enumerate(p):
+                b.set_mask(i, masks[d])
+            b.init_equilibrium(0.0, 0)
+            b.step(33)
+            got = b.conservation()
+            np.testing.assert_array_equal(got, want[p])
+            for i, d in enumerate(p):
+                np.testing.assert_array_equal(b.populations(i), whole.populations(d))
+            shards.append(got)
+    total = batch.sharded_totals(shards[0]) + batch.sharded_totals(shards[1])
+    np.testing.assert_allclose(total, want.sum(axis=0), rtol=1e-13)
+    d = 5
+    with lbm.Lattice(int(whole.nx[d]), int(whole.ny[d]), float(whole.omega[d]), lbm.EDGE_CHANNEL, lbm.F32) as lat:
+        lat.set_inlet_velocity(float(whole.u_in[d]))
+        lat.init_equilibrium(1.0, float(whole.u_in[d]), 0.0, 0.0, 0)
+        lat.draw_mask(masks[d])
+        lat.iterate(33)
+        np.testing.assert_allclose(lat.conservation(), want[d], rtol=1e-12)
+    whole.close()
