@@ -125,8 +125,10 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
             if (x0 + j < sa.L.nx) step_cell<St, EDGE_CHANNEL>(sa, x0 + j, y);
     } else {
       if constexpr (St::kDev) {
-        if (sa.ref.shift) ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(sa, xb, T.z, T.w, smem, full, empty, down);
-        else ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
+        if (sa.ref.shift)
+          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(sa, xb, T.z, T.w, smem, full, empty, down);
+        else
+          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
       } else {
         ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
       }

@@ -255,6 +255,9 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 
   // ---- consumers: CPT cells (columns x0 .. x0+CPT-1) per thread --------------
   const int lane = tid & 31;
+  auto plane = [&](int s) -> S* { return a.dstp[s]; };  // destination plane of slot s
+  auto rest_plane = [&]() -> S* { return a.rest; };
+  const bool mom_out = a.rho_out != nullptr;  // this step writes the moments
   const int e = G::kHalo + CPT * tid;  // element index of x0 in a moving segment
   const int k = (x0 >> 5) - (xb >> 5) + 4, b = x0 & 31;
   constexpr uint32_t kWin = (1u << (CPT + 2)) - 1u;
@@ -462,7 +465,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
         for (int q = 0; q < 9; q++) f[q][j] = g[q];
       }
       }
-      if (a.rho_out) {  // one uniform test per row, not one per cell
+      if (mom_out) {  // one uniform test per row, not one per cell
 #pragma unroll
         for (int j = 0; j < CPT; j++) {
           if (!act[j]) continue;
@@ -477,14 +480,14 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       if (CPT == 2 && all_act) {  // both cells: one 2-element store per plane
 #pragma unroll
         for (int q = 0; q < 9; q++) {
-          S* p = q == 4 ? a.rest + own : a.dstp[slot(q)] + own;
+          S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
           store_pair(p, f[q][0], f[q][CPT - 1]);
         }
       } else if constexpr (CPT == 4) {
         if (all_act) {  // four cells: one 8-byte store per plane
 #pragma unroll
           for (int q = 0; q < 9; q++) {
-            S* p = q == 4 ? a.rest + own : a.dstp[slot(q)] + own;
+            S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
             store_quad(p, f[q][0], f[q][1], f[q][2], f[q][3]);
           }
         } else {
@@ -493,8 +496,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
             if (!act[j]) continue;
 #pragma unroll
             for (int q = 0; q < 9; q++)
-              if (q != 4) a.dstp[slot(q)][own + j] = St::store(f[q][j], q);
-            a.rest[own + j] = St::store(f[4][j], 4);
+              if (q != 4) plane(slot(q))[own + j] = St::store(f[q][j], q);
+            rest_plane()[own + j] = St::store(f[4][j], 4);
           }
         }
       } else {
@@ -503,22 +506,22 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           if (!act[j]) continue;
 #pragma unroll
           for (int q = 0; q < 9; q++)
-            if (q != 4) a.dstp[slot(q)][own + j] = St::store(f[q][j], q);
-          a.rest[own + j] = St::store(f[4][j], 4);
+            if (q != 4) plane(slot(q))[own + j] = St::store(f[q][j], q);
+          rest_plane()[own + j] = St::store(f[4][j], 4);
         }
       }
     }
     // cells outside the fast path; inert channel cells only report moments
 #pragma unroll
     for (int j = 0; j < CPT; j++) {
-      if (EDGE == EDGE_CHANNEL && !a.rho_out) break;
+      if (EDGE == EDGE_CHANNEL && !mom_out) break;
       if (act[j] || !in_row[j]) continue;
       if (EDGE == EDGE_CHANNEL) {  // inlet column or a solid cell: inert
-        if (a.rho_out) {           // moments of its stored state
+        if (mom_out) {             // moments of its stored state
           C f[9];
 #pragma unroll
           for (int q = 0; q < 9; q++)
-            if (q != 4) f[q] = St::load(a.dstp[slot(q)][own + j], q);
+            if (q != 4) f[q] = St::load(plane(slot(q))[own + j], q);
           f[4] = St::load(reinterpret_cast<const S*>(s0 + 8 * G::kSegBytes)[CPT * tid + j], 4);
           C rho, jx, jy, aux;
           St::template moments<KM>(f, rho, aux, jx, jy, a.ref);
