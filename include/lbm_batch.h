@@ -72,7 +72,9 @@ int lbm_batch_conservation(lbm_batch* batch, double* out);
  * (4,2,512), the 512-column strips for f16 / bf16 only (f32 runs variants 4
  * and 5 with 256-column strips); dynamic 0 = tiles sorted longest first and dealt
  * round-robin to the persistent CTAs, 1 = CTAs take tiles from an atomic
- * counter; rows_per_bucket[3] = target band height for domains of height
+ * counter, 2 = dealt as 0 with each CTA's tiles run through one bulk-copy
+ * ring (the next tile's first rows are staged while the current one ends);
+ * rows_per_bucket[3] = target band height for domains of height
  * <= 128, <= 256 and taller (NULL keeps the current ones). */
 int lbm_batch_set_schedule(lbm_batch* batch, int variant, int dynamic, const int* rows_per_bucket);
 

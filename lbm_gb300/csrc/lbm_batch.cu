@@ -68,6 +68,42 @@ struct DomainDev {
 // so neighbouring bands run at the same time and, walking in opposite
 // directions, cross their shared halo rows together (one of the two reads
 // then hits L2).
+// A tile's step arguments from its domain's descriptor.
+template <class S, class C>
+__device__ void fill_args(StepArgs<S, C>& sa, const DomainDev& d, int src_i, int dst_i, int materialised,
+                          int write_moments, int rows, int* flag) {
+  sa.L = d.L;
+  sa.src = (const S*)d.f[src_i];
+  sa.dst = (S*)d.f[dst_i];
+  for (int p = 0; p < 8; p++) {
+    sa.srcp[p] = sa.src + (long long)p * d.L.ps;
+    sa.dstp[p] = sa.dst + (long long)p * d.L.ps;
+  }
+  sa.rest = (S*)d.rest;
+  sa.mask = d.mask;
+  sa.omega = (C)d.omega;
+  sa.ref = d.ref;
+  sa.materialised = materialised;
+  sa.rows = rows;
+  sa.row0 = 0;
+  sa.row_end = d.L.ny;
+  C* mom = (C*)d.mom;
+  sa.rho_out = write_moments ? mom : nullptr;
+  sa.jx_out = write_moments ? mom + d.L.ps : nullptr;
+  sa.jy_out = write_moments ? mom + 2 * d.L.ps : nullptr;
+  sa.flag = flag;
+  sa.closure = nullptr;
+  sa.fallback = nullptr;
+  sa.tau0 = sa.drift = 0.0f;
+}
+
+// Schedules: 0 static (tiles longest first, dealt round robin), 1 atomic
+// tickets, 2 static through one ring: a CTA's tiles follow each other in its
+// bulk-copy ring without draining it, the producer staging the next tile's
+// first rows while the consumers finish the current one.  The tile
+// arguments are then double-buffered: the producer writes tile k's copy just
+// before its first stage (the consumers read it after that stage arrives)
+// once the consumers have released the copy of tile k - 2 (`args_free`).
 template <class St, int NS, int CPT, int W>
 __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (CPT == 1 ? 4 : 6))
     k_batch_step(const DomainDev* __restrict__ doms, const int4* __restrict__ tiles, int ntiles, int src_i, int dst_i,
@@ -77,11 +113,58 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ __align__(8) uint64_t full[NS];
   __shared__ __align__(8) uint64_t empty[NS];
+  __shared__ __align__(8) uint64_t args_free[2];
   __shared__ StepArgs<S, C> sa;
+  __shared__ StepArgs<S, C> sa2[2];
   __shared__ int ticket, stop;
+  if (dynamic == 2 && !materialised) {
+    constexpr int kConsumers = W / CPT;
+    constexpr int kConsumerWarps = kConsumers / 32;
+    const int lane = threadIdx.x & 31;
+    const bool producer = (int)threadIdx.x >= kConsumers;
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < NS; i++) {
+        mbar_init(smem_addr(&full[i]), 1);
+        mbar_init(smem_addr(&empty[i]), kConsumerWarps);
+      }
+      mbar_init(smem_addr(&args_free[0]), kConsumerWarps);
+      mbar_init(smem_addr(&args_free[1]), kConsumerWarps);
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    uint32_t g = 0;  // rows staged for this CTA's earlier tiles
+    int k = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, k++) {
+      const int4 T = tiles[t];
+      const int xb = T.y & 0x3FFFFFFF;
+      const bool down = (T.y >> 30) != 0;
+      const bool last = t + (int)gridDim.x >= ntiles;
+      StepArgs<S, C>& A = sa2[k & 1];
+      if (producer) {
+        // the copy of tile k - 2's arguments is free once every consumer warp is done with that tile
+        if (k >= 2 && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&args_free[k & 1]), (uint32_t)(((k - 2) >> 1) & 1)))) {
+          if (lane == 0) atomicOr(flag, 2);
+        }
+        if (lane == 0) fill_args(A, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag);
+        __syncwarp();
+      }
+      if (St::kDev && doms[T.x].ref.shift)
+        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
+      else
+        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
+      if (!producer) {
+        __syncwarp();
+        if (lane == 0) mbar_arrive(smem_addr(&args_free[k & 1]));
+      }
+      g += (uint32_t)(T.w - T.z + 2);
+      if (*(volatile int*)flag & 2) break;  // a wait ran out somewhere: stop early
+    }
+    return;
+  }
   for (int it = 0;; it++) {
     if (threadIdx.x == 0) {
-      ticket = dynamic ? atomicAdd(counter, 1) : (int)blockIdx.x + it * (int)gridDim.x;
+      ticket = dynamic == 1 ? atomicAdd(counter, 1) : (int)blockIdx.x + it * (int)gridDim.x;
       stop = (*(volatile int*)flag & 2) != 0;  // a wait ran out somewhere: stop early
     }
     __syncthreads();
@@ -90,32 +173,7 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
     const int4 T = tiles[t];
     const int xb = T.y & 0x3FFFFFFF;
     const bool down = (T.y >> 30) != 0;
-    if (threadIdx.x == 0) {
-      const DomainDev& d = doms[T.x];
-      sa.L = d.L;
-      sa.src = (const S*)d.f[src_i];
-      sa.dst = (S*)d.f[dst_i];
-      for (int p = 0; p < 8; p++) {
-        sa.srcp[p] = sa.src + (long long)p * d.L.ps;
-        sa.dstp[p] = sa.dst + (long long)p * d.L.ps;
-      }
-      sa.rest = (S*)d.rest;
-      sa.mask = d.mask;
-      sa.omega = (C)d.omega;
-      sa.ref = d.ref;
-      sa.materialised = materialised;
-      sa.rows = T.w - T.z;
-      sa.row0 = 0;
-      sa.row_end = d.L.ny;
-      C* mom = (C*)d.mom;
-      sa.rho_out = write_moments ? mom : nullptr;
-      sa.jx_out = write_moments ? mom + d.L.ps : nullptr;
-      sa.jy_out = write_moments ? mom + 2 * d.L.ps : nullptr;
-      sa.flag = flag;
-      sa.closure = nullptr;
-      sa.fallback = nullptr;
-      sa.tau0 = sa.drift = 0.0f;
-    }
+    if (threadIdx.x == 0) fill_args(sa, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag);
     __syncthreads();
     if (materialised) {
       const int x0 = xb + CPT * (int)threadIdx.x;
@@ -157,7 +215,7 @@ StoreRef domain_ref(const DomainHost& h) { return make_store_ref(0.0f, h.omega);
 
 struct Config {
   int variant = 0;     // index into kVariants
-  int dynamic = 0;     // 0: static longest-first round robin, 1: atomic tickets
+  int dynamic = 0;     // 0: static longest-first round robin, 1: atomic tickets, 2: static through one ring
   int rows[kBuckets] = {32, 32, 32};
 };
 
@@ -290,7 +348,7 @@ int launch_step(lbm_batch* b, bool write_moments, int* counter) {
   const size_t smem = (size_t)NS * stage_bytes(b->storage, W);
   const int src = b->cur, dst = b->materialised ? b->cur : 1 - b->cur;
   int mat = b->materialised ? 1 : 0, wm = write_moments ? 1 : 0, dyn = b->cfg.dynamic;
-  if (dyn) BCK(cudaMemsetAsync(counter, 0, sizeof(int), b->stream));
+  if (dyn == 1) BCK(cudaMemsetAsync(counter, 0, sizeof(int), b->stream));
   void* args[] = {&b->d_doms, &b->d_tiles, &b->ntiles, (void*)&src, (void*)&dst, &mat, &wm, &dyn, &counter, &b->d_flag};
   auto go = [&](auto tag) -> int {
     using St = decltype(tag);
@@ -672,7 +730,7 @@ int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
 
 int lbm_batch_set_schedule(lbm_batch* b, int variant, int dynamic, const int* rows_per_bucket) {
   if (!b) return bfail(LBM_ERR_ARG, "null batch");
-  if (variant < 0 || variant >= kNumVariants || (dynamic != 0 && dynamic != 1))
+  if (variant < 0 || variant >= kNumVariants || dynamic < 0 || dynamic > 2)
     return bfail(LBM_ERR_ARG, "bad schedule");
   b->cfg.variant = variant;
   b->cfg.dynamic = dynamic;
@@ -733,7 +791,7 @@ int lbm_batch_autotune(lbm_batch* b, uint32_t steps_per_trial, char* report, siz
   // stage 1: ring depth x cells per thread x schedule
   const int variants = b->storage == STORE_F32 ? 2 : kNumVariants;
   for (int v = 0; v < variants; v++)
-    for (int dyn = 0; dyn < 2; dyn++) {
+    for (int dyn = 0; dyn < 3; dyn++) {
       b->cfg = best_cfg;
       b->cfg.variant = v;
       b->cfg.dynamic = dyn;
@@ -762,7 +820,7 @@ int lbm_batch_autotune(lbm_batch* b, uint32_t steps_per_trial, char* report, siz
            "\"schedule\": \"%s\", "
            "\"rows_per_band\": {\"ny<=128\": %d, \"ny<=256\": %d, \"ny>256\": %d}, \"ms_per_step\": %.5f, "
            "\"persistent_ctas\": %d, \"tiles\": %d}}",
-           NS, CPT, strip_of(b->cfg.variant, b->storage), b->cfg.dynamic ? "dynamic" : "static_longest_first", b->cfg.rows[0], b->cfg.rows[1], b->cfg.rows[2],
+           NS, CPT, strip_of(b->cfg.variant, b->storage), b->cfg.dynamic == 1 ? "dynamic" : (b->cfg.dynamic == 2 ? "static_one_ring" : "static_longest_first"), b->cfg.rows[0], b->cfg.rows[1], b->cfg.rows[2],
            best / T, b->grid, b->ntiles);
   rep += buf;
   b->report = rep;

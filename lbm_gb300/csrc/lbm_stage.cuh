@@ -178,9 +178,17 @@ template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / C
 // The order of rows does not change any cell's result.  KM is the storage
 // reference's shift mode (`shifted`): 0 or 1 where the caller has branched on
 // StoreRef::shift once for the whole tile.
+//
+// A CTA may run several tiles through one ring without draining it between
+// them: g0 is the number of rows staged for the CTA's earlier tiles (global
+// staged row g lives in slot g % NS, in phase (g / NS) & 1), `init` arms the
+// barriers (first tile only), and `drain` makes the producer wait for its last
+// copies before returning (last tile only; otherwise the consumers release
+// the tile's last two staged rows, which the next tile does not read).
 template <class St, int EDGE, int NS, int CPT, bool CL, int W, int KM, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
-                                        uint64_t* empty, bool down = false) {
+                                        uint64_t* empty, bool down = false, uint32_t g0 = 0, bool init = true,
+                                        bool drain = true) {
   using S = typename St::S;
   static_assert(CPT == 1 || (CPT == 2 && EDGE == EDGE_CHANNEL) ||
                     (CPT == 4 && EDGE == EDGE_CHANNEL && sizeof(S) == 2),
@@ -198,15 +206,17 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   // y0 - 1 + i upwards, y1 - i downwards
   const int n_stage = y1 - y0 + 2;
   const int r_first = down ? y1 : y0 - 1, r_step = down ? -1 : 1;
-  if (tid == 0) {
-    for (int i = 0; i < NS; i++) {
-      mbar_init(smem_addr(&full[i]), 1);
-      mbar_init(smem_addr(&empty[i]), kConsumerWarps);
+  if (init) {
+    if (tid == 0) {
+      for (int i = 0; i < NS; i++) {
+        mbar_init(smem_addr(&full[i]), 1);
+        mbar_init(smem_addr(&empty[i]), kConsumerWarps);
+      }
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     }
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
   }
-  __syncthreads();
 
   if (producer) {
     // The whole warp runs the loop on warp-uniform values; one elected lane
@@ -218,11 +228,13 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     const uint32_t rest_bytes = ((uint32_t)(w * (int)sizeof(S)) + 15u) & ~15u;
     const uint32_t rec_bytes = CL ? ((uint32_t)(w * 4) + 15u) & ~15u : 0u;
     const uint32_t copy_bytes = 8u * seg_bytes + rest_bytes + G::kMaskBytes + rec_bytes;
-    int i = 0, s = 0;
-    uint32_t empty_parity = 1;  // flips each time the ring wraps; the first round needs no wait
+    int i = 0, s = (int)(g0 % NS);
+    // flips each time the ring wraps; the CTA's first NS staged rows need no wait
+    uint32_t empty_parity = ((g0 / NS) & 1u) ^ 1u;
     bool ok = true;
     for (; i < n_stage; i++) {
-      if (i >= NS && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&empty[s]), empty_parity))) {
+      if (g0 + (uint32_t)i >= (uint32_t)NS &&
+          !__all_sync(0xffffffffu, mbar_wait(smem_addr(&empty[s]), empty_parity))) {
         ok = false;
         break;
       }
@@ -248,7 +260,11 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       if (!ok) atomicOr(a.flag, 2);
       // no copy may be in flight when the CTA exits: wait (bounded) for the
       // last NS stages issued
-      for (int q = max(0, i - NS); q < i; q++) mbar_wait(smem_addr(&full[q % NS]), (uint32_t)((q / NS) & 1));
+      if (drain || !ok) {
+        const uint32_t end = g0 + (uint32_t)i;
+        for (uint32_t q = end > (uint32_t)NS ? end - (uint32_t)NS : 0u; q < end; q++)
+          mbar_wait(smem_addr(&full[q % NS]), (q / NS) & 1u);
+      }
     }
     return;
   }
@@ -257,21 +273,24 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   const int lane = tid & 31;
   auto plane = [&](int s) -> S* { return a.dstp[s]; };  // destination plane of slot s
   auto rest_plane = [&]() -> S* { return a.rest; };
-  const bool mom_out = a.rho_out != nullptr;  // this step writes the moments
   const int e = G::kHalo + CPT * tid;  // element index of x0 in a moving segment
   const int k = (x0 >> 5) - (xb >> 5) + 4, b = x0 & 31;
   constexpr uint32_t kWin = (1u << (CPT + 2)) - 1u;
   // ring slots of the three staged rows around y, in arrival order (the
   // oldest is y-1 walking upwards, y+1 walking downwards), and the phase
   // parity of the newest
-  int slot_m = 0, slot_0 = 1 % NS, slot_p = 2 % NS;
-  uint32_t parity_p = 2 / NS;
-  bool ok = mbar_wait(smem_addr(&full[0]), 0) && mbar_wait(smem_addr(&full[1 % NS]), 1 / NS);
+  int slot_m = (int)(g0 % NS), slot_0 = (int)((g0 + 1) % NS), slot_p = (int)((g0 + 2) % NS);
+  uint32_t parity_p = ((g0 + 2) / NS) & 1u;
+  bool ok = mbar_wait(smem_addr(&full[slot_m]), (g0 / NS) & 1u) &&
+            mbar_wait(smem_addr(&full[slot_0]), ((g0 + 1) / NS) & 1u);
   uint32_t wa = 0, w0 = 0;  // mask windows of the oldest row and of row y
   if (ok) {
-    wa = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + G::kMaskOff), k, b);
+    wa = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_m * kStage + G::kMaskOff), k, b);
     w0 = winN<CPT>(reinterpret_cast<const uint32_t*>(smem + (size_t)slot_0 * kStage + G::kMaskOff), k, b);
   }
+  // (the tile's arguments are read only after its first stage has arrived:
+  // through one ring, the producer writes them just before that stage)
+  const bool mom_out = a.rho_out != nullptr;  // this step writes the moments
   // column classes; the channel inlet (x = 0) is inert, the channel outflow
   // (x = nx-1) pulls its x+1 populations from its own column
   bool in_row[CPT], xin[CPT];
@@ -543,6 +562,15 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
     slot_m = slot_0;
     slot_0 = slot_p;
     if (++slot_p == NS) { slot_p = 0; parity_p ^= 1u; }
+  }
+  // one ring through several tiles: this tile's last two staged rows are
+  // released as well (the loop released each row's oldest only)
+  if (!drain && ok) {
+    __syncwarp();
+    if (lane == 0) {
+      mbar_arrive(smem_addr(&empty[slot_m]));
+      mbar_arrive(smem_addr(&empty[slot_0]));
+    }
   }
   if (!(rho_sum - rho_sum == C(0))) atomicOr(a.flag, 1);
   if (!ok) atomicOr(a.flag, 2);

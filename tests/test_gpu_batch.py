@@ -73,7 +73,9 @@ def test_gpu_batch_matches_oracle_per_domain(lbm, cuda_ok, oracle_mod, storage, 
         assert b.info()[2] == 50
 
 
-SCHEDULES = [(v, dyn, rows) for v in range(6) for dyn in (0, 1) for rows in ([32, 32, 32], [5, 64, 7])]
+# (variant, schedule: 0 static, 1 tickets, 2 static through one ring, band rows); [5, 64, 7] gives
+# tiles shorter than the deepest ring, so one ring carries several of a CTA's tiles at once
+SCHEDULES = [(v, dyn, rows) for v in range(6) for dyn in (0, 1, 2) for rows in ([32, 32, 32], [5, 64, 7], [3, 2, 3])]
 
 
 @pytest.mark.parametrize("storage", [0, 1])
@@ -94,6 +96,27 @@ def test_gpu_batch_every_schedule_gives_the_same_state(lbm, cuda_ok, storage):
                 for d in range(b.count):
                     np.testing.assert_array_equal(got[d], ref[d], err_msg="schedule %s domain %d" %
                                                   ((v, dyn, rows), d))
+
+
+@pytest.mark.parametrize("storage,prec", [(0, 0), (1, 1)])
+def test_gpu_batch_one_ring_matches_oracle(lbm, cuda_ok, oracle_mod, storage, prec):
+    """The static schedule through one ring (2), with short bands so that a
+    CTA's tiles follow each other within a single ring depth: every domain
+    bit-exact against its oracle run over graph replays and plain steps."""
+    P = oracle_mod
+    b, masks = make_batch(lbm, storage, seed=6)
+    with b:
+        b.set_schedule(3 if storage else 0, 2, [4, 3, 5])
+        b.init_equilibrium(1e-2, 5)
+        orc = []
+        for d, m in enumerate(masks):
+            b.set_mask(d, m)
+            orc.append(oracle_for(P, b, d, prec, m, 1e-2, 5))
+        b.step(23)
+        b.step(1)
+        for d, o in enumerate(orc):
+            o.step(24)
+            assert_domain(b, d, o)
 
 
 def test_gpu_batch_two_cells_per_thread_in_f32(lbm, cuda_ok, oracle_mod):
@@ -122,7 +145,7 @@ def test_gpu_batch_autotune_then_parity(lbm, cuda_ok, oracle_mod):
         ch = rep["chosen"]
         assert ch["ring_stages"] in (4, 6, 8) and ch["cells_per_thread"] in (1, 2)
         assert ch["strip_columns"] in (256, 512)
-        assert ch["schedule"] in ("dynamic", "static_longest_first")
+        assert ch["schedule"] in ("dynamic", "static_longest_first", "static_one_ring")
         assert len(rep["trials"]) >= 8 and ch["ms_per_step"] > 0
         b.init_equilibrium(1e-3, 1)
         b.step(41)
