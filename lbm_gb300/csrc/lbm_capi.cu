@@ -367,11 +367,13 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     bands = (span + rows - 1) / rows;
   }
   a.rows = rows;
-  // 16-bit storage: programmatic dependent launch.  The grid may be
+  // Programmatic dependent launch from 2^19 cells up: the grid may be
   // scheduled while the previous step's grid drains; the kernel waits for
   // that grid to complete (griddepcontrol.wait) before it touches global
-  // memory.  Measured 1.3 % faster for 16-bit storage and 1.8 % slower for
-  // f32, whose launches stay plain (griddepcontrol is then a no-op).
+  // memory.  Measured per step, f32 / f16: 1024 x 512 5 % / 4 % faster,
+  // 2048 x 1024 neutral / 3 % faster, 4096 x 2048 within 0.3 %; 512 x 256 25 %
+  // / 11 % slower, so smaller lattices launch plain (griddepcontrol is then a
+  // no-op).
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((s->L.nx + W - 1) / W, bands);
   cfg.blockDim = dim3(TPB);
@@ -381,7 +383,7 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = sizeof(typename St::S) == 2 ? 1 : 0;
+  cfg.numAttrs = (long long)s->L.nx * s->L.ny >= (1LL << 19) ? 1 : 0;
   CK(cudaLaunchKernelEx(&cfg, kern, a));
   return LBM_OK;
 }
