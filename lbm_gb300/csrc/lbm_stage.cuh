@@ -640,7 +640,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int t
       unsigned int v;
       asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
       if (v >= target) break;
-      if (spins > (1u << 22)) {
+      if (spins > (1u << 24)) {
         atomicOr(flag, 2);
         ok = false;
         break;
