@@ -198,11 +198,8 @@ int lbm_step_rows(lbm_sim* sim, uint32_t y0, uint32_t y1, int flags);
  * omega, the step kernel, the launch shape, the stream or the closure
  * change).  On by default; results are the same either way.  Not on the
  * legacy default stream, which cannot be captured, nor while the caller is
- * capturing the lattice's stream.  Lattices below 2^19 cells instead run a
- * call of two or more steps (from a state that is not just edited) as ONE
- * cooperative launch with a grid-wide barrier between steps, for the default
- * staged kernels (3 for f32, 7 for 16-bit storage), with the closure too.
- * enable = 0 turns both off (a launch per step) and frees the graphs. */
+ * capturing the lattice's stream.  enable = 0 turns it off and frees the
+ * graphs. */
 int lbm_set_graphs(lbm_sim* sim, int enable);
 
 /* Wait for queued work; returns LBM_ERR_STATE if a step saw a non-finite density. */

@@ -270,11 +270,6 @@ class Lattice:
     def set_inlet_velocity(self, ux, reset_field=False):
         _check(_lib.lbm_set_inlet_velocity(self._h, float(ux), 1 if reset_field else 0))
 
-    def set_graphs(self, enable):
-        """Replay captured step graphs and fuse small lattices' calls into one
-        launch (the default), or launch every step on its own."""
-        _check(_lib.lbm_set_graphs(self._h, 1 if enable else 0))
-
     def set_storage_reference(self, inlet):
         """16-bit storage: keep the words relative to the rest weights (False,
         the default: f - w) or to the inlet equilibrium (True: smaller words,

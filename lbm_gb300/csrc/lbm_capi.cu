@@ -8,7 +8,6 @@
 #include <algorithm>
 #include <cstdarg>
 #include <cmath>
-#include <type_traits>
 
 #include "../../include/lbm.h"
 #include "lbm_kernels.cuh"
@@ -100,7 +99,6 @@ struct lbm_sim {
   void* mask_base = nullptr;
   void* mom = nullptr;  // rho, jx, jy planes
   int* flag_d = nullptr;
-  unsigned int* bar_d = nullptr;  // grid-barrier counter of the multi-step launch
   double* partial_d = nullptr;  // reduction partials
   float* staging_d = nullptr;   // readback staging (9 planes of f64 at most)
   size_t staging_bytes = 0;
@@ -325,7 +323,7 @@ void release(lbm_sim* s) {
   for (auto& g : s->run_graph)
     if (g) cudaGraphExecDestroy(g);
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
-  cudaFree(s->flag_d); cudaFree(s->bar_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
+  cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
   cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
   if (s->copied) cudaEventDestroy(s->copied);
   if (s->switched) cudaEventDestroy(s->switched);
@@ -513,7 +511,6 @@ int lbm_create(uint32_t nx, uint32_t ny, float omega, int edge_mode, int storage
   (void)plane;
   if ((rc = alloc(&s->mom, 3 * (size_t)s->L.ps * s->cs))) return rc;
   if ((rc = alloc((void**)&s->flag_d, 4))) return rc;
-  if ((rc = alloc((void**)&s->bar_d, 4))) return rc;
   if ((rc = alloc((void**)&s->partial_d, (size_t)kReduceBlocks * 3 * 8))) return rc;
   s->staging_bytes = (size_t)9 * nx * ny * 8;
   if ((rc = alloc((void**)&s->staging_d, s->staging_bytes))) return rc;
@@ -879,101 +876,6 @@ static int capture_steps(lbm_sim* s, cudaGraphExec_t& out, uint32_t n, bool mome
   return LBM_OK;
 }
 
-extern "C++" {
-// Lattices below this many cells take a whole lbm_step call in one
-// cooperative launch (k_step_ws_multi) where its kernel variant allows: a
-// launch per step costs them as much as the step.
-constexpr long long kMultiCells = 1LL << 19;
-
-// The multi-step launch of n >= 2 steps from a non-materialised state, for
-// the default staged variants (f32 kernel 3; 16-bit kernel 7), closure on or
-// off.  Returns kNoMulti (nothing launched) where it does not apply.
-constexpr int kNoMulti = -1;
-template <class St, int EDGE, int NS, int CPT, bool CL>
-static int launch_multi_k(lbm_sim* s, uint32_t n) {
-  using S = typename St::S;
-  using C = typename St::C;
-  constexpr int W = kStageW;
-  constexpr int TPB = stage_threads<CPT, W>();
-  const size_t smem = (size_t)NS * stage_bytes<S, W, CL>();
-  auto kern = k_step_ws_multi<St, EDGE, NS, CPT, CL, W>;
-  CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int occ = 0;
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, TPB, smem));
-  if (occ < 1) return kNoMulti;
-  const int strips = (s->L.nx + W - 1) / W;
-  const int rows = band_rows(s, occ, W, s->L.ny);
-  const int bands = (s->L.ny + rows - 1) / rows;
-  if ((long long)strips * bands > (long long)occ * s->sms) return kNoMulti;  // not all resident: no grid barrier
-  StepArgs<S, C> a[2];
-  for (int k = 0; k < 2; k++) {
-    const int src = k == 0 ? s->cur : 1 - s->cur;
-    a[k].L = s->L;
-    a[k].src = (const S*)s->f[src];
-    a[k].dst = (S*)s->f[1 - src];
-    for (int p = 0; p < 8; p++) {
-      a[k].srcp[p] = a[k].src + (long long)p * s->L.ps;
-      a[k].dstp[p] = a[k].dst + (long long)p * s->L.ps;
-    }
-    a[k].rest = (S*)s->rest;
-    a[k].mask = s->mask_d;
-    a[k].omega = (C)s->omega;
-    a[k].materialised = 0;
-    a[k].rows = rows;
-    a[k].row0 = 0;
-    a[k].row_end = s->L.ny;
-    a[k].rho_out = a[k].jx_out = a[k].jy_out = nullptr;  // the kernel sets them for its last step
-    a[k].flag = s->flag_d;
-    a[k].closure = CL ? s->closure_d : nullptr;
-    a[k].tau0 = 1.0f / s->omega;
-    a[k].drift = s->drift;
-    a[k].fallback = CL ? s->fallback_d : nullptr;
-    a[k].ref = store_ref(s);
-  }
-  CK(cudaMemsetAsync(s->bar_d, 0, sizeof(unsigned int), s->stream));
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(strips, bands);
-  cfg.blockDim = dim3(TPB);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s->stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeCooperative;
-  attr[0].val.cooperative = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  CK(cudaLaunchKernelEx(&cfg, kern, a[0], a[1], (int)n, (C*)mom_plane(s, 0), s->bar_d));
-  s->launches++;
-  s->steps += n;
-  s->cur ^= (int)(n & 1u);
-  s->moments_valid = true;
-  return LBM_OK;
-}
-
-static int launch_multi(lbm_sim* s, uint32_t n) {
-  if (s->storage == STORE_F64 || s->materialised || n < 2 || (long long)s->L.nx * s->L.ny >= kMultiCells)
-    return kNoMulti;
-  const bool cl = s->closure_on;
-  auto go = [&](auto tag) -> int {
-    using St = decltype(tag);
-    if constexpr (std::is_same<St, StF32>::value) {
-      if (s->kernel == 3) {
-        if (s->edge == EDGE_REF) return cl ? kNoMulti : launch_multi_k<St, EDGE_REF, 4, 1, false>(s, n);
-        return cl ? launch_multi_k<St, EDGE_CHANNEL, 4, 1, true>(s, n)
-                  : launch_multi_k<St, EDGE_CHANNEL, 4, 1, false>(s, n);
-      }
-    } else if constexpr (!std::is_same<St, StF64>::value) {  // 16-bit storage
-      if (s->kernel == 7) {
-        if (s->edge == EDGE_REF) return cl ? kNoMulti : launch_multi_k<St, EDGE_REF, 6, 1, false>(s, n);
-        return cl ? launch_multi_k<St, EDGE_CHANNEL, 6, 2, true>(s, n)
-                  : launch_multi_k<St, EDGE_CHANNEL, 6, 2, false>(s, n);
-      }
-    }
-    return kNoMulti;
-  };
-  return dispatch_storage(s->storage, go);
-}
-}  // extern "C++"
-
 int lbm_step(lbm_sim* s, uint32_t n) {
   CHECK_SIM(s);
   if (n == 0) return LBM_OK;
@@ -988,10 +890,6 @@ int lbm_step(lbm_sim* s, uint32_t n) {
            (s->storage == STORE_F64 || s->kernel < 2 ||
             s->staged_variant == 2 * s->kernel + (s->closure_on ? 1 : 0));
   };
-  if (s->use_graphs && capturing == cudaStreamCaptureStatusNone) {  // small lattices: the call in one launch
-    const int rc = launch_multi(s, n);
-    if (rc != kNoMulti) return rc;
-  }
   if (n >= 2 && n <= (uint32_t)kRunGraphMax && steady()) {
     const int c = s->cur;
     if (!s->run_graph[c] || s->run_n[c] != n || !(s->run_key[c] == graph_key(s))) {

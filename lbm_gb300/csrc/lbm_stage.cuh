@@ -623,88 +623,4 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
   }
 }
 
-// Grid-wide barrier of a cooperative launch: every CTA's thread 0 adds one
-// to `count` and waits (bounded, about a second) until it reaches `target`.
-// The stores of this step are made visible to the next step's bulk copies
-// (the async proxy) on any multiprocessor first.  False if the wait ran out
-// (error bit 2 set).
-__device__ __forceinline__ bool grid_barrier(unsigned int* count, unsigned int target, int* flag) {
-  __shared__ int barrier_ok;
-  asm volatile("fence.proxy.async.global;" ::: "memory");
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    atomicAdd(count, 1u);
-    bool ok = true;
-    for (uint32_t spins = 0;; spins++) {
-      unsigned int v;
-      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(count) : "memory");
-      if (v >= target) break;
-      if (spins > (1u << 24)) {
-        atomicOr(flag, 2);
-        ok = false;
-        break;
-      }
-      __nanosleep(64);
-    }
-    __threadfence();
-    barrier_ok = ok;
-  }
-  __syncthreads();
-  return barrier_ok != 0;
-}
-
-// Several steps in one cooperative launch, for lattices small enough that a
-// launch per step costs as much as the step: the staged step's one-wave grid
-// (every CTA resident), steps separated by a grid-wide barrier.  args[0]
-// steps from the current buffer, args[1] back; each CTA's ring runs through
-// all steps without being re-armed.  The last step writes the moments
-// (`mom`, three planes, or none).
-template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
-__global__ void __launch_bounds__(stage_threads<CPT, W>(),
-                                  W != kStageW ? 3 : (CPT == 1 ? 4 : (CPT == 2 ? (sizeof(typename St::S) == 8 ? 5 : 6) : 8)))
-    k_step_ws_multi(StepArgs<typename St::S, typename St::C> a0, StepArgs<typename St::S, typename St::C> a1,
-                    int nsteps, typename St::C* mom, unsigned int* bar) {
-  using S = typename St::S;
-  using C = typename St::C;
-  extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ __align__(8) uint64_t full[NS];
-  __shared__ __align__(8) uint64_t empty[NS];
-  __shared__ StepArgs<S, C> sa[2];
-  if (threadIdx.x == 0) {
-    sa[0] = a0;
-    sa[1] = a1;
-  }
-  __syncthreads();
-  const int xb = blockIdx.x * W;
-  const int y0 = a0.row0 + blockIdx.y * a0.rows;
-  const int y1 = min(y0 + a0.rows, a0.row_end);
-  const bool down = sizeof(S) == 4 && (blockIdx.y & 1u) != 0u;
-  const unsigned int nblocks = gridDim.x * gridDim.y;
-  uint32_t g = 0;
-  for (int s = 0; s < nsteps; s++) {
-    StepArgs<S, C>& A = sa[s & 1];
-    if (s == nsteps - 1 && mom && threadIdx.x == 0) {  // the last step writes the moments
-      A.rho_out = mom;
-      A.jx_out = mom + A.L.ps;
-      A.jy_out = mom + 2 * A.L.ps;
-    }
-    __syncthreads();
-    if (y0 < y1) {  // uniform per CTA; a CTA without rows still takes part in the barriers
-      const bool last = s == nsteps - 1;
-      if (St::kDev && A.ref.shift)
-        ws_tile<St, EDGE, NS, CPT, CL, W, 1>(A, xb, y0, y1, smem, full, empty, down, g, s == 0, last);
-      else
-        ws_tile<St, EDGE, NS, CPT, CL, W, 0>(A, xb, y0, y1, smem, full, empty, down, g, s == 0, last);
-      g += (uint32_t)(y1 - y0 + 2);
-    }
-    if (s + 1 < nsteps && !grid_barrier(bar, (unsigned int)(s + 1) * nblocks, A.flag)) break;
-  }
-  // after a barrier that ran out, no copy may still be in flight when the CTA
-  // exits: the producer waits (bounded) for its last stages
-  if (threadIdx.x == (unsigned)(W / CPT) && y0 < y1)
-    for (uint32_t q = g > (uint32_t)NS ? g - (uint32_t)NS : 0u; q < g; q++)
-      mbar_wait(smem_addr(&full[q % NS]), (q / NS) & 1u);
-}
-
 }  // namespace lbm
