@@ -367,13 +367,14 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
     bands = (span + rows - 1) / rows;
   }
   a.rows = rows;
-  // Programmatic dependent launch from 2^19 cells up: the grid may be
-  // scheduled while the previous step's grid drains; the kernel waits for
-  // that grid to complete (griddepcontrol.wait) before it touches global
-  // memory.  Measured per step, f32 / f16: 1024 x 512 5 % / 4 % faster,
-  // 2048 x 1024 neutral / 3 % faster, 4096 x 2048 within 0.3 %; 512 x 256 25 %
-  // / 11 % slower, so smaller lattices launch plain (griddepcontrol is then a
-  // no-op).
+  // Programmatic dependent launch: the grid may be scheduled while the
+  // previous step's grid drains; the kernel waits for that grid to complete
+  // (griddepcontrol.wait) before it touches global memory.  Measured per
+  // step against plain launches, f32 / f16: 512 x 256 25 % / 11 % slower;
+  // 1024 x 512 5 % / 4 % faster; 2048 x 1024 0 to 1.6 % slower / 3 % faster;
+  // 4096 x 2048 0.3 % faster to 1.5 % slower (two boxes) / within 0.2 %.  So
+  // 16-bit storage uses it from 2^19 cells up and f32 from 2^19 to 2^21;
+  // other launches stay plain (griddepcontrol is then a no-op).
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((s->L.nx + W - 1) / W, bands);
   cfg.blockDim = dim3(TPB);
@@ -383,7 +384,8 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
   attr[0].val.programmaticStreamSerializationAllowed = 1;
   cfg.attrs = attr;
-  cfg.numAttrs = (long long)s->L.nx * s->L.ny >= (1LL << 19) ? 1 : 0;
+  const long long cells = (long long)s->L.nx * s->L.ny;
+  cfg.numAttrs = cells >= (1LL << 19) && (sizeof(typename St::S) == 2 || cells < (1LL << 21)) ? 1 : 0;
   CK(cudaLaunchKernelEx(&cfg, kern, a));
   return LBM_OK;
 }
