@@ -188,6 +188,43 @@ def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0, stor
     return ms / steps, launches
 
 
+def time_batched_split(lbm, torch, storage, steps, warmup, min_seconds, rank=0, world=1, dist=None, count=512,
+                       seed=1):
+    """The batched workload's 512 domains dealt whole to `world` ranks by cell
+    count (batch.partition), each rank autotuning and stepping its share as
+    one batch; strong scaling (the whole workload is fixed).  Returns the
+    whole-job MLUPS over all cells and ms per step (median call of `steps`
+    steps, max over ranks), each rank's share, and the FP64 conservation
+    totals gathered over the ranks (batch.sharded_totals)."""
+    import numpy as np
+    from lbm_gb300 import batch as B
+    nx, ny, om, u, masks = B.batched_workload(count, seed)
+    parts = B.partition(nx, ny, world)
+    mine = parts[rank]
+    cells = int((nx.astype(np.int64) * ny).sum())
+    with B.Batch(nx[mine], ny[mine], om[mine], u[mine], storage) as b:
+        for i, d in enumerate(mine):
+            b.set_mask(i, masks[d])
+        rep = b.autotune(40)
+        b.init_equilibrium(1e-3, seed)
+        b.step(max(warmup, 3))
+        b.step(steps)
+        st = torch.cuda.ExternalStream(b.stream())
+        ms, calls, _ = repeat_timed(lambda: b.step(steps), st, min_seconds, world, dist)
+        try:
+            b.synchronize()
+        except lbm.LBMError:
+            pass  # domains whose flow went non-finite; the timing does not depend on it
+        totals = B.sharded_totals(b.conservation(), dist)
+    share = (nx[mine].astype(np.int64) * ny[mine]).sum()
+    return {"workload": "%d batched domains (widths 128-1024, heights 64-512) dealt whole to %d rank(s) by cell "
+                        "count, %s" % (count, world, "f16" if storage == lbm.F16 else "f32"),
+            "mlups": round(cells * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 5),
+            "calls": calls, "rank0_domains": int(len(mine)), "rank0_cell_share": round(float(share) / cells, 4),
+            "tuned_rank0": rep["chosen"]["schedule"],
+            "conservation_totals": [_finite_or_str(float(x), 6) for x in totals]}
+
+
 def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
     """The batched workload: `count` seeded channel domains (width 128-1024,
     height 64-512, multiples of 32; circles and rectangles at 5-15 % solid;
@@ -465,7 +502,7 @@ def run_ours(args):
     if world > 1:
         dist.barrier()
     lbm.load_library()
-    if world > 1 and not args.slab:
+    if world > 1 and not (args.slab or args.batched_split):
         # the scaling line is the replicated step and its e2e; the single-GPU
         # workloads beside it (slab, storage variants, precision, closure,
         # batched, CPU baseline) run at N = 1 only
@@ -486,6 +523,21 @@ def run_ours(args):
                 "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded circles)",
                 "config": {"workload": r["workload"], "parallelism": "y-slabs x%d" % world},
                 "gpu_launches": 3 * args.steps, "slab": r}), flush=True)
+        if world > 1:
+            dist.barrier()
+            dist.destroy_process_group()
+        return
+    if args.batched_split:
+        st = lbm.F16 if args.batched_split == "f16" else lbm.F32
+        r = time_batched_split(lbm, torch, st, args.steps, args.warmup, args.min_seconds, rank, world, dist)
+        if rank == 0:
+            print(json.dumps({
+                "metric": METRIC, "value": r["mlups"], "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": args.batched_split,
+                "data": "synthetic (seeded domains)",
+                "config": {"workload": r["workload"], "parallelism": "whole domains x%d ranks" % world},
+                "gpu_launches": args.steps, "batched_split": r}), flush=True)
         if world > 1:
             dist.barrier()
             dist.destroy_process_group()
@@ -820,6 +872,8 @@ def main():
     ap.add_argument("--no-slab", action="store_true")
     ap.add_argument("--slab", action="store_true",
                     help="time only the y-slab decomposition of the 16384x8192 grid across the ranks (strong scaling)")
+    ap.add_argument("--batched-split", choices=["f32", "f16"], default=None,
+                    help="time only the batched workload's domains dealt whole across the ranks (strong scaling)")
     ap.add_argument("--precision-steps", type=int, default=20000)
     ap.add_argument("--batched-steps", type=int, default=5000)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
