@@ -195,7 +195,8 @@ def time_batched_split(lbm, torch, storage, steps, warmup, min_seconds, rank=0, 
     one batch; strong scaling (the whole workload is fixed).  Returns the
     whole-job MLUPS over all cells and ms per step (median call of `steps`
     steps, max over ranks), each rank's share, and the FP64 conservation
-    totals gathered over the ranks (batch.sharded_totals)."""
+    totals gathered over the ranks (batch.sharded_totals) over the domains
+    whose flow stayed finite, with the count of the others."""
     import numpy as np
     from lbm_gb300 import batch as B
     nx, ny, om, u, masks = B.batched_workload(count, seed)
@@ -215,14 +216,18 @@ def time_batched_split(lbm, torch, storage, steps, warmup, min_seconds, rank=0, 
             b.synchronize()
         except lbm.LBMError:
             pass  # domains whose flow went non-finite; the timing does not depend on it
-        totals = B.sharded_totals(b.conservation(), dist)
+        c = b.conservation()
+        finite = np.isfinite(c).all(axis=1)
+        totals = B.sharded_totals(c[finite], dist)  # over the domains whose flow stayed finite
+        bad = B.sharded_totals(np.c_[(~finite).astype(np.float64), np.zeros((len(c), 2))], dist)[0]
     share = (nx[mine].astype(np.int64) * ny[mine]).sum()
     return {"workload": "%d batched domains (widths 128-1024, heights 64-512) dealt whole to %d rank(s) by cell "
                         "count, %s" % (count, world, "f16" if storage == lbm.F16 else "f32"),
             "mlups": round(cells * steps / (ms * 1e-3) / 1e6, 1), "ms_per_step": round(ms / steps, 5),
             "calls": calls, "rank0_domains": int(len(mine)), "rank0_cell_share": round(float(share) / cells, 4),
             "tuned_rank0": rep["chosen"]["schedule"],
-            "conservation_totals": [_finite_or_str(float(x), 6) for x in totals]}
+            "conservation_totals_finite_domains": [_finite_or_str(float(x), 6) for x in totals],
+            "nonfinite_domains": int(bad)}
 
 
 def time_batched(lbm, torch, storage, steps, warmup, count=512, seed=1):
