@@ -113,16 +113,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def repeat_timed(call, stream, min_seconds, world, dist, max_calls=5000):
+def repeat_timed(call, stream, min_seconds, world, dist, max_calls=5000, between=None):
     """Median device time (ms) of one `call()`: each call is bracketed by a
     barrier (N > 1) and a device synchronisation on both sides and timed with
     CUDA events on `stream`; calls repeat until `min_seconds` of wall time have
-    passed (at least 3).  The number of calls is agreed over ranks and each
+    passed (at least 3).  `between()`, if given, runs before each call,
+    outside the timing.  The number of calls is agreed over ranks and each
     call's time is the maximum over ranks.  Returns (median_ms, calls, wall_s)."""
     import torch
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def once():
+        if between is not None:
+            between()
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
@@ -151,6 +154,34 @@ def repeat_timed(call, stream, min_seconds, world, dist, max_calls=5000):
     return statistics.median(ms), calls, wall
 
 
+# Plain BGK on the 4096 x 2048 workload (tau 0.55, speeds reaching 0.3 to
+# 0.4 around the circles) goes non-finite between steps 28,000 and 34,000 in
+# every storage, f32 included.  Timed runs restart from the initial
+# equilibrium (untimed) before they would pass this many steps.
+RESTART_STEPS = 12000
+
+
+class restarter:
+    """A `between` hook for repeat_timed: before a call of k steps that would
+    take the lattice past RESTART_STEPS, re-initialise it to the workload's
+    start and take its first (in-place) step, which keeps the buffer parity
+    the captured step graphs were made for.  `launches` counts the kernels
+    it launched (none of them inside a timed call)."""
+
+    def __init__(self, lat, k):
+        self.lat, self.k, self.launches, self.restarts = lat, k, 0, 0
+
+    def __call__(self):
+        lat = self.lat
+        if lat.get_compute_num() + self.k > RESTART_STEPS:
+            l0 = lat.launch_count()
+            lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
+            lat.iterate(1)
+            lat.synchronize()
+            self.launches += lat.launch_count() - l0
+            self.restarts += 1
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -163,14 +194,16 @@ def workload_mask():
     return geometry.random_circles(NX, NY, NCIRC, 4, 32, seed=SEED, inlet_clearance=64)
 
 
-def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0, store_inlet=False):
+def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0, store_inlet=False, sr=False):
     """Device-resident MLUPS of one storage format, timed like `value` (the
     K-step call made untimed first, then repeated for `min_seconds`, median
     call); returns (ms_per_step, launches per call).  store_inlet=True keeps
     16-bit words relative to the inlet equilibrium (lbm_set_storage_reference
-    1) instead of the rest weights."""
+    1) instead of the rest weights; sr=True rounds them stochastically."""
     lat = lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, storage)
     lat.set_storage_reference(store_inlet)
+    if sr:
+        lat.set_rounding(lbm.ROUND_STOCHASTIC, SR_SEED)
     stream = torch.cuda.Stream()
     lat.set_stream(stream.cuda_stream)
     lat.set_inlet_velocity(UX)
@@ -181,9 +214,10 @@ def time_storage(lbm, torch, storage, mask, steps, warmup, min_seconds=1.0, stor
     lat.iterate(steps)
     lat.synchronize()
     l0 = lat.launch_count()
-    ms, calls, _ = repeat_timed(lambda: lat.iterate(steps), stream, min_seconds, 1, None)
+    rs = restarter(lat, steps)
+    ms, calls, _ = repeat_timed(lambda: lat.iterate(steps), stream, min_seconds, 1, None, between=rs)
     lat.synchronize()
-    launches = (lat.launch_count() - l0) // (calls + 1)
+    launches = (lat.launch_count() - l0 - rs.launches) // (calls + 1)
     lat.close()
     return ms / steps, launches
 
@@ -313,8 +347,9 @@ def time_slab(lbm, torch, steps, warmup, min_seconds, rank=0, world=1, dist=None
 def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     """Storage precision on the 4096 x 2048 workload: the same seeded run in
     f64 (the GPU's FP64 run is the reference), f32, f16 and bf16 (words
-    relative to the rest weights, f - w) and f16_inlet / bf16_inlet (relative
-    to the inlet equilibrium) for `steps` steps.  For each: the relative L2 error over fluid
+    relative to the rest weights, f - w), f16_inlet / bf16_inlet (relative
+    to the inlet equilibrium), and each 16-bit form again with stochastic
+    rounding (the _sr runs) for `steps` steps.  For each: the relative L2 error over fluid
     cells, against f64, of the velocity at step `short` (before the unsteady
     wake amplifies rounding differences into different vortex trajectories),
     of the velocity time-averaged over the second half (samples every `every`
@@ -330,7 +365,7 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
     fl[:, 0] = False  # the inlet column is set, not computed
     tmp = torch.empty((NY, NX), dtype=torch.float32, device=dev)
     runs = {}
-    for name, st, inlet in STORAGE_RUNS:
+    for name, st, inlet, sr in STORAGE_RUNS:
         stream = torch.cuda.Stream()
         acc = torch.zeros((2, NY, NX), dtype=torch.float64, device=dev)
         fin = torch.empty((2, NY, NX), dtype=torch.float64, device=dev)
@@ -338,6 +373,8 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
         n_avg = 0
         with lbm.Lattice(NX, NY, 1.0 / TAU, lbm.EDGE_CHANNEL, st) as lat:
             lat.set_storage_reference(inlet)
+            if sr:
+                lat.set_rounding(lbm.ROUND_STOCHASTIC, SR_SEED)
             lat.set_stream(stream.cuda_stream)
             lat.set_inlet_velocity(UX)
             lat.init_equilibrium(1.0, UX, 0.0, 1e-4, SEED)
@@ -390,9 +427,11 @@ def precision_check(lbm, torch, mask, steps, every=500, short=1000):
 
 
 # (name, storage, 16-bit words relative to the inlet equilibrium instead of
-# the rest weights, the default)
-STORAGE_RUNS = (("f64", 3, False), ("f32", 0, False), ("f16", 1, False), ("bf16", 2, False), ("f16_inlet", 1, True),
-                ("bf16_inlet", 2, True))
+# the rest weights (the default), stochastic rounding of the stored words)
+STORAGE_RUNS = (("f64", 3, False, False), ("f32", 0, False, False), ("f16", 1, False, False), ("bf16", 2, False, False),
+                ("f16_inlet", 1, True, False), ("bf16_inlet", 2, True, False), ("f16_sr", 1, False, True),
+                ("bf16_sr", 2, False, True), ("f16_inlet_sr", 1, True, True), ("bf16_inlet_sr", 2, True, True))
+SR_SEED = 0x5EED
 
 STEADY = {"nx": 1024, "ny": 512, "cx": 256, "cy": 256, "r": 24, "ux": 0.05, "tau": 0.8}
 
@@ -414,10 +453,12 @@ def steady_precision(lbm, steps=20000, every=1000):
     fl = mask == 0
     fl[:, 0] = False
     res = {}
-    for name, st, inlet in STORAGE_RUNS:
+    for name, st, inlet, sr in STORAGE_RUNS:
         acc, n = 0.0, 0
         with lbm.Lattice(c["nx"], c["ny"], 1.0 / c["tau"], lbm.EDGE_CHANNEL, st) as lat:
             lat.set_storage_reference(inlet)
+            if sr:
+                lat.set_rounding(lbm.ROUND_STOCHASTIC, SR_SEED)
             lat.set_inlet_velocity(c["ux"])
             lat.init_equilibrium(1.0, c["ux"], 0.0, 0.0, 0)
             lat.draw_mask(mask)
@@ -436,7 +477,7 @@ def steady_precision(lbm, steps=20000, every=1000):
 
     out = {"workload": "steady cylinder wake (Re 24): 1024x512 channel, r 24, tau 0.8, ux 0.05, %d steps" % steps,
            "reference": "f64 storage on the GPU"}
-    for name in ("f32", "f16", "bf16", "f16_inlet", "bf16_inlet"):
+    for name in [r[0] for r in STORAGE_RUNS[1:]]:
         out[name] = {"rel_err_final_velocity": _finite_or_str(rel(res[name][0], res["f64"][0]), 7),
                      "rel_err_time_avg_velocity": _finite_or_str(rel(res[name][1], res["f64"][1]), 7)}
     return out
@@ -550,7 +591,7 @@ def run_ours(args):
     if args.kernel_only:
         st = {"f32": lbm.F32, "f16": lbm.F16, "bf16": lbm.BF16, "f64": lbm.F64}[args.kernel_only]
         ms, launches = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds,
-                                    args.inlet_reference)
+                                    args.inlet_reference, args.stochastic)
         gbs = BYTES_PER_CELL[args.kernel_only] * active / (ms * 1e-3) / 1e9
         print(json.dumps({"kernel_only": args.kernel_only, "ms_per_step": round(ms, 5),
                           "mlups": round(n / (ms * 1e-3) / 1e6, 1), "achieved_gbs": round(gbs, 1),
@@ -571,10 +612,12 @@ def run_ours(args):
     lat.iterate(args.steps)
     lat.synchronize()
     l0 = lat.launch_count()
+    rs = restarter(lat, args.steps)
     with ClockSampler(local) as clocks:
-        dev_ms, calls, wall = repeat_timed(lambda: lat.iterate(args.steps), stream, args.min_seconds, world, dist)
+        dev_ms, calls, wall = repeat_timed(lambda: lat.iterate(args.steps), stream, args.min_seconds, world, dist,
+                                           between=rs)
     lat.synchronize()
-    launches = (lat.launch_count() - l0) // (calls + 1)
+    launches = (lat.launch_count() - l0 - rs.launches) // (calls + 1)
     ms_step = dev_ms / args.steps
     mlups = world * n * args.steps / (dev_ms * 1e-3) / 1e6
     # one launch per step, replayed from a graph: the per-step device time is
@@ -645,8 +688,8 @@ def run_ours(args):
     # --- storage variants (same workload) -----------------------------------------
     variants = {}
     if not args.no_variants:
-        for name, st, inlet in STORAGE_RUNS[2:]:
-            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds, inlet)
+        for name, st, inlet, sr in STORAGE_RUNS[2:]:
+            vms, _ = time_storage(lbm, torch, st, mask, args.steps, args.warmup, args.min_seconds, inlet, sr)
             gbs = BYTES_PER_CELL[name.split("_")[0]] * active / (vms * 1e-3) / 1e9
             variants[name] = {"mlups": round(n / (vms * 1e-3) / 1e6, 1), "ms_per_step": round(vms, 4),
                               "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4)}
@@ -701,6 +744,7 @@ def run_ours(args):
         "slab": slab,
         "gpu_launches": int(launches),
         "timing": {"calls": calls, "per_call": "median", "min_seconds": args.min_seconds,
+                   "restarts": rs.restarts, "restart_steps": RESTART_STEPS,
                    "graph": "the K-step call replays a captured graph, instantiated before timing"},
         "clocks": clocks.summary(),
         "wall_s_timed": round(wall, 4),
@@ -886,6 +930,8 @@ def main():
                     help="repeat the timed K-step call until this much wall time has passed (median reported)")
     ap.add_argument("--inlet-reference", action="store_true",
                     help="with --kernel-only f16 / bf16: words relative to the inlet equilibrium")
+    ap.add_argument("--stochastic", action="store_true",
+                    help="with --kernel-only f16 / bf16: stochastic rounding of the stored words")
     ap.add_argument("--kernel-only", choices=["f32", "f16", "bf16", "f64"], default=None,
                     help="time only the step kernel of one storage format (profiling runs)")
     ap.add_argument("--case", choices=["batched64", "batched64_f16", "closure2048"], default=None,

@@ -155,6 +155,30 @@ int lbm_set_inlet_velocity(lbm_sim* sim, float ux, int reset_field);
 int lbm_set_storage_reference(lbm_sim* sim, int inlet);
 int lbm_get_storage_reference(const lbm_sim* sim, int* inlet);
 
+/* Rounding of the words each step stores (16-bit storage only; no reference
+ * counterpart).  LBM_ROUND_NEAREST (the default) rounds to nearest even.
+ * LBM_ROUND_STOCHASTIC rounds each word up or down with probabilities set by
+ * its distance to the two neighbouring 16-bit values (the hardware's
+ * cvt.rs conversions), so rounding adds no bias. Round-to-nearest gives a
+ * steady flow the same error every step, and that error accumulates. The
+ * random bits are a hash of (seed, step index, row + row origin, column
+ * pair, direction): runs are deterministic, and graph replays, row-range
+ * steps, checkpoints and kernel variants give identical states.
+ * Initialisation, uploads and re-expression still round to nearest.
+ * LBM_ERR_ARG for stochastic rounding with f32 / f64 storage.  The setting
+ * travels with checkpoints. */
+#define LBM_ROUND_NEAREST 0
+#define LBM_ROUND_STOCHASTIC 1
+int lbm_set_rounding(lbm_sim* sim, int mode, uint32_t seed);
+int lbm_get_rounding(const lbm_sim* sim, int* mode, uint32_t* seed);
+
+/* Row origin of the stochastic-rounding hash: row y hashes as y + origin
+ * (default 0).  A lattice that holds rows [y0, y1) of a larger one (a slab)
+ * sets the origin so its rounding matches the undivided lattice.  Travels
+ * with checkpoints. */
+int lbm_set_row_origin(lbm_sim* sim, int32_t origin);
+int lbm_get_row_origin(const lbm_sim* sim, int32_t* origin);
+
 /* reset_to_equilibrium (lbm.rs:1076-1088): set_equil(0.1, 0, 1) everywhere. */
 int lbm_reset_to_equilibrium(lbm_sim* sim);
 

@@ -15,7 +15,8 @@
  *   f32 omega, u_in, drift; u64 steps; u32 cur, materialised, closure,
  *   elem_bytes; u64 payload_bytes; u32 crc32 (zlib's CRC-32 of the header
  *   with this field zero, continued over the payload); u32 store_inlet
- *   (lbm_set_storage_reference); u32 reserved[4]
+ *   (lbm_set_storage_reference); u32 rounding, rounding_seed
+ *   (lbm_set_rounding); i32 row_origin (lbm_set_row_origin); u32 reserved
  * then the payload, every plane dense row-major (nx * ny, row 0 first):
  *   mask (u8 per cell); buffer 0 (8 planes, direction slots 0..3 = nw, n, ne,
  *   w and 4..7 = e, sw, s, se); buffer 1 (8 planes); rest plane; closure
@@ -37,8 +38,8 @@ int lbm_checkpoint_size(const lbm_sim* sim, size_t* bytes);
 int lbm_checkpoint_save(lbm_sim* sim, void* buf, size_t len);
 /* From a buffer; LBM_ERR_ARG, before any device work, on a size / mode
  * mismatch, a CRC error, or a header field out of range (cur, materialised
- * closure and store_inlet must be 0 or 1; omega in (0, 2); u_in finite; drift finite and
- * > 0). */
+ * closure and store_inlet must be 0 or 1; rounding 0, or 1 with 16-bit
+ * storage; omega in (0, 2); u_in finite; drift finite and > 0). */
 int lbm_checkpoint_load(lbm_sim* sim, const void* buf, size_t len);
 
 /* Host only (no device work, no lattice): check a checkpoint buffer as
@@ -52,6 +53,9 @@ typedef struct lbm_checkpoint_info {
   float omega, u_in, drift;
   uint64_t steps;
   int closure, store_inlet;
+  int rounding;            /* LBM_ROUND_NEAREST / LBM_ROUND_STOCHASTIC */
+  uint32_t rounding_seed;
+  int32_t row_origin;
 } lbm_checkpoint_info;
 int lbm_checkpoint_inspect(const void* buf, size_t len, lbm_checkpoint_info* info);
 /* The same through a file. */

@@ -25,6 +25,7 @@ import os
 import numpy as np
 
 __all__ = ["Lattice", "LBMError", "load_library", "EDGE_REF", "EDGE_CHANNEL", "F32", "F16", "BF16", "F64",
+           "ROUND_NEAREST", "ROUND_STOCHASTIC",
            "SummaryStat", "ColorMap", "FIELD"]
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -32,6 +33,7 @@ LIB_PATH = os.path.join(HERE, "liblbm_gb300.so")
 
 EDGE_REF, EDGE_CHANNEL = 0, 1
 F32, F16, BF16, F64 = 0, 1, 2, 3
+ROUND_NEAREST, ROUND_STOCHASTIC = 0, 1
 FIELD = {"rho": 0, "jx": 1, "jy": 2, "ux": 3, "uy": 4, "curl": 5, "vorticity": 6, "speed": 7}
 
 
@@ -75,6 +77,10 @@ _SIGS = [
     ("lbm_set_storage_reference", ctypes.c_int, [_P, ctypes.c_int]),
     ("lbm_init_equilibrium_noise", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P]),
     ("lbm_get_storage_reference", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int)]),
+    ("lbm_set_rounding", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32]),
+    ("lbm_get_rounding", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32)]),
+    ("lbm_set_row_origin", ctypes.c_int, [_P, ctypes.c_int32]),
+    ("lbm_get_row_origin", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int32)]),
     ("lbm_reset_to_equilibrium", ctypes.c_int, [_P]),
     ("lbm_init_equilibrium", ctypes.c_int, [_P, ctypes.c_float, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                                             ctypes.c_uint64]),
@@ -153,7 +159,8 @@ class CheckpointInfo(ctypes.Structure):
     """lbm_checkpoint_info (include/lbm_checkpoint.h)."""
     _fields_ = [("nx", ctypes.c_uint32), ("ny", ctypes.c_uint32), ("edge", ctypes.c_int), ("storage", ctypes.c_int),
                 ("omega", ctypes.c_float), ("u_in", ctypes.c_float), ("drift", ctypes.c_float),
-                ("steps", ctypes.c_uint64), ("closure", ctypes.c_int), ("store_inlet", ctypes.c_int)]
+                ("steps", ctypes.c_uint64), ("closure", ctypes.c_int), ("store_inlet", ctypes.c_int),
+                ("rounding", ctypes.c_int), ("rounding_seed", ctypes.c_uint32), ("row_origin", ctypes.c_int32)]
 
 
 def checkpoint_info(buf):
@@ -283,6 +290,33 @@ class Lattice:
         v = ctypes.c_int()
         _check(_lib.lbm_get_storage_reference(self._h, ctypes.byref(v)))
         return bool(v.value)
+
+    def set_rounding(self, mode, seed=0):
+        """Rounding of the words each step stores: ROUND_NEAREST (the
+        default) or ROUND_STOCHASTIC (16-bit storage only: each word rounds
+        up or down with probabilities set by its distance to the two
+        neighbouring 16-bit values, from a seeded hash of step, cell and
+        direction; rounding then adds no bias that a steady flow would
+        accumulate)."""
+        _check(_lib.lbm_set_rounding(self._h, int(mode), int(seed) & 0xFFFFFFFF))
+
+    @property
+    def rounding(self):
+        """(mode, seed)."""
+        m, sd = ctypes.c_int(), ctypes.c_uint32()
+        _check(_lib.lbm_get_rounding(self._h, ctypes.byref(m), ctypes.byref(sd)))
+        return m.value, sd.value
+
+    def set_row_origin(self, y0):
+        """Row y of this lattice hashes as y + y0 in the stochastic rounding
+        (a slab of a larger lattice sets its first row's index)."""
+        _check(_lib.lbm_set_row_origin(self._h, int(y0)))
+
+    @property
+    def row_origin(self):
+        v = ctypes.c_int32()
+        _check(_lib.lbm_get_row_origin(self._h, ctypes.byref(v)))
+        return v.value
 
     def reset_to_equilibrium(self):
         _check(_lib.lbm_reset_to_equilibrium(self._h))

@@ -95,6 +95,10 @@ __device__ void fill_args(StepArgs<S, C>& sa, const DomainDev& d, int src_i, int
   sa.closure = nullptr;
   sa.fallback = nullptr;
   sa.tau0 = sa.drift = 0.0f;
+  sa.sr.on = 0u;  // batched domains round to nearest
+  sa.sr.seed = sa.sr.t = 0u;
+  sa.sr.clock = nullptr;
+  sa.sr.y0 = 0;
 }
 
 // Schedules: 0 static (tiles longest first, dealt round robin), 1 atomic

@@ -75,11 +75,14 @@ struct StepGraphKey {
   int kernel = -1, rows = 0, bands = 0, staged_rows = 0;
   const void* closure = nullptr;
   cudaStream_t stream = nullptr;
+  uint32_t sr_on = 0, sr_seed = 0;
+  int sr_y0 = 0;
   bool operator==(const StepGraphKey& o) const {
     return omega == o.omega && drift == o.drift && u_in == o.u_in && store_inlet == o.store_inlet &&
            kernel == o.kernel && rows == o.rows &&
            bands == o.bands &&
-           staged_rows == o.staged_rows && closure == o.closure && stream == o.stream;
+           staged_rows == o.staged_rows && closure == o.closure && stream == o.stream && sr_on == o.sr_on &&
+           sr_seed == o.sr_seed && sr_y0 == o.sr_y0;
   }
 };
 
@@ -88,6 +91,13 @@ struct lbm_sim {
   int edge = 0, storage = 0;
   float omega = 1.0f, u_in = 0.1f;
   bool store_inlet = false;  // 16-bit words relative to the inlet equilibrium (else to the rest weights)
+  // rounding of the words each step stores (lbm_set_rounding): stochastic
+  // with this seed, rows hashed from origin sr_y0 (lbm_set_row_origin)
+  uint32_t sr_on = 0, sr_seed = 0;
+  int sr_y0 = 0;
+  uint32_t* clock_d = nullptr;   // step index of a captured run's first step (set before each replay)
+  bool capturing = false;        // launches are being captured: they read the step index from clock_d
+  uint64_t capture_steps0 = 0;   // the step index the capture started at
   Layout L{};
   size_t es = 4;   // bytes per stored population
   size_t cs = 4;   // bytes of the arithmetic type (moments)
@@ -323,7 +333,7 @@ void release(lbm_sim* s) {
   for (auto& g : s->run_graph)
     if (g) cudaGraphExecDestroy(g);
   cudaFree(s->f_base[0]); cudaFree(s->f_base[1]); cudaFree(s->rest_base); cudaFree(s->mask_base); cudaFree(s->mom);
-  cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d);
+  cudaFree(s->flag_d); cudaFree(s->partial_d); cudaFree(s->staging_d); cudaFree(s->clock_d);
   cudaFree(s->closure_base); cudaFree(s->cnn_w); cudaFree(s->cnn_wpack); cudaFree(s->fallback_d);
   if (s->copied) cudaEventDestroy(s->copied);
   if (s->switched) cudaEventDestroy(s->switched);
@@ -341,6 +351,9 @@ int band_rows(const lbm_sim* s, int occ, int W, int span) {
   return std::max((span + bands - 1) / bands, std::min(s->rows > 0 ? s->rows : 2, span));
 }
 
+// The cached launch shape's key: kernel variant, closure, stochastic rounding.
+int staged_key(int kernel, bool closure, bool sr) { return 4 * kernel + (closure ? 1 : 0) + (sr ? 2 : 0); }
+
 // Staged step launch over rows [a.row0, a.row_end): one strip of W columns
 // per grid column, row bands sized so that all CTAs are resident at once
 // (one wave, equal work).  The whole lattice's shape is cached.
@@ -349,7 +362,10 @@ int launch_staged(lbm_sim* s, StepArgs<typename St::S, typename St::C> a) {
   constexpr int TPB = stage_threads<CPT, W>();
   const size_t smem = (size_t)NS * stage_bytes<typename St::S, W, CL>();
   auto kern = k_step_ws<St, EDGE, NS, CPT, CL, W>;
-  const int variant = 2 * s->kernel + (CL ? 1 : 0);
+  if constexpr (St::kDev) {
+    if (a.sr.on) kern = k_step_ws<St, EDGE, NS, CPT, CL, W, true>;
+  }
+  const int variant = staged_key(s->kernel, CL, a.sr.on != 0u);
   if (s->staged_variant != variant) {
     CK(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0;
@@ -713,6 +729,38 @@ int lbm_get_storage_reference(const lbm_sim* s, int* inlet) {
   return LBM_OK;
 }
 
+int lbm_set_rounding(lbm_sim* s, int mode, uint32_t seed) {
+  CHECK_SIM(s);
+  if (mode != LBM_ROUND_NEAREST && mode != LBM_ROUND_STOCHASTIC)
+    return fail(LBM_ERR_ARG, "rounding mode %d: 0 nearest, 1 stochastic", mode);
+  if (mode == LBM_ROUND_STOCHASTIC && s->storage != STORE_F16 && s->storage != STORE_BF16)
+    return fail(LBM_ERR_ARG, "stochastic rounding applies to 16-bit storage");
+  if (mode == LBM_ROUND_STOCHASTIC && !s->clock_d && cudaMalloc(&s->clock_d, sizeof(uint32_t)) != cudaSuccess)
+    return fail(LBM_ERR_NOMEM, "step clock word");
+  s->sr_on = mode == LBM_ROUND_STOCHASTIC ? 1u : 0u;
+  s->sr_seed = s->sr_on ? seed : 0u;
+  return LBM_OK;
+}
+
+int lbm_get_rounding(const lbm_sim* s, int* mode, uint32_t* seed) {
+  if (!s || !mode || !seed) return fail(LBM_ERR_ARG, "null argument");
+  *mode = s->sr_on ? LBM_ROUND_STOCHASTIC : LBM_ROUND_NEAREST;
+  *seed = s->sr_seed;
+  return LBM_OK;
+}
+
+int lbm_set_row_origin(lbm_sim* s, int32_t origin) {
+  CHECK_SIM(s);
+  s->sr_y0 = origin;
+  return LBM_OK;
+}
+
+int lbm_get_row_origin(const lbm_sim* s, int32_t* origin) {
+  if (!s || !origin) return fail(LBM_ERR_ARG, "null argument");
+  *origin = s->sr_y0;
+  return LBM_OK;
+}
+
 int lbm_reset_to_equilibrium(lbm_sim* s) {
   CHECK_SIM(s);
   return launch_init(s, 1.0, 0.1, 0.0, 0.0, 0, -1, -1);
@@ -798,6 +846,11 @@ static int launch_rows(lbm_sim* s, bool last, int row0, int row_end, int dst) {
     a.drift = s->drift;
     a.fallback = s->closure_on ? s->fallback_d : nullptr;
     a.ref = store_ref(s);
+    a.sr.on = s->sr_on;
+    a.sr.seed = s->sr_seed;
+    a.sr.y0 = s->sr_y0;
+    a.sr.clock = s->capturing && s->sr_on ? s->clock_d : nullptr;
+    a.sr.t = a.sr.clock ? (uint32_t)(s->steps - s->capture_steps0) : (uint32_t)s->steps;
     if (variant >= 2) {
       return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
     } else if (variant == 1) {
@@ -840,7 +893,20 @@ static StepGraphKey graph_key(const lbm_sim* s) {
   k.stream = s->stream;
   k.bands = s->staged_bands;
   k.staged_rows = s->staged_rows;
+  k.sr_on = s->sr_on;
+  k.sr_seed = s->sr_seed;
+  k.sr_y0 = s->sr_y0;
   return k;
+}
+
+// Before a captured run replays: its launches read their step index as the
+// run's first step (this word) plus their offset in the run.
+static int set_clock(lbm_sim* s) {
+  if (!s->sr_on) return LBM_OK;
+  k_set_clock<<<1, 1, 0, s->stream>>>(s->clock_d, (uint32_t)s->steps);
+  CK_LAUNCH();
+  s->launches++;
+  return LBM_OK;
 }
 
 static void drop_step_graphs(lbm_sim* s) {
@@ -864,7 +930,10 @@ static int capture_steps(lbm_sim* s, cudaGraphExec_t& out, uint32_t n, bool mome
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
   int rc = LBM_OK;
+  s->capturing = true;
+  s->capture_steps0 = steps0;
   for (uint32_t k = 0; k < n && !rc; k++) rc = launch_step(s, moments && k + 1 == n);
+  s->capturing = false;
   const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->cur = cur0;  // the capture recorded the launches without running them
   s->steps = steps0;
@@ -890,7 +959,7 @@ int lbm_step(lbm_sim* s, uint32_t n) {
   auto steady = [&]() {
     return s->use_graphs && s->stream != nullptr && capturing == cudaStreamCaptureStatusNone && !s->materialised &&
            (s->storage == STORE_F64 || s->kernel < 2 ||
-            s->staged_variant == 2 * s->kernel + (s->closure_on ? 1 : 0));
+            s->staged_variant == staged_key(s->kernel, s->closure_on, s->sr_on != 0u));
   };
   if (n >= 2 && n <= (uint32_t)kRunGraphMax && steady()) {
     const int c = s->cur;
@@ -900,6 +969,8 @@ int lbm_step(lbm_sim* s, uint32_t n) {
       s->run_key[c] = graph_key(s);
       s->run_n[c] = n;
     }
+    int rc = set_clock(s);
+    if (rc) return rc;
     CK(cudaGraphLaunch(s->run_graph[c], s->stream));
     s->steps += n;
     s->launches += n;
@@ -915,6 +986,8 @@ int lbm_step(lbm_sim* s, uint32_t n) {
         if (rc) return rc;
         s->graph_key[s->cur] = graph_key(s);
       }
+      int rc = set_clock(s);
+      if (rc) return rc;
       CK(cudaGraphLaunch(s->graph[s->cur], s->stream));
       s->steps += kStepGraph;  // even: the buffer parity is unchanged
       s->launches += kStepGraph;
@@ -1372,7 +1445,10 @@ struct CkHeader {  // 96 bytes, little-endian, written as is
   uint64_t payload_bytes;
   uint32_t crc32;  // over the header (with this field zero), then the payload
   uint32_t store_inlet;  // 16-bit words relative to the inlet equilibrium (1) or the rest weights (0)
-  uint32_t reserved[4];
+  uint32_t rounding;     // LBM_ROUND_NEAREST or LBM_ROUND_STOCHASTIC (16-bit storage)
+  uint32_t rounding_seed;
+  int32_t row_origin;
+  uint32_t reserved;
 };
 static_assert(sizeof(CkHeader) == 96, "checkpoint header layout");
 
@@ -1452,6 +1528,9 @@ int lbm_checkpoint_save(lbm_sim* s, void* buf, size_t len) {
   h.closure = closure ? 1u : 0u;
   h.elem_bytes = (uint32_t)e;
   h.store_inlet = s->store_inlet ? 1u : 0u;
+  h.rounding = s->sr_on;
+  h.rounding_seed = s->sr_seed;
+  h.row_origin = s->sr_y0;
   h.payload_bytes = need - sizeof(CkHeader);
   uint8_t* p = (uint8_t*)buf + sizeof(CkHeader);
   std::memcpy(p, s->mask_h.data(), cells);
@@ -1482,6 +1561,9 @@ int ck_check(const void* buf, size_t len, CkHeader& h) {
   if (!(h.omega > 0.0f && h.omega < 2.0f) || !std::isfinite(h.u_in) || !(h.drift > 0.0f) || !std::isfinite(h.drift))
     return fail(LBM_ERR_ARG, "checkpoint header: omega %g, inlet %g, drift %g out of range", (double)h.omega,
                 (double)h.u_in, (double)h.drift);
+  if (h.rounding > 1u || (h.rounding == 1u && h.storage != STORE_F16 && h.storage != STORE_BF16))
+    return fail(LBM_ERR_ARG, "checkpoint header: rounding %u with storage %d (stochastic rounding is 16-bit only)",
+                h.rounding, h.storage);
   const int es = h.storage == STORE_F32 ? 4 : h.storage == STORE_F64 ? 8 : 2;
   if (h.nx < 3 || h.ny < 3 || (h.edge != EDGE_REF && h.edge != EDGE_CHANNEL) || h.storage < STORE_F32 ||
       h.storage > STORE_F64 || h.elem_bytes != (uint32_t)es)
@@ -1511,6 +1593,9 @@ int lbm_checkpoint_inspect(const void* buf, size_t len, lbm_checkpoint_info* inf
     info->steps = h.steps;
     info->closure = (int)h.closure;
     info->store_inlet = (int)h.store_inlet;
+    info->rounding = (int)h.rounding;
+    info->rounding_seed = h.rounding_seed;
+    info->row_origin = h.row_origin;
   }
   return LBM_OK;
 }
@@ -1531,6 +1616,8 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
     int rc = lbm_closure_enable(s, h.drift);
     if (rc) return rc;
   }
+  if (h.rounding && !s->clock_d && cudaMalloc(&s->clock_d, sizeof(uint32_t)) != cudaSuccess)
+    return fail(LBM_ERR_NOMEM, "step clock word");
   const size_t cells = (size_t)s->L.nx * s->L.ny, e = s->es;
   for (size_t i = 0; i < cells; i++) s->mask_h[i] = p[i] ? 1 : 0;
   s->mask_h_valid = true;
@@ -1546,6 +1633,9 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
   s->omega = h.omega;
   s->u_in = h.u_in;
   s->store_inlet = h.store_inlet != 0;
+  s->sr_on = h.rounding;
+  s->sr_seed = h.rounding_seed;
+  s->sr_y0 = h.row_origin;
   s->drift = h.drift;
   s->closure_on = closure;
   s->steps = h.steps;

@@ -49,6 +49,61 @@ struct StoreRef {
   float ux, uy;
   int shift;  // u_ref != 0
 };
+// Stochastic rounding of the words a step stores (16-bit storage,
+// lbm_set_rounding).  Each word is rounded to one of its two neighbouring
+// 16-bit values, the farther one with probability equal to its share of the
+// gap, so the rounding adds no bias: a steady flow no longer receives the
+// same rounding error every step.  The random bits of direction q of cell
+// (x, y) at step t are a hash of (seed, t, y + row origin, x / 2, q):
+//   s_t = fmix32(seed ^ t * 0x9E3779B1)              once per step
+//   k_y = fmix32(s_t + y_g * 0x85EBCA77)             once per row
+//   k_p = fmix32(k_y ^ (x >> 1) * 0xC2B2AE3D)        once per column pair
+//   R_q = k_p * sr_mul(q) mod 2^32                   one multiply per direction
+// fmix32 is the 32-bit finaliser of MurmurHash3.  sr_mul(q) is odd, so R_q
+// is a bijection of k_p and each of its bit fields is as uniform as k_p's
+// (the high word of the product would not be: it stays below sr_mul(q)).  The pair's even cell uses
+// bits [12:0] (binary16) or [15:0] (bfloat16) of R_q, the odd cell bits
+// [28:16] or [31:16]: the fields the pair conversions cvt.rs.f16x2.f32 and
+// cvt.rs.bf16x2.f32 read, so one R_q serves two cells stored as one word or
+// either cell stored alone, and every kernel variant rounds alike.
+struct SrArgs {
+  uint32_t on;            // 1: stochastic rounding (16-bit storage only)
+  uint32_t seed;
+  uint32_t t;             // the step index, or its offset from *clock
+  const uint32_t* clock;  // step index of a captured run's first step, or null
+  int y0;                 // row origin: row y hashes as y + y0
+};
+__host__ __device__ constexpr uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85EBCA6Bu;
+  h ^= h >> 13;
+  h *= 0xC2B2AE35u;
+  h ^= h >> 16;
+  return h;
+}
+// Odd multiplier of direction q: the high word of SplitMix64's output for
+// the state (q + 1) * 0x9E3779B97F4A7C15, low bit set.
+__host__ __device__ constexpr uint32_t sr_mul(int q) {
+  uint64_t z = (uint64_t)(q + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (uint32_t)(z >> 32) | 1u;
+}
+__device__ __forceinline__ uint32_t sr_step_key(const SrArgs& s) {
+  // the clock word changes between replays of the same graph: read it at L2
+  // (ld.global.cg), never from a line an earlier replay left in L1
+  const uint32_t t = s.clock ? __ldcg(s.clock) + s.t : s.t;
+  return fmix32(s.seed ^ (t * 0x9E3779B1u));
+}
+__device__ __forceinline__ uint32_t sr_row_key(uint32_t step_key, int y, const SrArgs& s) {
+  return fmix32(step_key + (uint32_t)(y + s.y0) * 0x85EBCA77u);
+}
+__device__ __forceinline__ uint32_t sr_pair_key(uint32_t row_key, int x) {
+  return fmix32(row_key ^ ((uint32_t)(x >> 1) * 0xC2B2AE3Du));
+}
+__device__ __forceinline__ uint32_t sr_bits(uint32_t pair_key, int q) { return pair_key * sr_mul(q); }
+
 // Shift modes of the policies' arithmetic: 0 and 1 fix StoreRef::shift at
 // compile time (the staged kernels instantiate both and branch once per
 // CTA), 2 reads it at run time.
@@ -198,6 +253,7 @@ struct StF32 {
   __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
+  __device__ static S store_sr(C v, uint32_t, int) { return v; }
   __device__ static C f_of(S s, int, const StoreRef&) { return s; }
   __device__ static S of_f(C f, int, const StoreRef&) { return f; }
   template <int M = 2> __device__ static C bounce(S s, int, const StoreRef&) { return s; }
@@ -213,6 +269,7 @@ struct StF64 {
   __device__ static Om omega_consts(C w) { return w; }
   __device__ static C load(S s, int) { return s; }
   __device__ static S store(C v, int) { return v; }
+  __device__ static S store_sr(C v, uint32_t, int) { return v; }
   __device__ static C f_of(S s, int, const StoreRef&) { return s; }
   __device__ static S of_f(C f, int, const StoreRef&) { return f; }
   template <int M = 2> __device__ static C bounce(S s, int, const StoreRef&) { return s; }
@@ -230,6 +287,15 @@ template <class Word> struct StDev {
   __device__ static Om omega_consts(C w) { return DevOmega(w); }
   __device__ static C load(S s, int) { return Word::to_f(s); }
   __device__ static S store(C v, int) { return Word::of(v); }
+  // stochastic rounding with the random bits R of the cell's column pair;
+  // x is the cell's column (its parity picks the half of R)
+  __device__ static S store_sr(C v, uint32_t R, int x) {
+    const bool odd = (x & 1) != 0;
+    const uint32_t w = Word::of2_sr(odd ? 0.0f : v, odd ? v : 0.0f, R);
+    return Word::of_bits((uint16_t)(odd ? w >> 16 : w & 0xffffu));
+  }
+  // the even and odd cells of a column pair as one word (the even cell low)
+  __device__ static uint32_t store2_sr(C even, C odd, uint32_t R) { return Word::of2_sr(even, odd, R); }
   __device__ static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + Word::to_f(s); }
   __device__ static S of_f(C f, int q, const StoreRef& R) { return Word::of((f - weight<float>(q)) - R.d[q]); }
   // the own population 8 - q bounced back into direction q: with a shift,
@@ -273,11 +339,26 @@ struct WordF16 {
   using S = __half;
   __device__ static float to_f(S s) { return __half2float(s); }
   __device__ static S of(float v) { return __float2half_rn(v); }
+  __device__ static S of_bits(uint16_t b) { return __ushort_as_half(b); }
+  // stochastic rounding of a pair: the odd cell to the high half with bits
+  // [28:16] of R, the even cell to the low half with bits [12:0]
+  __device__ static uint32_t of2_sr(float even, float odd, uint32_t R) {
+    uint32_t d;
+    asm("cvt.rs.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(odd), "f"(even), "r"(R));
+    return d;
+  }
 };
 struct WordBF16 {
   using S = __nv_bfloat16;
   __device__ static float to_f(S s) { return __bfloat162float(s); }
   __device__ static S of(float v) { return __float2bfloat16_rn(v); }
+  __device__ static S of_bits(uint16_t b) { return __ushort_as_bfloat16(b); }
+  // the same for bfloat16: bits [31:16] and [15:0] of R
+  __device__ static uint32_t of2_sr(float even, float odd, uint32_t R) {
+    uint32_t d;
+    asm("cvt.rs.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(odd), "f"(even), "r"(R));
+    return d;
+  }
 };
 using StF16 = StDev<WordF16>;    // binary16 words
 using StBF16 = StDev<WordBF16>;  // bfloat16 words

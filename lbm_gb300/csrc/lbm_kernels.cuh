@@ -41,7 +41,30 @@ template <class S, class C> struct StepArgs {
   float tau0, drift;
   unsigned long long* __restrict__ fallback;  // cells that fell back to plain BGK, or null
   StoreRef ref;  // reference state of 16-bit storage (inlet velocity, lattice omega)
+  SrArgs sr;     // rounding of the stored words (stochastic: 16-bit storage only)
 };
+
+// One cell's collided words, stored with the lattice's rounding.
+template <class St>
+__device__ __forceinline__ void store_cell(const StepArgs<typename St::S, typename St::C>& a, long long own, int x,
+                                           int y, const typename St::C f[9]) {
+  if (St::kDev && a.sr.on) {
+    const uint32_t kp = sr_pair_key(sr_row_key(sr_step_key(a.sr), y, a.sr), x);
+#pragma unroll
+    for (int q = 0; q < 9; q++) {
+      if (q == 4) continue;
+      a.dst[(long long)slot(q) * a.L.ps + own] = St::store_sr(f[q], sr_bits(kp, q), x);
+    }
+    a.rest[own] = St::store_sr(f[4], sr_bits(kp, 4), x);
+    return;
+  }
+#pragma unroll
+  for (int q = 0; q < 9; q++) {
+    if (q == 4) continue;
+    a.dst[(long long)slot(q) * a.L.ps + own] = St::store(f[q], q);
+  }
+  a.rest[own] = St::store(f[4], 4);
+}
 
 // Relaxation rate of a cell under the closure record `rec`: 1 / (tau0 +
 // delta_tau) while the cell's speed stays within the drift bound of the
@@ -189,12 +212,7 @@ __device__ __forceinline__ void step_cell(const StepArgs<typename St::S, typenam
   }
   if (frozen) return;  // channel inlet: fixed equilibrium, never collided
   St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy), a.ref);
-#pragma unroll
-  for (int q = 0; q < 9; q++) {
-    if (q == 4) continue;
-    a.dst[(long long)slot(q) * L.ps + own] = St::store(f[q], q);
-  }
-  a.rest[own] = St::store(f[4], 4);
+  store_cell<St>(a, own, x, y, f);
 }
 
 // Fused collide + stream.  Block = 128 threads along x (4 warps, each aligned
@@ -368,12 +386,7 @@ __global__ void __launch_bounds__(128, MINB) k_step_pf(StepArgs<typename St::S, 
     }
     if (!frozen) {
       St::collide(f, rho, aux, jx, jy, cell_omega(a, own, rho, jx, jy), a.ref);
-#pragma unroll
-      for (int q = 0; q < 9; q++) {
-        if (q == 4) continue;
-        a.dst[(long long)slot(q) * L.ps + own] = St::store(f[q], q);
-      }
-      a.rest[own] = St::store(f[4], 4);
+      store_cell<St>(a, own, x, y, f);
     }
     if (more) {
 #pragma unroll
@@ -487,6 +500,9 @@ __global__ void k_read_pops(Layout L, const typename St::S* f, const typename St
 
 // Bit-packs a dense nx-wide byte mask (nonzero = solid) into the pitched mask
 // words: one thread per word, bits past column nx-1 cleared.
+// The step index a captured run of steps starts at (stochastic rounding).
+static __global__ void k_set_clock(uint32_t* clock, uint32_t t) { *clock = t; }
+
 static __global__ void k_pack_mask(Layout L, const uint8_t* __restrict__ bytes, uint32_t* __restrict__ words) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;

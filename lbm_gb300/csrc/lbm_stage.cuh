@@ -185,7 +185,7 @@ template <int CPT, int W = kStageW> constexpr int stage_threads() { return W / C
 // barriers (first tile only), and `drain` makes the producer wait for its last
 // copies before returning (last tile only; otherwise the consumers release
 // the tile's last two staged rows, which the next tile does not read).
-template <class St, int EDGE, int NS, int CPT, bool CL, int W, int KM, class A>
+template <class St, int EDGE, int NS, int CPT, bool CL, int W, int KM, bool SR = false, class A>
 __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsigned char* smem, uint64_t* full,
                                         uint64_t* empty, bool down = false, uint32_t g0 = 0, bool init = true,
                                         bool drain = true) {
@@ -313,6 +313,11 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
   uint32_t own = (uint32_t)y_start * (uint32_t)L.pitch + (uint32_t)x0;
   const uint32_t own_step = down ? 0u - (uint32_t)L.pitch : (uint32_t)L.pitch;
   const typename St::Om om = St::omega_consts(a.omega);
+  // stochastic rounding of the stored words (16-bit storage, a kernel of its
+  // own): the step's key; each row forms the keys of this thread's column pairs
+  constexpr bool sr = SR && St::kDev;
+  const uint32_t sr_key = sr ? sr_step_key(a.sr) : 0u;
+  constexpr int kPairs = (CPT + 1) / 2;
   for (int y = y_start, it = y0; it < y1 && ok; it++, y += y_step, own += own_step) {
     if (!mbar_wait(smem_addr(&full[slot_p]), parity_p)) { ok = false; break; }
     // rows y-1 (sm) and y+1 (sp) by the walking direction
@@ -339,6 +344,12 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       const bool own_solid = (w0 >> (j + 1)) & 1u;
       act[j] = in_row[j] && xin[j] && yin && !(EDGE == EDGE_CHANNEL && own_solid);
       any_act |= act[j];
+    }
+    uint32_t kp[kPairs];
+    if constexpr (sr) {
+      const uint32_t kr = sr_row_key(sr_key, y, a.sr);
+#pragma unroll
+      for (int i = 0; i < kPairs; i++) kp[i] = sr_pair_key(kr, x0 + 2 * i);
     }
     // pulled populations of this thread's cells; every lane loads (stage
     // indices stay inside the stage), lanes without an active cell discard them
@@ -417,8 +428,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       St::collide(f, rho, aux, jx, jy, a.omega, a.ref);
 #pragma unroll
       for (int q = 0; q < 9; q++)
-        if (q != 4) a.dstp[slot(q)][own] = St::store(f[q], q);
-      a.rest[own] = St::store(f[4], 4);
+        if (q != 4) a.dstp[slot(q)][own] = sr ? St::store_sr(f[q], sr_bits(kp[0], q), x0) : St::store(f[q], q);
+      a.rest[own] = sr ? St::store_sr(f[4], sr_bits(kp[0], 4), x0) : St::store(f[4], 4);
     } else if (any_act) {
       if (near_solid) {  // half-way bounce-back: upstream solid -> own opposite population
 #pragma unroll
@@ -496,18 +507,45 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
       bool all_act = true;
 #pragma unroll
       for (int j = 0; j < CPT; j++) all_act &= act[j];
+      // one cell's word of direction q, by the lattice's rounding
+      auto word = [&](int q, int j) -> S {
+        return sr ? St::store_sr(f[q][j], sr_bits(kp[j >> 1], q), x0 + j) : St::store(f[q][j], q);
+      };
       if (CPT == 2 && all_act) {  // both cells: one 2-element store per plane
+        if constexpr (sr && CPT == 2) {
+          {
 #pragma unroll
-        for (int q = 0; q < 9; q++) {
-          S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
-          store_pair(p, f[q][0], f[q][CPT - 1]);
+            for (int q = 0; q < 9; q++) {
+              S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
+              *reinterpret_cast<uint32_t*>(p) = St::store2_sr(f[q][0], f[q][1], sr_bits(kp[0], q));
+            }
+          }
         }
-      } else if constexpr (CPT == 4) {
-        if (all_act) {  // four cells: one 8-byte store per plane
+        if (!sr) {
 #pragma unroll
           for (int q = 0; q < 9; q++) {
             S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
-            store_quad(p, f[q][0], f[q][1], f[q][2], f[q][3]);
+            store_pair(p, f[q][0], f[q][CPT - 1]);
+          }
+        }
+      } else if constexpr (CPT == 4) {
+        if (all_act) {  // four cells: one 8-byte store per plane
+          if constexpr (sr) {
+            {
+#pragma unroll
+              for (int q = 0; q < 9; q++) {
+                S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
+                *reinterpret_cast<uint2*>(p) = make_uint2(St::store2_sr(f[q][0], f[q][1], sr_bits(kp[0], q)),
+                                                          St::store2_sr(f[q][2], f[q][3], sr_bits(kp[1], q)));
+              }
+            }
+          }
+          if (!sr) {
+#pragma unroll
+            for (int q = 0; q < 9; q++) {
+              S* p = q == 4 ? rest_plane() + own : plane(slot(q)) + own;
+              store_quad(p, f[q][0], f[q][1], f[q][2], f[q][3]);
+            }
           }
         } else {
 #pragma unroll
@@ -515,8 +553,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
             if (!act[j]) continue;
 #pragma unroll
             for (int q = 0; q < 9; q++)
-              if (q != 4) plane(slot(q))[own + j] = St::store(f[q][j], q);
-            rest_plane()[own + j] = St::store(f[4][j], 4);
+              if (q != 4) plane(slot(q))[own + j] = word(q, j);
+            rest_plane()[own + j] = word(4, j);
           }
         }
       } else {
@@ -525,8 +563,8 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
           if (!act[j]) continue;
 #pragma unroll
           for (int q = 0; q < 9; q++)
-            if (q != 4) plane(slot(q))[own + j] = St::store(f[q][j], q);
-          rest_plane()[own + j] = St::store(f[4][j], 4);
+            if (q != 4) plane(slot(q))[own + j] = word(q, j);
+          rest_plane()[own + j] = word(4, j);
         }
       }
     }
@@ -581,7 +619,7 @@ __device__ __forceinline__ void ws_tile(const A& a, int xb, int y0, int y1, unsi
 }
 
 // The staged step over one lattice: CTA (bx, by) takes strip bx and row band by.
-template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW>
+template <class St, int EDGE, int NS, int CPT, bool CL, int W = kStageW, bool SR = false>
 __global__ void __launch_bounds__(stage_threads<CPT, W>(),
                                   W != kStageW ? 3 : (CPT == 1 ? 4 : (CPT == 2 ? (sizeof(typename St::S) == 8 ? 5 : 6) : 8)))
     k_step_ws(StepArgs<typename St::S, typename St::C> a) {
@@ -615,9 +653,11 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(),
   const bool down = sizeof(typename St::S) == 4 && (blockIdx.y & 1u) != 0u;
   // 16-bit storage: the arithmetic of the lattice's storage reference is
   // fixed per instantiation, chosen here once for the CTA
+  // Stochastic rounding is a separate kernel (SR), so that the
+  // round-to-nearest kernel keeps its own registers and code.
   if constexpr (St::kDev) {
-    if (a.ref.shift) ws_tile<St, EDGE, NS, CPT, CL, W, 1>(a, xb, y0, y1, smem, full, empty, down);
-    else ws_tile<St, EDGE, NS, CPT, CL, W, 0>(a, xb, y0, y1, smem, full, empty, down);
+    if (a.ref.shift) ws_tile<St, EDGE, NS, CPT, CL, W, 1, SR>(a, xb, y0, y1, smem, full, empty, down);
+    else ws_tile<St, EDGE, NS, CPT, CL, W, 0, SR>(a, xb, y0, y1, smem, full, empty, down);
   } else {
     ws_tile<St, EDGE, NS, CPT, CL, W, 0>(a, xb, y0, y1, smem, full, empty, down);
   }

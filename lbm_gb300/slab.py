@@ -53,9 +53,11 @@ class SlabLattice:
     """Rank `rank`'s slab of an nx x ny channel lattice.  `make_lattice(nx,
     rows)` builds the local lattice (default: lbm_gb300.Lattice in channel
     mode with the given omega and storage); the exchanger is attached with
-    `attach`."""
+    `attach`.  `rounding` = (mode, seed) sets the local lattice's rounding
+    (Lattice.set_rounding); its row origin is the slab's first row less one
+    (the ghost row), so stochastic rounding matches the undivided lattice."""
 
-    def __init__(self, nx, ny, omega, rank, world, storage=F32, u_in=0.1, make_lattice=None):
+    def __init__(self, nx, ny, omega, rank, world, storage=F32, u_in=0.1, make_lattice=None, rounding=None):
         if ny % world or ny // world < 2:
             raise ValueError("ny = %d does not split into %d slabs of >= 2 rows" % (ny, world))
         self.nx, self.ny, self.rank, self.world = nx, ny, rank, world
@@ -69,6 +71,10 @@ class SlabLattice:
                 lat.set_inlet_velocity(u_in)
                 return lat
         self.lat = make_lattice(nx, self.h + 2)
+        if hasattr(self.lat, "set_row_origin"):
+            self.lat.set_row_origin(self.y0 - 1)
+        if rounding is not None:
+            self.lat.set_rounding(*rounding)
         self.exchanger = None
         self.bufs = None
 

@@ -112,6 +112,60 @@ uint16_t float_to_bf16_rn(float f) {
 }
 float bf16_to_float(uint16_t b) { return u2f((uint32_t)b << 16); }
 
+// ---- stochastic rounding: the engine's cvt.rs.{f16x2,bf16x2}.f32 ---------
+// With k dropped bits (13 to a binary16 mantissa, 16 to a bfloat16 one) and
+// k random bits R, the magnitude rounds to floor(|f| / ulp + R / 2^k) ulps,
+// ulp the 16-bit spacing at |f| (the subnormal spacing 2^-24 below 2^-14 in
+// binary16); the sign is kept.  These are the conversions' observed results
+// on a GB300: 2^20 seeded pairs of each kind, across normal, subnormal,
+// overflowing and zero inputs, matched bit for bit.  Past the largest finite
+// binary16 the result is infinity (no saturation).  NaN stays NaN.
+uint16_t float_to_half_rs(float f, uint32_t r13) {
+  const uint32_t x = f2u(f), sign = (x >> 16) & 0x8000u, ax = x & 0x7fffffffu;
+  if (ax > 0x7f800000u) return (uint16_t)(sign | 0x7e00u);
+  const uint32_t e = ax >> 23;
+  uint32_t q;
+  if (e >= 113) {  // |f| >= 2^-14: add R below the kept mantissa, truncate, rebias 127 -> 15
+    const uint64_t t = (((uint64_t)ax + r13) >> 13) - (112u << 10);
+    q = t >= 0x7c00u ? 0x7c00u : (uint32_t)t;
+  } else {  // subnormal binary16: |f| * 2^24 = M >> k, with the kept quotient plus R / 2^13
+    const uint32_t m = (ax & 0x7fffffu) | (e ? 0x800000u : 0u);
+    const uint32_t k = 113u - (e ? e : 1u);  // 1 .. 112
+    const uint32_t mk = k >= 32u ? 0u : (m >> k);
+    q = (mk + r13) >> 13;
+  }
+  return (uint16_t)(sign | q);
+}
+uint16_t float_to_bf16_rs(float f, uint32_t r16) {
+  const uint32_t x = f2u(f), ax = x & 0x7fffffffu;
+  if (ax > 0x7f800000u) return (uint16_t)((x >> 16) | 0x40u);
+  return (uint16_t)(((x >> 16) & 0x8000u) | ((ax + r16) >> 16));
+}
+
+// Random bits of the stochastic rounding: a hash of (seed, step t, row y +
+// row origin, column pair x / 2, direction q).  fmix32 is MurmurHash3's
+// 32-bit finaliser; R_q = k_p * sr_mul(q) mod 2^32 with sr_mul(q) the odd
+// multiplier of direction q, the high word of SplitMix64's output for
+// (q + 1) * 0x9E3779B97F4A7C15 with the low bit set.  The even cell of a column pair takes bits [12:0] (binary16) or
+// [15:0] (bfloat16) of R_q, the odd cell bits [28:16] or [31:16].
+inline uint32_t fmix32(uint32_t h) {
+  h ^= h >> 16; h *= 0x85EBCA6Bu; h ^= h >> 13; h *= 0xC2B2AE35u; h ^= h >> 16;
+  return h;
+}
+inline uint32_t sr_mul(int q) {
+  uint64_t z = (uint64_t)(q + 1) * 0x9E3779B97F4A7C15ull;
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  z ^= z >> 31;
+  return (uint32_t)(z >> 32) | 1u;
+}
+inline uint32_t sr_pair_bits(uint32_t seed, uint64_t t, long y_global, long x, int q) {
+  const uint32_t st = fmix32(seed ^ ((uint32_t)t * 0x9E3779B1u));
+  const uint32_t ky = fmix32(st + (uint32_t)y_global * 0x85EBCA77u);
+  const uint32_t kp = fmix32(ky ^ ((uint32_t)(x >> 1) * 0xC2B2AE3Du));
+  return kp * sr_mul(q);  // mod 2^32: a bijection of kp (sr_mul is odd)
+}
+
 // Rest-state weights w_q = f_q^eq(rho=1, u=0), as f32 constants.
 template <class C> inline C weight(int q) {
   if (q == 4) return C(4.0) / C(9.0);
@@ -170,11 +224,13 @@ struct StF64 { using S = double; using C = double; static constexpr bool kDev = 
 struct StF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
   static C load(S s, int) { return half_to_float(s); }
   static S store(C v, int) { return float_to_half_rn(v); }
+  static S store_sr(C v, uint32_t R, long x) { return float_to_half_rs(v, (x & 1) ? (R >> 16) & 0x1fffu : R & 0x1fffu); }
   static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + half_to_float(s); }
   static S of_f(C v, int q, const StoreRef& R) { return float_to_half_rn((v - weight<float>(q)) - R.d[q]); } };
 struct StBF16 { using S = uint16_t; using C = float; static constexpr bool kDev = true;
   static C load(S s, int) { return bf16_to_float(s); }
   static S store(C v, int) { return float_to_bf16_rn(v); }
+  static S store_sr(C v, uint32_t R, long x) { return float_to_bf16_rs(v, (x & 1) ? R >> 16 : R & 0xffffu); }
   static C f_of(S s, int q, const StoreRef& R) { return R.r[q] + bf16_to_float(s); }
   static S of_f(C v, int q, const StoreRef& R) { return float_to_bf16_rn((v - weight<float>(q)) - R.d[q]); } };
 
@@ -284,6 +340,9 @@ struct SimBase {
   uint64_t step = 0;                 // compute_step, lbm.rs:1115
   double u_in = 0.1;                 // channel inlet velocity (and the 16-bit storage reference)
   bool store_inlet = false;          // 16-bit words relative to (u_in, 0); false (default): to the rest weights
+  bool sr_on = false;                // stochastic rounding of the collided 16-bit words
+  uint32_t sr_seed = 0;
+  long sr_y0 = 0;                    // row origin of the rounding hash
   std::vector<uint8_t> barrier;      // 1 = solid (the reference's u32 barrier buffer)
   virtual void set_omega(double w) = 0;
   virtual void set_inlet_velocity(double u) = 0;
@@ -477,7 +536,13 @@ template <class St> struct Sim : SimBase {
         rho[i] = r;
         if (frozen(i)) continue;
         collide_dev(g, r, dr, jxv, jyv, (float)w, ref);
-        for (int q = 0; q < 9; q++) (q == 4 ? origin[i] : F[q][i]) = St::store(g[q], q);
+        if (sr_on) {
+          const long x = (long)(i % (size_t)X), y = (long)(i / (size_t)X);
+          for (int q = 0; q < 9; q++)
+            (q == 4 ? origin[i] : F[q][i]) = St::store_sr(g[q], sr_pair_bits(sr_seed, step, y + sr_y0, x, q), x);
+        } else {
+          for (int q = 0; q < 9; q++) (q == 4 ? origin[i] : F[q][i]) = St::store(g[q], q);
+        }
       }
     } else {
     // pre_collide_corner, corner_pre_collision.wgsl:19-21
@@ -662,6 +727,17 @@ void orc_set_omega(orc_sim* h, double w) { ((SimBase*)h)->set_omega(w); }
 // re-expresses the stored words; lbm_set_inlet_velocity).
 void orc_set_inlet(orc_sim* h, double u) { ((SimBase*)h)->set_inlet_velocity(u); }
 void orc_set_storage_reference(orc_sim* h, int inlet) { ((SimBase*)h)->set_storage_reference(inlet != 0); }
+// stochastic rounding (16-bit storage): mode 1 on, 0 nearest
+void orc_set_rounding(orc_sim* h, int mode, uint32_t seed) {
+  SimBase* b = (SimBase*)h;
+  b->sr_on = mode == 1 && (b->prec == 1 || b->prec == 2);
+  b->sr_seed = b->sr_on ? seed : 0u;
+}
+void orc_set_row_origin(orc_sim* h, long y0) { ((SimBase*)h)->sr_y0 = y0; }
+// the conversions alone, for their known-answer tests
+uint16_t orc_half_rs(float v, uint32_t r13) { return float_to_half_rs(v, r13); }
+uint16_t orc_bf16_rs(float v, uint32_t r16) { return float_to_bf16_rs(v, r16); }
+uint32_t orc_sr_bits(uint32_t seed, uint64_t t, long y, long x, int q) { return sr_pair_bits(seed, t, y, x, q); }
 void orc_init_equilibrium(orc_sim* h, double rho, double ux, double uy, double amp, uint64_t seed) {
   ((SimBase*)h)->init_equilibrium(rho, ux, uy, amp, seed);
 }

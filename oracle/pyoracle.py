@@ -60,6 +60,14 @@ def lib():
         L.orc_set_omega.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_set_inlet.argtypes = [ctypes.c_void_p, ctypes.c_double]
         L.orc_set_storage_reference.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.orc_set_rounding.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32]
+        L.orc_set_row_origin.argtypes = [ctypes.c_void_p, ctypes.c_long]
+        L.orc_half_rs.restype = ctypes.c_uint16
+        L.orc_half_rs.argtypes = [ctypes.c_float, ctypes.c_uint32]
+        L.orc_bf16_rs.restype = ctypes.c_uint16
+        L.orc_bf16_rs.argtypes = [ctypes.c_float, ctypes.c_uint32]
+        L.orc_sr_bits.restype = ctypes.c_uint32
+        L.orc_sr_bits.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_long, ctypes.c_long, ctypes.c_int]
         L.orc_init_equilibrium.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_uint64]
         L.orc_init_equilibrium_noise.argtypes = [ctypes.c_void_p, ctypes.c_double, ctypes.c_double,
@@ -122,6 +130,14 @@ class Oracle:
     def set_storage_reference(self, inlet):
         """16-bit words relative to the inlet equilibrium (True) or the rest weights."""
         lib().orc_set_storage_reference(self.h, 1 if inlet else 0)
+
+    def set_rounding(self, mode, seed=0):
+        """Rounding of the collided 16-bit words: 0 nearest, 1 stochastic (seeded)."""
+        lib().orc_set_rounding(self.h, int(mode), int(seed) & 0xFFFFFFFF)
+
+    def set_row_origin(self, y0):
+        """Row y hashes as y + y0 in the stochastic rounding."""
+        lib().orc_set_row_origin(self.h, int(y0))
 
     def init_equilibrium(self, rho=1.0, ux=0.1, uy=0.0, noise=0.0, seed=0):
         lib().orc_init_equilibrium(self.h, rho, ux, uy, noise, seed)
@@ -195,6 +211,21 @@ class Oracle:
 
 
 _ref = None
+
+
+def half_rs(v, r13):
+    """binary16 bits of float32 `v` rounded stochastically with 13 random bits."""
+    return lib().orc_half_rs(float(v), int(r13))
+
+
+def bf16_rs(v, r16):
+    """bfloat16 bits of float32 `v` rounded stochastically with 16 random bits."""
+    return lib().orc_bf16_rs(float(v), int(r16))
+
+
+def sr_bits(seed, t, y, x, q):
+    """The 32 random bits of direction q for the column pair of cell (x, y) at step t."""
+    return lib().orc_sr_bits(int(seed) & 0xFFFFFFFF, int(t), int(y), int(x), int(q))
 
 
 def ref_available():

@@ -153,10 +153,12 @@ def _forge(ck, fmt, offset, *values):
 @pytest.mark.parametrize("field,fmt,offset,value", [
     ("cur", "<I", 48, 2), ("materialised", "<I", 52, 7), ("closure", "<I", 56, 2),
     ("omega", "<f", 28, float("nan")), ("omega", "<f", 28, 2.5), ("u_in", "<f", 32, float("inf")),
-    ("drift", "<f", 36, float("nan")), ("drift", "<f", 36, -1.0), ("store_inlet", "<I", 76, 2)])
+    ("drift", "<f", 36, float("nan")), ("drift", "<f", 36, -1.0), ("store_inlet", "<I", 76, 2),
+    ("rounding", "<I", 80, 2), ("rounding", "<I", 80, 1)])
 def test_gpu_checkpoint_header_fields_are_range_checked(lbm, cuda_ok, field, fmt, offset, value):
     """A header whose fields steer device work (the buffer index `cur`, the
-    flags, omega, the inlet and the drift bound) is refused with LBM_ERR_ARG
+    flags, omega, the inlet, the drift bound, the rounding mode: stochastic
+    rounding of this f32 lattice included) is refused with LBM_ERR_ARG
     before anything is copied, even with a matching CRC."""
     a = make(lbm, 40, 20, 1, lbm.F32, 3)
     a.iterate(4)
@@ -166,7 +168,7 @@ def test_gpu_checkpoint_header_fields_are_range_checked(lbm, cuda_ok, field, fmt
         a.restore(_forge(ck, fmt, offset, value))
     assert e.value.code == 1 and "checkpoint header" in str(e.value)
     np.testing.assert_array_equal(a.populations(), want)  # the lattice is untouched
-    a.restore(_forge(ck, "<I", 80, 5))  # a reserved word: accepted once the CRC matches
+    a.restore(_forge(ck, "<I", 92, 5))  # the reserved word: accepted once the CRC matches
     a.close()
 
 
