@@ -67,6 +67,14 @@ int lbm_batch_read_populations(lbm_batch* batch, uint32_t domain, float* out);
  * else crosses between ranks. */
 int lbm_batch_conservation(lbm_batch* batch, double* out);
 
+/* Rounding of the stored words (lbm_set_rounding): LBM_ROUND_NEAREST (the
+ * default) or, for f16 / bf16 batches, LBM_ROUND_STOCHASTIC.  Domain d then
+ * rounds exactly as a single lattice of its size with seed `seed + d`; the
+ * step index is the batch's.  LBM_ERR_ARG for stochastic rounding of an
+ * f32 batch. */
+int lbm_batch_set_rounding(lbm_batch* batch, int mode, uint32_t seed);
+int lbm_batch_get_rounding(const lbm_batch* batch, int* mode, uint32_t* seed);
+
 /* Fix the schedule by hand: variant 0..5 = (ring stages, cells per thread,
  * strip columns) (4,1,256) (6,1,256) (4,2,256) (8,2,256) (6,2,512)
  * (4,2,512), the 512-column strips for f16 / bf16 only (f32 runs variants 4

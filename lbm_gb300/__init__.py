@@ -151,6 +151,8 @@ _SIGS = [
     ("lbm_batch_read_populations", ctypes.c_int, [_P, ctypes.c_uint32, _P]),
     ("lbm_batch_conservation", ctypes.c_int, [_P, _P]),
     ("lbm_batch_set_schedule", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, _P]),
+    ("lbm_batch_set_rounding", ctypes.c_int, [_P, ctypes.c_int, ctypes.c_uint32]),
+    ("lbm_batch_get_rounding", ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32)]),
     ("lbm_batch_autotune", ctypes.c_int, [_P, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]),
 ]
 

@@ -96,6 +96,19 @@ class Batch:
         _check(self._lib.lbm_batch_conservation(self._h, _ptr(out)))
         return out.reshape(-1, 3)
 
+    def set_rounding(self, mode, seed=0):
+        """Rounding of the stored words (Lattice.set_rounding): domain d rounds
+        as a single lattice with seed `seed + d`; stochastic rounding needs
+        f16 / bf16 storage."""
+        _check(self._lib.lbm_batch_set_rounding(self._h, int(mode), int(seed) & 0xFFFFFFFF))
+
+    @property
+    def rounding(self):
+        """(mode, seed)."""
+        m, sd = ctypes.c_int(), ctypes.c_uint32()
+        _check(self._lib.lbm_batch_get_rounding(self._h, ctypes.byref(m), ctypes.byref(sd)))
+        return m.value, sd.value
+
     def set_schedule(self, variant=0, dynamic=0, rows=None):
         r = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
         _check(self._lib.lbm_batch_set_schedule(self._h, int(variant), int(dynamic), None if r is None else _ptr(r)))

@@ -71,7 +71,7 @@ struct DomainDev {
 // A tile's step arguments from its domain's descriptor.
 template <class S, class C>
 __device__ void fill_args(StepArgs<S, C>& sa, const DomainDev& d, int src_i, int dst_i, int materialised,
-                          int write_moments, int rows, int* flag) {
+                          int write_moments, int rows, int* flag, const SrArgs& sr, int domain) {
   sa.L = d.L;
   sa.src = (const S*)d.f[src_i];
   sa.dst = (S*)d.f[dst_i];
@@ -95,9 +95,9 @@ __device__ void fill_args(StepArgs<S, C>& sa, const DomainDev& d, int src_i, int
   sa.closure = nullptr;
   sa.fallback = nullptr;
   sa.tau0 = sa.drift = 0.0f;
-  sa.sr.on = 0u;  // batched domains round to nearest
-  sa.sr.seed = sa.sr.t = 0u;
-  sa.sr.clock = nullptr;
+  // rounding: domain d rounds as a single lattice with seed + d
+  sa.sr = sr;
+  sa.sr.seed = sr.seed + (uint32_t)domain;
   sa.sr.y0 = 0;
 }
 
@@ -108,10 +108,12 @@ __device__ void fill_args(StepArgs<S, C>& sa, const DomainDev& d, int src_i, int
 // arguments are then double-buffered: the producer writes tile k's copy just
 // before its first stage (the consumers read it after that stage arrives)
 // once the consumers have released the copy of tile k - 2 (`args_free`).
-template <class St, int NS, int CPT, int W>
+// SR: stochastic rounding of the stored 16-bit words, a kernel of its own so
+// that the round-to-nearest kernel keeps its registers.
+template <class St, int NS, int CPT, int W, bool SR = false>
 __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (CPT == 1 ? 4 : 6))
     k_batch_step(const DomainDev* __restrict__ doms, const int4* __restrict__ tiles, int ntiles, int src_i, int dst_i,
-                 int materialised, int write_moments, int dynamic, int* counter, int* flag) {
+                 int materialised, int write_moments, int dynamic, int* counter, int* flag, SrArgs sr) {
   using S = typename St::S;
   using C = typename St::C;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -150,13 +152,13 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
         if (k >= 2 && !__all_sync(0xffffffffu, mbar_wait(smem_addr(&args_free[k & 1]), (uint32_t)(((k - 2) >> 1) & 1)))) {
           if (lane == 0) atomicOr(flag, 2);
         }
-        if (lane == 0) fill_args(A, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag);
+        if (lane == 0) fill_args(A, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag, sr, T.x);
         __syncwarp();
       }
       if (St::kDev && doms[T.x].ref.shift)
-        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
+        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1, SR>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
       else
-        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
+        ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0, SR>(A, xb, T.z, T.w, smem, full, empty, down, g, false, last);
       if (!producer) {
         __syncwarp();
         if (lane == 0) mbar_arrive(smem_addr(&args_free[k & 1]));
@@ -177,7 +179,8 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
     const int4 T = tiles[t];
     const int xb = T.y & 0x3FFFFFFF;
     const bool down = (T.y >> 30) != 0;
-    if (threadIdx.x == 0) fill_args(sa, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag);
+    if (threadIdx.x == 0)
+      fill_args(sa, doms[T.x], src_i, dst_i, materialised, write_moments, T.w - T.z, flag, sr, T.x);
     __syncthreads();
     if (materialised) {
       const int x0 = xb + CPT * (int)threadIdx.x;
@@ -188,9 +191,9 @@ __global__ void __launch_bounds__(stage_threads<CPT, W>(), W != kStageW ? 3 : (C
     } else {
       if constexpr (St::kDev) {
         if (sa.ref.shift)
-          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1>(sa, xb, T.z, T.w, smem, full, empty, down);
+          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 1, SR>(sa, xb, T.z, T.w, smem, full, empty, down);
         else
-          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
+          ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0, SR>(sa, xb, T.z, T.w, smem, full, empty, down);
       } else {
         ws_tile<St, EDGE_CHANNEL, NS, CPT, false, W, 0>(sa, xb, T.z, T.w, smem, full, empty, down);
       }
@@ -254,6 +257,12 @@ struct lbm_batch {
   int grid = 0;  // persistent CTAs
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // kGraphSteps steps from buffer parity 0 / 1
   std::string report;
+  // stochastic rounding (16-bit storage): domain d uses seed sr_seed + d;
+  // captured graphs read their first step's index from clock_d
+  uint32_t sr_on = 0, sr_seed = 0;
+  uint32_t* clock_d = nullptr;
+  bool capturing = false;
+  uint64_t capture_steps0 = 0;
 };
 
 namespace {
@@ -267,17 +276,22 @@ template <class F> int dispatch_st(int storage, F&& f) {
   return bfail(LBM_ERR_ARG, "batched lattices support f32, f16 and bf16 storage");
 }
 
-template <class St, int NS, int CPT, int W> void* kernel_ptr() { return (void*)k_batch_step<St, NS, CPT, W>; }
+template <class St, int NS, int CPT, int W> void* kernel_ptr(bool sr) {
+  if constexpr (St::kDev) {
+    if (sr) return (void*)k_batch_step<St, NS, CPT, W, true>;
+  }
+  return (void*)k_batch_step<St, NS, CPT, W>;
+}
 
-template <class St> void* variant_kernel(int v) {
+template <class St> void* variant_kernel(int v, bool sr) {
   constexpr bool k16 = sizeof(typename St::S) == 2;
   switch (v) {
-    case 0: return kernel_ptr<St, 4, 1, kStageW>();
-    case 1: return kernel_ptr<St, 6, 1, kStageW>();
-    case 2: return kernel_ptr<St, 4, 2, kStageW>();
-    case 3: return kernel_ptr<St, 8, 2, kStageW>();
-    case 4: return k16 ? kernel_ptr<St, 6, 2, 2 * kStageW>() : kernel_ptr<St, 6, 2, kStageW>();
-    default: return k16 ? kernel_ptr<St, 4, 2, 2 * kStageW>() : kernel_ptr<St, 4, 2, kStageW>();
+    case 0: return kernel_ptr<St, 4, 1, kStageW>(sr);
+    case 1: return kernel_ptr<St, 6, 1, kStageW>(sr);
+    case 2: return kernel_ptr<St, 4, 2, kStageW>(sr);
+    case 3: return kernel_ptr<St, 8, 2, kStageW>(sr);
+    case 4: return k16 ? kernel_ptr<St, 6, 2, 2 * kStageW>(sr) : kernel_ptr<St, 6, 2, kStageW>(sr);
+    default: return k16 ? kernel_ptr<St, 4, 2, 2 * kStageW>(sr) : kernel_ptr<St, 4, 2, kStageW>(sr);
   }
 }
 
@@ -331,7 +345,7 @@ int configure(lbm_batch* b) {
   const size_t smem = (size_t)NS * stage_bytes(b->storage, W);
   auto setup = [&](auto tag) -> int {
     using St = decltype(tag);
-    void* k = variant_kernel<St>(b->cfg.variant);
+    void* k = variant_kernel<St>(b->cfg.variant, b->sr_on != 0u);
     BCK(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int occ = 0, sms = 0;
     BCK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, W / CPT + 32, smem));
@@ -353,11 +367,18 @@ int launch_step(lbm_batch* b, bool write_moments, int* counter) {
   const int src = b->cur, dst = b->materialised ? b->cur : 1 - b->cur;
   int mat = b->materialised ? 1 : 0, wm = write_moments ? 1 : 0, dyn = b->cfg.dynamic;
   if (dyn == 1) BCK(cudaMemsetAsync(counter, 0, sizeof(int), b->stream));
-  void* args[] = {&b->d_doms, &b->d_tiles, &b->ntiles, (void*)&src, (void*)&dst, &mat, &wm, &dyn, &counter, &b->d_flag};
+  SrArgs sr;
+  sr.on = b->sr_on;
+  sr.seed = b->sr_seed;
+  sr.clock = b->capturing && b->sr_on ? b->clock_d : nullptr;
+  sr.t = sr.clock ? (uint32_t)(b->steps - b->capture_steps0) : (uint32_t)b->steps;
+  sr.y0 = 0;
+  void* args[] = {&b->d_doms, &b->d_tiles, &b->ntiles, (void*)&src, (void*)&dst, &mat, &wm, &dyn, &counter, &b->d_flag,
+                  &sr};
   auto go = [&](auto tag) -> int {
     using St = decltype(tag);
-    BCK(cudaLaunchKernel(variant_kernel<St>(b->cfg.variant), dim3(b->grid), dim3(W / CPT + 32), args, smem,
-                         b->stream));
+    BCK(cudaLaunchKernel(variant_kernel<St>(b->cfg.variant, b->sr_on != 0u), dim3(b->grid), dim3(W / CPT + 32), args,
+                         smem, b->stream));
     return LBM_OK;
   };
   int rc = dispatch_st(b->storage, go);
@@ -390,7 +411,10 @@ int capture_graph(lbm_batch* b) {
   cudaGraph_t g;
   BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   int rc = LBM_OK;
+  b->capturing = true;
+  b->capture_steps0 = steps0;
   for (int k = 0; k < kGraphSteps && !rc; k++) rc = launch_step(b, false, b->d_counter + 1 + k);
+  b->capturing = false;
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   b->cur = cur0;  // capture recorded the launches without running them
   b->steps = steps0;
@@ -444,6 +468,7 @@ void release(lbm_batch* b) {
   cudaFree(b->d_tiles);
   cudaFree(b->d_counter);
   cudaFree(b->d_flag);
+  cudaFree(b->clock_d);
   cudaFree(b->d_staging);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
@@ -615,6 +640,11 @@ int lbm_batch_step(lbm_batch* b, uint32_t n) {
     const bool last = left == 1;
     if (!b->materialised && !last && left > (uint32_t)kGraphSteps) {
       if (!b->graph[b->cur] && (rc = capture_graph(b))) return rc;
+      if (b->sr_on) {  // the replay's first step index, read by its launches
+        k_set_clock<<<1, 1, 0, b->stream>>>(b->clock_d, (uint32_t)b->steps);
+        BCK(cudaGetLastError());
+        b->launches++;
+      }
       BCK(cudaGraphLaunch(b->graph[b->cur], b->stream));
       b->launches += kGraphSteps;
       b->steps += kGraphSteps;  // kGraphSteps is even: the buffer parity is unchanged
@@ -729,6 +759,26 @@ int lbm_batch_read_populations(lbm_batch* b, uint32_t domain, float* out) {
   b->launches++;
   BCK(cudaMemcpyAsync(out, b->d_staging, (size_t)9 * h.nx * h.ny * 4, cudaMemcpyDeviceToHost, b->stream));
   BCK(cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+int lbm_batch_set_rounding(lbm_batch* b, int mode, uint32_t seed) {
+  if (!b) return bfail(LBM_ERR_ARG, "null batch");
+  if (mode != LBM_ROUND_NEAREST && mode != LBM_ROUND_STOCHASTIC)
+    return bfail(LBM_ERR_ARG, "rounding mode %d: 0 nearest, 1 stochastic", mode);
+  if (mode == LBM_ROUND_STOCHASTIC && b->storage == STORE_F32)
+    return bfail(LBM_ERR_ARG, "stochastic rounding applies to 16-bit storage");
+  if (mode == LBM_ROUND_STOCHASTIC && !b->clock_d && cudaMalloc(&b->clock_d, sizeof(uint32_t)) != cudaSuccess)
+    return bfail(LBM_ERR_NOMEM, "step clock word");
+  b->sr_on = mode == LBM_ROUND_STOCHASTIC ? 1u : 0u;
+  b->sr_seed = b->sr_on ? seed : 0u;
+  return configure(b);  // the kernel, its occupancy and the captured graphs change
+}
+
+int lbm_batch_get_rounding(const lbm_batch* b, int* mode, uint32_t* seed) {
+  if (!b || !mode || !seed) return bfail(LBM_ERR_ARG, "null argument");
+  *mode = b->sr_on ? LBM_ROUND_STOCHASTIC : LBM_ROUND_NEAREST;
+  *seed = b->sr_seed;
   return LBM_OK;
 }
 

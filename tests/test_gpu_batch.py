@@ -73,6 +73,37 @@ def test_gpu_batch_matches_oracle_per_domain(lbm, cuda_ok, oracle_mod, storage, 
         assert b.info()[2] == 50
 
 
+@pytest.mark.parametrize("storage,prec", [(1, 1), (2, 2)])
+@pytest.mark.parametrize("variant,dynamic", [(2, 0), (3, 1), (4, 2), (0, 1)])
+def test_gpu_batch_stochastic_rounding_matches_oracle_per_domain(lbm, cuda_ok, oracle_mod, storage, prec, variant,
+                                                                 dynamic):
+    """Stochastic rounding in the batch: domain d rounds as a single lattice
+    with seed + d, through plain launches and graph replays (47 steps), every
+    schedule form, bit for bit against its oracle run."""
+    P = oracle_mod
+    b, masks = make_batch(lbm, storage)
+    with b:
+        b.set_schedule(variant, dynamic, [32, 64, 32])
+        b.set_rounding(lbm.ROUND_STOCHASTIC, 900)
+        assert b.rounding == (lbm.ROUND_STOCHASTIC, 900)
+        b.init_equilibrium(1e-2, 5)
+        orc = []
+        for d, m in enumerate(masks):
+            b.set_mask(d, m)
+            o = oracle_for(P, b, d, prec, m, 1e-2, 5)
+            o.set_rounding(1, 900 + d)
+            orc.append(o)
+        b.step(47)
+        for o in orc:
+            o.step(47)
+        for d in range(b.count):
+            assert_domain(b, d, orc[d])
+    f32, _ = make_batch(lbm, 0)
+    with f32:
+        with pytest.raises(lbm.LBMError):
+            f32.set_rounding(lbm.ROUND_STOCHASTIC, 1)
+
+
 # (variant, schedule: 0 static, 1 tickets, 2 static through one ring, band rows); [5, 64, 7] gives
 # tiles shorter than the deepest ring, so one ring carries several of a CTA's tiles at once
 SCHEDULES = [(v, dyn, rows) for v in range(6) for dyn in (0, 1, 2) for rows in ([32, 32, 32], [5, 64, 7], [3, 2, 3])]
