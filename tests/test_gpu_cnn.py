@@ -166,13 +166,16 @@ def test_gpu_fused_inference_matches_oracle(lbm, torch_cuda, kernel):
     assert np.abs(sp.reshape(ny, nx) - speed)[fl].max() <= 2e-3 * speed[fl].max()
 
 
-@pytest.mark.parametrize("storage", [0, 1, 2])
+@pytest.mark.parametrize("storage,sr", [(0, False), (1, False), (2, False), (1, True), (2, True)])
 @pytest.mark.parametrize("kernel", [0, 1, 3, 8, 9, 11])
-def test_gpu_closure_step_equals_plain_step_at_the_same_omega(lbm, torch_cuda, storage, kernel):
+def test_gpu_closure_step_equals_plain_step_at_the_same_omega(lbm, torch_cuda, storage, sr, kernel):
     """All-zero weights give z = bias = 0, delta_tau = DT_MAX / 2 = 0.125
     exactly, so every fluid cell relaxes with 1 / (1 / omega + 0.125): that
     must reproduce a plain run at that omega bit for bit.  A NaN bias gives
-    no valid prediction: every cell takes the plain omega and is counted."""
+    no valid prediction: every cell takes the plain omega and is counted.
+    With stochastic rounding the closure kernels store cell by cell and the
+    plain 16-bit kernels two cells per word, from the same random bits: the
+    runs still agree bit for bit."""
     if storage == 0 and kernel == 8:
         kernel = 6
     from lbm_gb300 import closure, geometry
@@ -188,6 +191,8 @@ def test_gpu_closure_step_equals_plain_step_at_the_same_omega(lbm, torch_cuda, s
             lat.set_inlet_velocity(0.07)
             lat.init_equilibrium(1.0, 0.07, 0.0, 1e-2, 2)
             lat.draw_mask(mask)
+            if sr:
+                lat.set_rounding(lbm.ROUND_STOCHASTIC, 31)
             fb = ctypes.c_uint64(0)
             if weights is not None:
                 lbm._check(L.lbm_closure_set_weights(lat.handle, weights.ctypes.data_as(ctypes.c_void_p),

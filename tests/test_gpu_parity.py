@@ -73,7 +73,7 @@ def test_gpu_matches_reference_single_cell_fixture(lbm, cuda_ok):
 
 
 def run_pair(lbm, P, nx, ny, omega, edge, storage, prec, steps, mask, ux=0.1, noise=1e-3, seed=0, rows=8,
-             chunks=None, edits=None, kernel=1, store_inlet=None):
+             chunks=None, edits=None, kernel=1, store_inlet=None, sr_seed=None):
     lat = lbm.Lattice(nx, ny, omega, edge, storage)
     lat.set_tuning(rows, kernel)
     o = P.Oracle(nx, ny, float(np.float32(omega)), edge, prec)
@@ -87,6 +87,9 @@ def run_pair(lbm, P, nx, ny, omega, edge, storage, prec, steps, mask, ux=0.1, no
     if mask is not None:
         lat.draw_mask(mask)
         o.set_mask(mask)
+    if sr_seed is not None:  # stochastic rounding of the stored 16-bit words
+        lat.set_rounding(lbm.ROUND_STOCHASTIC, sr_seed)
+        o.set_rounding(1, sr_seed)
     for k, c in enumerate(chunks or [steps]):
         lat.iterate(c)
         o.step(c)
@@ -176,14 +179,17 @@ def test_gpu_random_small_grids(lbm, cuda_ok, oracle_mod, storage, prec, f64, ed
 
 
 @pytest.mark.parametrize("edge", [0, 1])
-@pytest.mark.parametrize("storage,store_inlet", [(0, True), (1, True), (2, True), (1, False), (2, False)])
-def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge, storage, store_inlet):
+@pytest.mark.parametrize("storage,store_inlet,sr", [(0, True, False), (1, True, False), (2, True, False),
+                                                    (1, False, False), (2, False, False), (1, True, True),
+                                                    (2, False, True)])
+def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge, storage, store_inlet, sr):
     """Barrier edits, omega and inlet changes between iterate calls keep the
     reference's step semantics (the fused state is materialised first).  In
     16-bit storage the inlet change re-expresses the stored words against the
     new inlet equilibrium (or, with the rest-weight reference, leaves them),
     and the last edit switches the storage reference; every step of it
-    matches the oracle bit for bit."""
+    matches the oracle bit for bit, with stochastic rounding too (the edits
+    and re-expressions round to nearest, the steps stochastically)."""
     P = oracle_mod
     nx, ny = 64, 40
     rng = np.random.default_rng(5 + edge)
@@ -213,7 +219,8 @@ def test_gpu_state_edits_between_steps(lbm, cuda_ok, oracle_mod, edge, storage, 
         assert lat.storage_reference == (not store_inlet)
 
     lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.7, edge, storage, storage, 0, mask, chunks=[7, 5, 1, 9, 4, 6, 5],
-                      edits=[draw, omega, inlet, draw, reset_barrier, switch_reference], store_inlet=store_inlet)
+                      edits=[draw, omega, inlet, draw, reset_barrier, switch_reference], store_inlet=store_inlet,
+                      sr_seed=77 if sr else None)
     assert_same_state(lat, o)
     assert lat.get_compute_num() == o.step_count
     lat.close()
