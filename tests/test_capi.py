@@ -46,6 +46,27 @@ def test_error_path_without_device(lbm):
     assert L.lbm_step(None, 1) == 1
 
 
+def test_limits_and_null_arguments_without_device(lbm):
+    """Grids past the size limits, unknown storage, null outputs and null
+    handles are refused with LBM_ERR_ARG (1) before any device work; so are
+    the rounding entry points without a lattice or without outputs."""
+    L = lbm.load_library()
+    h = ctypes.c_void_p()
+    assert L.lbm_create(1 << 20, 1 << 15, 1.0, 0, 0, ctypes.byref(h)) == 1  # 8 planes past 2^32 cells
+    assert b"too large" in L.lbm_last_error()
+    assert L.lbm_create(64, 70000, 1.0, 0, 0, ctypes.byref(h)) == 1  # more rows than the limit
+    assert L.lbm_create(64, 64, 1.0, 0, 9, ctypes.byref(h)) == 1
+    assert b"storage" in L.lbm_last_error()
+    assert L.lbm_create(64, 64, 1.0, 0, 0, None) == 1
+    mode, seed, origin = ctypes.c_int(), ctypes.c_uint32(), ctypes.c_int32()
+    assert L.lbm_set_rounding(None, 1, 5) == 1
+    assert L.lbm_get_rounding(None, ctypes.byref(mode), ctypes.byref(seed)) == 1
+    assert L.lbm_set_row_origin(None, 3) == 1
+    assert L.lbm_get_row_origin(None, ctypes.byref(origin)) == 1
+    assert L.lbm_batch_set_rounding(None, 1, 5) == 1
+    assert L.lbm_batch_get_rounding(None, ctypes.byref(mode), ctypes.byref(seed)) == 1
+
+
 def test_library_is_built_for_sm_103a(lbm):
     """ptxas reports every kernel compiled for sm_103a (the build keeps its log)."""
     logs = glob.glob(os.path.join(ROOT, "lbm_gb300", "_build", "*.ptxas.txt"))
