@@ -41,15 +41,17 @@ import time
 
 import numpy as np
 
-from . import EDGE_CHANNEL, F16, F32, LBMError, Lattice, _check, load_library
+from . import EDGE_CHANNEL, F16, F32, ROUND_STOCHASTIC, LBMError, Lattice, _check, load_library
 from .geometry import random_circles
 
 
-def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, drift=1.0, seed=1, ramp=0):
+def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, drift=1.0, seed=1, ramp=0,
+        stochastic=False):
     """One run (see the module docstring).  ramp > 0 starts the fluid at rest
     and raises the inlet velocity linearly to u over the first `ramp` steps
     (lbm_set_inlet_velocity between samples, outside the timing) instead of
-    starting the whole field at u."""
+    starting the whole field at u.  stochastic=True rounds the stored words
+    of 16-bit storage stochastically (Lattice.set_rounding, seeded by `seed`)."""
     import torch
     lib = load_library()
     stream = torch.cuda.Stream()
@@ -57,9 +59,13 @@ def run(nx, ny, tau, u, mask, steps, every, storage, params=None, refresh=20, dr
     acc = torch.zeros((2, ny, nx), dtype=torch.float32, device=dev)
     tmp = torch.empty((ny, nx), dtype=torch.float32, device=dev)
     active = int((mask[:, 1:] == 0).sum())
-    out = {"storage": "f32" if storage == F32 else "f16", "closure": params is not None, "ramp": ramp}
+    sr = stochastic and storage != F32
+    out = {"storage": "f32" if storage == F32 else "f16", "closure": params is not None, "ramp": ramp,
+           "rounding": "stochastic" if sr else "nearest"}
     with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
         lat.set_stream(stream.cuda_stream)
+        if sr:
+            lat.set_rounding(ROUND_STOCHASTIC, seed)
         u0 = 0.0 if ramp else u
         lat.set_inlet_velocity(u0)
         lat.init_equilibrium(1.0, u0, 0.0, 1e-4, seed)
@@ -128,14 +134,16 @@ def _field(lat, lib, code, tmp):
     return tmp
 
 
-def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refresh=20, drift=1.0, seed=1, ramp=0):
+def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refresh=20, drift=1.0, seed=1, ramp=0,
+             stochastic=False):
     """Where and how a run first goes non-finite (see the module docstring).
     `first_bad` is the sample at which the step kernels' flag was first seen
     set; the run is repeated to `first_bad - every` and then stepped singly.
     The repeat follows run()'s schedule exactly (one step, then the closure
     inferred before steps 1, 1 + refresh, ..., and with a ramp the inlet
     raised after steps 1 + every, 1 + 2 every, ...), so it retraces the same
-    states bit for bit."""
+    states bit for bit (with the same rounding: stochastic rounding is a
+    function of seed, step and cell)."""
     import torch
     from scipy import ndimage
     lib = load_library()
@@ -144,6 +152,8 @@ def diagnose(nx, ny, tau, u, mask, storage, first_bad, every, params=None, refre
     rep = {}
     with Lattice(nx, ny, 1.0 / tau, EDGE_CHANNEL, storage) as lat:
         lat.set_stream(stream.cuda_stream)
+        if stochastic and storage != F32:
+            lat.set_rounding(ROUND_STOCHASTIC, seed)
         u0 = 0.0 if ramp else u
         lat.set_inlet_velocity(u0)
         lat.init_equilibrium(1.0, u0, 0.0, 1e-4, seed)
@@ -239,6 +249,8 @@ def main(argv=None):
                          "whole field at --u)")
     ap.add_argument("--outlet-clearance", type=int, default=128,
                     help="keep the circles this many cells from the outflow column (-1: they may touch it)")
+    ap.add_argument("--stochastic", action="store_true",
+                    help="round the f16 runs' stored words stochastically (lbm_set_rounding)")
     ap.add_argument("--diagnose", action="store_true",
                     help="for each run that goes non-finite, locate the first non-finite step and cells")
     a = ap.parse_args(argv)
@@ -264,19 +276,21 @@ def main(argv=None):
     def diag(r, storage, params=None):
         if a.diagnose and r["first_nonfinite_by_step"] is not None:
             r["diagnosis"] = diagnose(nx, ny, a.tau, a.u, mask, storage, r["first_nonfinite_by_step"], a.every,
-                                      params=params, refresh=a.refresh, drift=a.drift, seed=a.seed, ramp=a.ramp)
+                                      params=params, refresh=a.refresh, drift=a.drift, seed=a.seed, ramp=a.ramp,
+                                      stochastic=a.stochastic)
 
     if not a.closure_only:
         r32, u32 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F32, seed=a.seed, ramp=a.ramp)
         diag(r32, F32)
-        r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed, ramp=a.ramp)
+        r16, u16 = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, seed=a.seed, ramp=a.ramp,
+                       stochastic=a.stochastic)
         diag(r16, F16)
         r16["vel_err_vs_f32"] = err(u16)
         rep["runs"] = [r32, r16]
     if a.closure:
         params = np.load(a.closure)["params"]
         rc, uc = run(nx, ny, a.tau, a.u, mask, a.steps, a.every, F16, params=params, refresh=a.refresh, ramp=a.ramp,
-                     drift=a.drift, seed=a.seed)
+                     drift=a.drift, seed=a.seed, stochastic=a.stochastic)
         diag(rc, F16, params)
         rc["vel_err_vs_f32"] = err(uc)
         rc["refresh"], rc["drift"] = a.refresh, a.drift
