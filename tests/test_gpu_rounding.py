@@ -160,3 +160,21 @@ def test_gpu_stochastic_rounding_checkpoint_resume(lbm, cuda_ok, oracle_mod, sto
         assert again.rounding == (lbm.ROUND_STOCHASTIC, 4242) and again.row_origin == -7
         again.iterate(30)
         np.testing.assert_array_equal(again.populations(), want)
+
+
+def test_gpu_stochastic_rounding_full_size(lbm, cuda_ok, oracle_mod):
+    """The 4096 x 2048 workload (200 circles, tau 0.55, ux 0.08) in f16 with
+    f - w words, default kernel, 200 steps with stochastic rounding: the
+    populations equal the oracle's bit for bit on the full grid (graph
+    replays with the step index read from the clock word, programmatic
+    launches between steps)."""
+    from lbm_gb300 import geometry
+    P = oracle_mod
+    nx, ny = 4096, 2048
+    mask = geometry.random_circles(nx, ny, 200, 4, 32, seed=1, inlet_clearance=64)
+    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.55, 1, lbm.F16, P.P_F16, 0, mask, ux=0.08, noise=1e-4, seed=1,
+                      rows=2, kernel=11, sr_seed=0x5EED)
+    lat.iterate(200)
+    o.step(200)
+    np.testing.assert_array_equal(lat.populations(), o.state()[0].astype(np.float32))
+    lat.close()
