@@ -226,7 +226,12 @@ int lbm_step_rows(lbm_sim* sim, uint32_t y0, uint32_t y1, int flags);
  * change).  On by default; results are the same either way.  Not on the
  * legacy default stream, which cannot be captured, nor while the caller is
  * capturing the lattice's stream.  enable = 0 turns it off and frees the
- * graphs. */
+ * graphs.  Steps recorded in a caller's own capture are plain launches
+ * that replay from the buffer parity they were recorded at: record an even
+ * number of steps, from a state that has taken at least one step since its
+ * last initialisation or edit (that step collides in place), and the
+ * graph can be replayed any number of times.  The host-side step count
+ * advances once, by the recorded steps, not per replay. */
 int lbm_set_graphs(lbm_sim* sim, int enable);
 
 /* Wait for queued work; returns LBM_ERR_STATE if a step saw a non-finite density. */

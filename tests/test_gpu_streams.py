@@ -74,3 +74,31 @@ def test_gpu_rebase_queued_before_a_stream_switch_comes_first(lbm, cuda_ok, stor
     lat.iterate(20)
     np.testing.assert_array_equal(lat.populations(), want)
     lat.close()
+
+
+@pytest.mark.parametrize("storage,prec", [(0, 0), (1, 1)])
+def test_gpu_steps_in_a_callers_own_capture(lbm, cuda_ok, oracle_mod, storage, prec):
+    """lbm_step inside the caller's stream capture records plain launches;
+    replaying the caller's graph three times advances the state by three
+    times the recorded (even) steps, bit for bit with the oracle."""
+    import torch
+    from test_gpu_parity import run_pair
+    P = oracle_mod
+    rng = np.random.default_rng(21)
+    nx, ny = 200, 64
+    mask = (rng.random((ny, nx)) < 0.08).astype(np.uint8)
+    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, storage, prec, 2, mask, ux=0.07, noise=1e-2, seed=3)
+    s = torch.cuda.Stream()
+    lat.set_stream(s.cuda_stream)
+    lat.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="thread_local"):
+        lat.iterate(10)
+    for _ in range(3):
+        g.replay()
+    torch.cuda.synchronize()
+    o.step(30)
+    pops, rho, _, _ = o.state()
+    np.testing.assert_array_equal(lat.populations(), pops.astype(np.float32))
+    np.testing.assert_array_equal(lat.field("rho"), rho.astype(np.float32))
+    lat.close()
