@@ -166,10 +166,9 @@ int lbm_get_storage_reference(const lbm_sim* sim, int* inlet);
  * steps, checkpoints and kernel variants give identical states.
  * Initialisation, uploads and re-expression still round to nearest.
  * LBM_ERR_ARG for stochastic rounding with f32 / f64 storage.  The setting
- * travels with checkpoints.  Steps recorded in a caller's own stream
- * capture keep the step index they were captured at, so replays of that
- * graph repeat the same random bits (and a repeated rounding is biased
- * again); lbm_step's own graphs take a fresh index on every replay. */
+ * travels with checkpoints.  The step index comes from a counter in device
+ * memory that every step call advances in stream order, so graphs replay
+ * with fresh indices: lbm_step's own and a caller's capture alike. */
 #define LBM_ROUND_NEAREST 0
 #define LBM_ROUND_STOCHASTIC 1
 int lbm_set_rounding(lbm_sim* sim, int mode, uint32_t seed);

@@ -258,11 +258,12 @@ struct lbm_batch {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};  // kGraphSteps steps from buffer parity 0 / 1
   std::string report;
   // stochastic rounding (16-bit storage): domain d uses seed sr_seed + d;
-  // captured graphs read their first step's index from clock_d
+  // the step clock: clock_d holds the index of the first step not yet
+  // counted in, a launch reads it plus its offset clock_pending, and
+  // advance_clock adds the launches made since (recorded in graphs too)
   uint32_t sr_on = 0, sr_seed = 0;
   uint32_t* clock_d = nullptr;
-  bool capturing = false;
-  uint64_t capture_steps0 = 0;
+  uint32_t clock_pending = 0;
 };
 
 namespace {
@@ -370,8 +371,8 @@ int launch_step(lbm_batch* b, bool write_moments, int* counter) {
   SrArgs sr;
   sr.on = b->sr_on;
   sr.seed = b->sr_seed;
-  sr.clock = b->capturing && b->sr_on ? b->clock_d : nullptr;
-  sr.t = sr.clock ? (uint32_t)(b->steps - b->capture_steps0) : (uint32_t)b->steps;
+  sr.clock = b->sr_on ? b->clock_d : nullptr;
+  sr.t = b->clock_pending;
   sr.y0 = 0;
   void* args[] = {&b->d_doms, &b->d_tiles, &b->ntiles, (void*)&src, (void*)&dst, &mat, &wm, &dyn, &counter, &b->d_flag,
                   &sr};
@@ -387,6 +388,27 @@ int launch_step(lbm_batch* b, bool write_moments, int* counter) {
   b->cur = dst;
   b->materialised = false;
   b->steps++;
+  if (b->sr_on) b->clock_pending++;
+  return LBM_OK;
+}
+
+// Count the step launches made since the clock last advanced into it.
+int advance_clock(lbm_batch* b) {
+  if (!b->sr_on || b->clock_pending == 0) return LBM_OK;
+  k_add_clock<<<1, 1, 0, b->stream>>>(b->clock_d, b->clock_pending);
+  BCK(cudaGetLastError());
+  b->launches++;
+  b->clock_pending = 0;
+  return LBM_OK;
+}
+
+// The clock set to the host's step count.
+int reset_clock(lbm_batch* b) {
+  if (!b->sr_on) return LBM_OK;
+  k_set_clock<<<1, 1, 0, b->stream>>>(b->clock_d, (uint32_t)b->steps);
+  BCK(cudaGetLastError());
+  b->launches++;
+  b->clock_pending = 0;
   return LBM_OK;
 }
 
@@ -408,13 +430,13 @@ int capture_graph(lbm_batch* b) {
   }
   const int cur0 = b->cur;
   const uint64_t steps0 = b->steps, launches0 = b->launches;
+  int rc = advance_clock(b);  // the graph's launches count from the clock as it stands
+  if (rc) return rc;
   cudaGraph_t g;
   BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = LBM_OK;
-  b->capturing = true;
-  b->capture_steps0 = steps0;
   for (int k = 0; k < kGraphSteps && !rc; k++) rc = launch_step(b, false, b->d_counter + 1 + k);
-  b->capturing = false;
+  if (!rc) rc = advance_clock(b);  // recorded: every replay advances the clock
+  b->clock_pending = 0;
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   b->cur = cur0;  // capture recorded the launches without running them
   b->steps = steps0;
@@ -629,7 +651,7 @@ int lbm_batch_init_equilibrium(lbm_batch* b, float noise_amp, uint64_t seed) {
   b->materialised = true;
   b->moments_valid = false;
   b->steps = 0;
-  return LBM_OK;
+  return reset_clock(b);
 }
 
 int lbm_batch_step(lbm_batch* b, uint32_t n) {
@@ -640,13 +662,9 @@ int lbm_batch_step(lbm_batch* b, uint32_t n) {
     const bool last = left == 1;
     if (!b->materialised && !last && left > (uint32_t)kGraphSteps) {
       if (!b->graph[b->cur] && (rc = capture_graph(b))) return rc;
-      if (b->sr_on) {  // the replay's first step index, read by its launches
-        k_set_clock<<<1, 1, 0, b->stream>>>(b->clock_d, (uint32_t)b->steps);
-        BCK(cudaGetLastError());
-        b->launches++;
-      }
+      if ((rc = advance_clock(b))) return rc;
       BCK(cudaGraphLaunch(b->graph[b->cur], b->stream));
-      b->launches += kGraphSteps;
+      b->launches += kGraphSteps + (b->sr_on ? 1 : 0);
       b->steps += kGraphSteps;  // kGraphSteps is even: the buffer parity is unchanged
       k += kGraphSteps;
       continue;
@@ -654,6 +672,7 @@ int lbm_batch_step(lbm_batch* b, uint32_t n) {
     if ((rc = launch_step(b, last, b->d_counter))) return rc;
     k++;
   }
+  if ((rc = advance_clock(b))) return rc;
   if (n) b->moments_valid = true;
   return LBM_OK;
 }
@@ -772,6 +791,8 @@ int lbm_batch_set_rounding(lbm_batch* b, int mode, uint32_t seed) {
     return bfail(LBM_ERR_NOMEM, "step clock word");
   b->sr_on = mode == LBM_ROUND_STOCHASTIC ? 1u : 0u;
   b->sr_seed = b->sr_on ? seed : 0u;
+  int rc = reset_clock(b);  // the clock counts on from the current step
+  if (rc) return rc;
   return configure(b);  // the kernel, its occupancy and the captured graphs change
 }
 

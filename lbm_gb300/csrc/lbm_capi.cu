@@ -95,9 +95,12 @@ struct lbm_sim {
   // with this seed, rows hashed from origin sr_y0 (lbm_set_row_origin)
   uint32_t sr_on = 0, sr_seed = 0;
   int sr_y0 = 0;
-  uint32_t* clock_d = nullptr;   // step index of a captured run's first step (set before each replay)
-  bool capturing = false;        // launches are being captured: they read the step index from clock_d
-  uint64_t capture_steps0 = 0;   // the step index the capture started at
+  // The step clock of stochastic rounding: clock_d holds the index of the
+  // first step not yet counted in; a step launch reads it plus its offset
+  // clock_pending among the launches made since, and advance_clock adds those
+  // in stream order (inside a captured graph too, so every replay advances it)
+  uint32_t* clock_d = nullptr;
+  uint32_t clock_pending = 0;
   Layout L{};
   size_t es = 4;   // bytes per stored population
   size_t cs = 4;   // bytes of the arithmetic type (moments)
@@ -281,6 +284,17 @@ int materialise(lbm_sim* s) {
   return LBM_OK;
 }
 
+// The step clock of stochastic rounding set to the host's step count (after
+// an initialisation, an upload, a checkpoint load, or switching it on).
+int reset_clock(lbm_sim* s) {
+  if (!s->sr_on) return LBM_OK;
+  k_set_clock<<<1, 1, 0, s->stream>>>(s->clock_d, (uint32_t)s->steps);
+  CK_LAUNCH();
+  s->launches++;
+  s->clock_pending = 0;
+  return LBM_OK;
+}
+
 int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64_t seed, int single,
                 long long single_cell, const float* noise_d = nullptr) {
   dim3 grid((s->L.nx + kBlockX - 1) / kBlockX, s->L.ny);
@@ -301,7 +315,7 @@ int launch_init(lbm_sim* s, double rho, double ux, double uy, double amp, uint64
   s->materialised = true;
   s->moments_valid = false;
   s->steps = 0;
-  return LBM_OK;
+  return reset_clock(s);
 }
 
 int check_sim(const lbm_sim* s, bool pending_ok) {
@@ -739,7 +753,7 @@ int lbm_set_rounding(lbm_sim* s, int mode, uint32_t seed) {
     return fail(LBM_ERR_NOMEM, "step clock word");
   s->sr_on = mode == LBM_ROUND_STOCHASTIC ? 1u : 0u;
   s->sr_seed = s->sr_on ? seed : 0u;
-  return LBM_OK;
+  return reset_clock(s);  // the clock counts on from the current step
 }
 
 int lbm_get_rounding(const lbm_sim* s, int* mode, uint32_t* seed) {
@@ -849,8 +863,8 @@ static int launch_rows(lbm_sim* s, bool last, int row0, int row_end, int dst) {
     a.sr.on = s->sr_on;
     a.sr.seed = s->sr_seed;
     a.sr.y0 = s->sr_y0;
-    a.sr.clock = s->capturing && s->sr_on ? s->clock_d : nullptr;
-    a.sr.t = a.sr.clock ? (uint32_t)(s->steps - s->capture_steps0) : (uint32_t)s->steps;
+    a.sr.clock = s->sr_on ? s->clock_d : nullptr;
+    a.sr.t = s->clock_pending;
     if (variant >= 2) {
       return s->edge == EDGE_REF ? launch_staged_ns<St, EDGE_REF>(s, a) : launch_staged_ns<St, EDGE_CHANNEL>(s, a);
     } else if (variant == 1) {
@@ -877,6 +891,7 @@ static int launch_step(lbm_sim* s, bool last) {
   s->cur = dst;
   s->materialised = false;
   s->steps++;
+  if (s->sr_on) s->clock_pending++;
   return LBM_OK;
 }
 
@@ -899,13 +914,13 @@ static StepGraphKey graph_key(const lbm_sim* s) {
   return k;
 }
 
-// Before a captured run replays: its launches read their step index as the
-// run's first step (this word) plus their offset in the run.
-static int set_clock(lbm_sim* s) {
-  if (!s->sr_on) return LBM_OK;
-  k_set_clock<<<1, 1, 0, s->stream>>>(s->clock_d, (uint32_t)s->steps);
+// Count the step launches made since the clock last advanced into it.
+static int advance_clock(lbm_sim* s) {
+  if (!s->sr_on || s->clock_pending == 0) return LBM_OK;
+  k_add_clock<<<1, 1, 0, s->stream>>>(s->clock_d, s->clock_pending);
   CK_LAUNCH();
   s->launches++;
+  s->clock_pending = 0;
   return LBM_OK;
 }
 
@@ -927,13 +942,13 @@ static int capture_steps(lbm_sim* s, cudaGraphExec_t& out, uint32_t n, bool mome
   }
   const int cur0 = s->cur;
   const uint64_t steps0 = s->steps, launches0 = s->launches;
+  int rc = advance_clock(s);  // the run's launches count from the clock as it stands
+  if (rc) return rc;
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-  int rc = LBM_OK;
-  s->capturing = true;
-  s->capture_steps0 = steps0;
   for (uint32_t k = 0; k < n && !rc; k++) rc = launch_step(s, moments && k + 1 == n);
-  s->capturing = false;
+  if (!rc) rc = advance_clock(s);  // recorded: every replay advances the clock by n
+  s->clock_pending = 0;
   const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
   s->cur = cur0;  // the capture recorded the launches without running them
   s->steps = steps0;
@@ -969,11 +984,11 @@ int lbm_step(lbm_sim* s, uint32_t n) {
       s->run_key[c] = graph_key(s);
       s->run_n[c] = n;
     }
-    int rc = set_clock(s);
+    int rc = advance_clock(s);
     if (rc) return rc;
     CK(cudaGraphLaunch(s->run_graph[c], s->stream));
     s->steps += n;
-    s->launches += n;
+    s->launches += n + (s->sr_on ? 1 : 0);
     s->cur = c ^ (int)(n & 1u);
     s->moments_valid = true;
     return LBM_OK;
@@ -986,11 +1001,11 @@ int lbm_step(lbm_sim* s, uint32_t n) {
         if (rc) return rc;
         s->graph_key[s->cur] = graph_key(s);
       }
-      int rc = set_clock(s);
+      int rc = advance_clock(s);
       if (rc) return rc;
       CK(cudaGraphLaunch(s->graph[s->cur], s->stream));
       s->steps += kStepGraph;  // even: the buffer parity is unchanged
-      s->launches += kStepGraph;
+      s->launches += kStepGraph + (s->sr_on ? 1 : 0);
       k += kStepGraph;
       continue;
     }
@@ -998,6 +1013,8 @@ int lbm_step(lbm_sim* s, uint32_t n) {
     if (rc) return rc;
     k++;
   }
+  int rc = advance_clock(s);
+  if (rc) return rc;
   s->moments_valid = true;
   return LBM_OK;
 }
@@ -1020,6 +1037,8 @@ int lbm_step_rows(lbm_sim* s, uint32_t y0, uint32_t y1, int flags) {
     s->materialised = false;
     s->steps++;
     s->moments_valid = s->pending_moments;
+    if (s->sr_on) s->clock_pending++;  // every row range of the step read the same index
+    return advance_clock(s);
   }
   return LBM_OK;
 }
@@ -1159,7 +1178,7 @@ static int write_pops(lbm_sim* s, const void* in, bool f64) {
   s->materialised = true;
   s->moments_valid = false;
   s->steps = 0;
-  return LBM_OK;
+  return reset_clock(s);
 }
 
 int lbm_write_populations(lbm_sim* s, const float* in) { return write_pops(s, in, false); }
@@ -1642,7 +1661,7 @@ int lbm_checkpoint_load(lbm_sim* s, const void* buf, size_t len) {
   s->cur = (int)h.cur;
   s->materialised = h.materialised != 0;
   s->moments_valid = false;
-  return LBM_OK;
+  return reset_clock(s);
 }
 
 int lbm_checkpoint_write(lbm_sim* s, const char* path) {

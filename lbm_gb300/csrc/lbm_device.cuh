@@ -69,8 +69,8 @@ struct StoreRef {
 struct SrArgs {
   uint32_t on;            // 1: stochastic rounding (16-bit storage only)
   uint32_t seed;
-  uint32_t t;             // the step index, or its offset from *clock
-  const uint32_t* clock;  // step index of a captured run's first step, or null
+  uint32_t t;             // the step's offset from *clock (or its index when clock is null)
+  const uint32_t* clock;  // the step clock: index of the first step not yet counted in
   int y0;                 // row origin: row y hashes as y + y0
 };
 __host__ __device__ constexpr uint32_t fmix32(uint32_t h) {
@@ -91,8 +91,8 @@ __host__ __device__ constexpr uint32_t sr_mul(int q) {
   return (uint32_t)(z >> 32) | 1u;
 }
 __device__ __forceinline__ uint32_t sr_step_key(const SrArgs& s) {
-  // the clock word changes between replays of the same graph: read it at L2
-  // (ld.global.cg), never from a line an earlier replay left in L1
+  // the clock word changes between launches of the same graph: read it at
+  // L2 (ld.global.cg), never from a line an earlier launch left in L1
   const uint32_t t = s.clock ? __ldcg(s.clock) + s.t : s.t;
   return fmix32(s.seed ^ (t * 0x9E3779B1u));
 }

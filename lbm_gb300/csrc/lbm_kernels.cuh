@@ -500,8 +500,9 @@ __global__ void k_read_pops(Layout L, const typename St::S* f, const typename St
 
 // Bit-packs a dense nx-wide byte mask (nonzero = solid) into the pitched mask
 // words: one thread per word, bits past column nx-1 cleared.
-// The step index a captured run of steps starts at (stochastic rounding).
+// The step clock of stochastic rounding: set it, or count launched steps in.
 static __global__ void k_set_clock(uint32_t* clock, uint32_t t) { *clock = t; }
+static __global__ void k_add_clock(uint32_t* clock, uint32_t n) { *clock += n; }
 
 static __global__ void k_pack_mask(Layout L, const uint8_t* __restrict__ bytes, uint32_t* __restrict__ words) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;

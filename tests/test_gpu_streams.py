@@ -76,18 +76,21 @@ def test_gpu_rebase_queued_before_a_stream_switch_comes_first(lbm, cuda_ok, stor
     lat.close()
 
 
-@pytest.mark.parametrize("storage,prec", [(0, 0), (1, 1)])
-def test_gpu_steps_in_a_callers_own_capture(lbm, cuda_ok, oracle_mod, storage, prec):
+@pytest.mark.parametrize("storage,prec,sr", [(0, 0, False), (1, 1, False), (1, 1, True), (2, 2, True)])
+def test_gpu_steps_in_a_callers_own_capture(lbm, cuda_ok, oracle_mod, storage, prec, sr):
     """lbm_step inside the caller's stream capture records plain launches;
     replaying the caller's graph three times advances the state by three
-    times the recorded (even) steps, bit for bit with the oracle."""
+    times the recorded (even) steps, bit for bit with the oracle.  With
+    stochastic rounding each replay reads fresh step indices from the
+    device step clock, which the recorded graph advances itself."""
     import torch
     from test_gpu_parity import run_pair
     P = oracle_mod
     rng = np.random.default_rng(21)
     nx, ny = 200, 64
     mask = (rng.random((ny, nx)) < 0.08).astype(np.uint8)
-    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, storage, prec, 2, mask, ux=0.07, noise=1e-2, seed=3)
+    lat, o = run_pair(lbm, P, nx, ny, 1.0 / 0.6, 1, storage, prec, 2, mask, ux=0.07, noise=1e-2, seed=3,
+                      sr_seed=44 if sr else None)
     s = torch.cuda.Stream()
     lat.set_stream(s.cuda_stream)
     lat.synchronize()
