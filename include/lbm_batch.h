@@ -76,7 +76,7 @@ int lbm_batch_set_rounding(lbm_batch* batch, int mode, uint32_t seed);
 int lbm_batch_get_rounding(const lbm_batch* batch, int* mode, uint32_t* seed);
 
 /* Fix the schedule by hand: variant 0..5 = (ring stages, cells per thread,
- * strip columns) (4,1,256) (6,1,256) (5,2,256) (8,2,256) (6,2,512)
+ * strip columns) (5,1,256) (6,1,256) (5,2,256) (8,2,256) (6,2,512)
  * (4,2,512), the 512-column strips for f16 / bf16 only (f32 runs variants 4
  * and 5 with 256-column strips); dynamic 0 = tiles sorted longest first and dealt
  * round-robin to the persistent CTAs, 1 = CTAs take tiles from an atomic

@@ -229,7 +229,7 @@ struct Config {
 // (ring depth, cells per thread)
 // (ring stages, cells per thread, strip columns); the 512-column strips exist
 // for 16-bit storage only (f32 runs them as 256-column strips)
-constexpr int kVariants[6][3] = {{4, 1, 256}, {6, 1, 256}, {5, 2, 256}, {8, 2, 256}, {6, 2, 512}, {4, 2, 512}};
+constexpr int kVariants[6][3] = {{5, 1, 256}, {6, 1, 256}, {5, 2, 256}, {8, 2, 256}, {6, 2, 512}, {4, 2, 512}};
 constexpr int kNumVariants = 6;
 int strip_of(int variant, int storage) { return storage == STORE_F32 ? kStageW : kVariants[variant][2]; }
 
@@ -287,7 +287,7 @@ template <class St, int NS, int CPT, int W> void* kernel_ptr(bool sr) {
 template <class St> void* variant_kernel(int v, bool sr) {
   constexpr bool k16 = sizeof(typename St::S) == 2;
   switch (v) {
-    case 0: return kernel_ptr<St, 4, 1, kStageW>(sr);
+    case 0: return kernel_ptr<St, 5, 1, kStageW>(sr);
     case 1: return kernel_ptr<St, 6, 1, kStageW>(sr);
     case 2: return kernel_ptr<St, 5, 2, kStageW>(sr);
     case 3: return kernel_ptr<St, 8, 2, kStageW>(sr);
